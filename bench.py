@@ -1,0 +1,325 @@
+"""Benchmark: correlations/s at <= 1e-5 relative error vs FP64.
+
+Workload (one GPU): one_to_many, FP32, one left 256x256 and 64 right 256x256
+matrices, values i.i.d. uniform [0,1) from a fixed seed; 64 full outputs of
+511x511.  Synthetic data with the configuration's shapes and distribution.
+
+A step is one batched correlation of the whole workload.  `value` counts the
+correlations (output matrices) completed per second with inputs already in
+HBM, timed with CUDA events on the launching stream; L2 is flushed (a 256 MiB
+write) before every timed step, outside the timed region.  `e2e` is the same
+metric through the C ABI's host-buffer entry point (xc_correlate_host) with
+pinned host buffers: host->device copy, correlation and device->host copy all
+inside the timed region.  Every reported output is checked against an FP64
+reference before the number is printed (all 64 outputs against an FP64 FFT
+on the GPU, two of them also against the CPU oracle).
+
+`--impl reference` times the reference's CPU algorithm (cpu_cross_corr_*,
+restated in C as oracle/xcorr_oracle.c because the reference's own CPU code
+needs Boost) on the host cores, on a bounded sample of pairs per step.
+
+Launch: python bench.py [--gpus N --steps K --warmup W]; for N>1 under
+torchrun each rank runs the same per-GPU workload (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cross-corr_gb300")
+for p in (ROOT, PKG):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+WORKLOAD = {"workload": "one_to_many fp32 256x256 x 64 right", "mode": "one_to_many", "left": [1, 256, 256],
+            "right": [64, 256, 256], "distribution": "uniform[0,1)", "seed": 2}
+METRIC = "correlations/s at <=1e-5 rel err vs FP64"
+GATE = 1e-5
+
+
+def make_inputs():
+    rng = np.random.default_rng(WORKLOAD["seed"])
+    left = rng.random(WORKLOAD["left"]).astype(np.float32)
+    right = rng.random(WORKLOAD["right"]).astype(np.float32)
+    return left, right
+
+
+def algorithmic_flops(left_shape, right_shape, pairs):
+    return 2.0 * left_shape[-2] * left_shape[-1] * right_shape[-2] * right_shape[-1] * pairs
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "sm_max_mhz": 2070.0}, \
+            "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._thr = None
+
+    def _loop(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.rows.append([c.strip() for c in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._thr = threading.Thread(target=self._loop, daemon=True)
+        self._thr.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._thr:
+            self._thr.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def cpu_reference_rate(left, right, pairs: int, threads: int):
+    """Reference CPU algorithm (T=float, oracle/xcorr_oracle.c restatement of
+    cpu_cross_corr_one_to_many) on `pairs` right matrices; returns pairs/s."""
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    oracle.run_mode("one_to_many", left, right[:pairs], dtype="f32", threads=threads)
+    dt = time.perf_counter() - t0
+    return pairs / dt, dt
+
+
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    left, right = make_inputs()
+    threads = os.cpu_count() or 1
+    sample = 16  # pairs per step: ~6.9e10 MACs, several seconds on 16 cores
+    for _ in range(args.warmup):
+        cpu_reference_rate(left, right, 1, threads)
+    t_total, pairs_total = 0.0, 0
+    for _ in range(args.steps):
+        _, dt = cpu_reference_rate(left, right, sample, threads)
+        t_total += dt
+        pairs_total += sample
+    value = pairs_total / t_total
+    line = {
+        "metric": METRIC, "value": value, "unit": "correlations/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * t_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": dict(WORKLOAD, parallelism="host threads"),
+        "cpu_baseline": {"value": value, "unit": "correlations/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} of 64 pairs per step (cpu_cross_corr_one_to_many restated in C, "
+                                   f"T=float, {threads} threads)"},
+        "e2e": {"value": value, "unit": "correlations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def accuracy_gate(out_dev, left, right, torch, xcorr):
+    """All outputs vs an FP64 FFT on the GPU; two outputs vs the CPU oracle."""
+    from oracle import oracle
+
+    l64 = torch.from_numpy(left).double().cuda()
+    r64 = torch.from_numpy(right).double().cuda()
+    ref = xcorr.correlate("one_to_many", l64, r64, method="fft")
+    torch.cuda.synchronize()
+    o = out_dev.double()
+    err = ((o - ref).abs().amax(dim=(1, 2)) / ref.abs().amax(dim=(1, 2))).max().item()
+    o_cpu = out_dev[:2].cpu().numpy()
+    ref_cpu = oracle.run_mode("one_to_many", left, right[:2], dtype="f32acc64", threads=os.cpu_count() or 1)
+    err_oracle = max(oracle.max_rel_to_max(o_cpu[k], ref_cpu[k]) for k in range(2))
+    del l64, r64, ref
+    return max(err, err_oracle), err, err_oracle
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+
+    import xcorr
+
+    torch.cuda.set_device(local_rank)
+    xcorr.check(xcorr.lib().xc_device_check(local_rank))
+    left, right = make_inputs()
+    pairs = right.shape[0]
+    dl = torch.from_numpy(left).cuda()
+    dr = torch.from_numpy(right).cuda()
+    method = args.method
+    out = torch.empty((pairs, 511, 511), device="cuda", dtype=torch.float32)
+    ws_bytes = xcorr.workspace_size("one_to_many", "f32", method, (256, 256), 1, (256, 256), pairs)
+    ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def step():
+        xcorr.correlate("one_to_many", dl, dr, method=method, out=out, workspace=ws if ws_bytes else None)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    gate, gate_fft, gate_oracle = accuracy_gate(out, left, right, torch, xcorr)
+    if gate > GATE:
+        raise SystemExit(f"accuracy gate failed: {gate:.3e} > {GATE}")
+
+    # ---- device-resident timing: per-step CUDA events, L2 flushed between steps
+    times = []
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = sum(times) / len(times)
+    ms_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = t.item()
+    value = pairs * world / (ms_max / 1000.0)
+
+    # ---- end to end through the C ABI host-buffer call (pinned host memory)
+    hl = torch.from_numpy(left).pin_memory()
+    hr = torch.from_numpy(right).pin_memory()
+    ho = torch.empty((pairs, 511, 511), dtype=torch.float32).pin_memory()
+    L = xcorr.lib()
+
+    def e2e_step():
+        xcorr.check(L.xc_correlate_host(xcorr.MODES["one_to_many"], 0, xcorr.METHODS[method], hl.data_ptr(),
+                                        xcorr.size2(256, 256), 1, hr.data_ptr(), xcorr.size2(256, 256), pairs,
+                                        ho.data_ptr(), stream.cuda_stream))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()  # synchronises the stream before returning
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = t.item()
+    e2e_err = float(np.abs(ho.numpy()[:2].astype(np.float64) - out[:2].cpu().numpy()).max())
+
+    peaks, peak_src = measured_peaks()
+    flops = algorithmic_flops(left.shape, right.shape, pairs)
+    achieved = flops / (ms / 1000.0) / 1e12
+    if method == "tc_bf16x3":
+        bound, peak, unit = "tensor", float(peaks.get("bf16_tflops", 1900.0)), "TFLOP/s"
+        peak_note = f"{peak_src} cuBLAS bf16 burst; algorithmic FP32 flops (3 bf16 products each)"
+    else:
+        mhz = float(peaks.get("sm_max_mhz", 2070.0))
+        bound, peak, unit = "fp32", 152 * 128 * 2 * mhz * 1e6 / 1e12, "TFLOP/s"
+        peak_note = "nominal FP32 FMA peak (152 SMs x 128 lanes x 2 x max SM clock); no measured SIMT peak exists"
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "correlations/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(WORKLOAD, method=method, l2="flushed (256 MiB write) before every timed step",
+                       parallelism=f"replica per GPU x{world}"),
+        "accuracy": {"max_rel_err_vs_fp64": gate, "vs_gpu_fp64_fft_all_outputs": gate_fft,
+                     "vs_cpu_oracle_2_outputs": gate_oracle, "gate": GATE},
+        "e2e": {"value": pairs * world / e2e_s, "unit": "correlations/s",
+                "h2d_bytes_per_step": int(left.nbytes + right.nbytes), "d2h_bytes_per_step": int(ho.numel() * 4),
+                "api": "xc_correlate_host (pinned host buffers)", "max_abs_diff_vs_device_run": e2e_err},
+        "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                     "traffic": None, "kernel": "direct_kernel" if method != "tc_bf16x3" else "tc_kernel",
+                     "algorithmic_flops_per_launch": flops, "peak_source": peak_note},
+        "clocks": clocks,
+        "gpu_launches": gpu_launches(method, args.steps),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, dt = cpu_reference_rate(left, right, 16, os.cpu_count() or 1)
+        line["cpu_baseline"] = {"value": rate, "unit": "correlations/s", "cores": os.cpu_count() or 1,
+                                "kind": "port", "sample": f"16 of 64 pairs ({dt:.1f} s), cpu_cross_corr_one_to_many "
+                                                          "restated in C, T=float"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def gpu_launches(method, steps):
+    per_step = {"direct": 1, "fft": 6, "tc_bf16x3": 2}.get(method, 1)
+    return per_step * steps
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default="direct", choices=["direct", "fft", "tc_bf16x3"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

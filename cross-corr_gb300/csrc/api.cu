@@ -1,0 +1,455 @@
+// api.cu -- the C ABI (include/xcorr.h): argument checks, method dispatch,
+// per-thread caches of FFT plans and device buffers, and the drop-in
+// launchers for the reference's run_* kernel-launch layer (src/kernels.cuh).
+#include <cufft.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+
+#include "xc_common.cuh"
+#include "xc_internal.h"
+
+namespace xc {
+const char* last_error_cstr();
+xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
+                       void* workspace, size_t ws_bytes, cudaStream_t stream);
+size_t tc_workspace_size(const Geometry& g, const PairMap& pm);
+}  // namespace xc
+
+using namespace xc;
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+xc_status check_sizes(xc_size2 left, xc_size2 right) {
+  if (left.x == 0 || left.y == 0 || right.x == 0 || right.y == 0)
+    return fail(XC_ERR_INVALID_ARGUMENT, "matrix sizes must be positive");
+  if ((uint64_t)left.x + right.x - 1 > 0x7fffffffu || (uint64_t)left.y + right.y - 1 > 0x7fffffffu)
+    return fail(XC_ERR_INVALID_ARGUMENT, "matrix sizes too large");
+  return XC_OK;
+}
+
+size_t elem_size(xc_dtype d) { return d == XC_F32 ? sizeof(float) : sizeof(double); }
+
+// Per-thread cache of FFT plans, keyed by the full problem description.
+using PlanKey = std::tuple<int, int, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, int>;
+struct PlanDeleter {
+  void operator()(FftPlanImpl* p) const { fft_plan_destroy(p); }
+};
+
+struct ThreadCache {
+  std::map<PlanKey, std::unique_ptr<FftPlanImpl, PlanDeleter>> plans;
+  // xc_correlate_host buffers (grow-only).
+  void* d_left = nullptr;
+  void* d_right = nullptr;
+  void* d_out = nullptr;
+  void* d_ws = nullptr;
+  size_t left_bytes = 0, right_bytes = 0, out_bytes = 0, ws_bytes = 0;
+  int device = -1;
+
+  void release() {
+    plans.clear();
+    cudaFree(d_left);
+    cudaFree(d_right);
+    cudaFree(d_out);
+    cudaFree(d_ws);
+    d_left = d_right = d_out = d_ws = nullptr;
+    left_bytes = right_bytes = out_bytes = ws_bytes = 0;
+  }
+  ~ThreadCache() {
+    // Process teardown may already have destroyed the CUDA context; only the
+    // host side is released here.
+    for (auto& kv : plans) kv.second.release();
+  }
+};
+
+ThreadCache& cache() {
+  static thread_local ThreadCache c;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (c.device != dev) {
+    if (c.device >= 0) {
+      int cur = dev;
+      cudaSetDevice(c.device);
+      c.release();
+      cudaSetDevice(cur);
+    }
+    c.device = dev;
+  }
+  return c;
+}
+
+xc_status cached_plan(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                      uint32_t n_right, FftPlanImpl** plan) {
+  ThreadCache& c = cache();
+  PlanKey key{(int)mode, (int)dtype, left.x, left.y, n_left, right.x, right.y, n_right, 0};
+  auto it = c.plans.find(key);
+  if (it != c.plans.end()) {
+    *plan = it->second.get();
+    return XC_OK;
+  }
+  FftPlanImpl* p = nullptr;
+  XC_TRY(fft_plan_create(&p, mode, dtype, left, n_left, right, n_right, xc_size2{0, 0}));
+  c.plans.emplace(key, std::unique_ptr<FftPlanImpl, PlanDeleter>(p));
+  *plan = p;
+  return XC_OK;
+}
+
+size_t fft_workspace_bytes(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                           uint32_t n_right) {
+  PairMap pm;
+  uint64_t n_out = 0;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out)) return 0;
+  long long py, px;
+  if (left.x == right.x && left.y == right.y) {
+    py = 2LL * left.y;
+    px = 2LL * left.x;
+  } else {
+    // upper bound: the smooth size found at plan time is at most 2x the full size
+    py = 2LL * (left.y + right.y);
+    px = 2LL * (left.x + right.x);
+  }
+  const long long bins = py * (px / 2 + 1);
+  const size_t ce = 2 * elem_size(dtype);
+  return (size_t)(n_left + n_right) * bins * ce + (size_t)n_out * bins * ce + 256;
+}
+
+xc_method resolve(xc_method m, xc_dtype dtype) {
+  (void)dtype;
+  if (m == XC_METHOD_AUTO) return XC_METHOD_DIRECT;
+  return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* xc_version(void) { return "xcorr-gb300 0.1.0 (sm_103a)"; }
+
+const char* xc_status_string(xc_status s) {
+  switch (s) {
+    case XC_OK: return "ok";
+    case XC_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case XC_ERR_CUDA: return "CUDA error";
+    case XC_ERR_CUFFT: return "cuFFT error";
+    case XC_ERR_UNSUPPORTED: return "unsupported";
+    case XC_ERR_WORKSPACE: return "workspace too small";
+    case XC_ERR_TIMEOUT: return "device wait timed out";
+  }
+  return "unknown status";
+}
+
+const char* xc_last_error(void) { return last_error_cstr(); }
+
+xc_status xc_device_check(int device) {
+  cudaDeviceProp prop;
+  XC_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(XC_ERR_UNSUPPORTED, std::string("device ") + prop.name + " is sm_" + std::to_string(prop.major) +
+                                        std::to_string(prop.minor) + "; this library is built for sm_103a");
+  return XC_OK;
+}
+
+xc_status xc_output_count(xc_mode mode, uint32_t n_left, uint32_t n_right, uint64_t* n_out) {
+  PairMap pm;
+  if (n_out == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "n_out is NULL");
+  if (!make_pair_map(mode, n_left, n_right, &pm, n_out))
+    return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts " + std::to_string(n_left) + " x " +
+                                             std::to_string(n_right) + " for mode " + std::to_string((int)mode));
+  return XC_OK;
+}
+
+xc_status xc_output_size(xc_size2 left, xc_size2 right, xc_size2* out) {
+  if (out == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "out is NULL");
+  XC_TRY(check_sizes(left, right));
+  out->x = left.x + right.x - 1;
+  out->y = left.y + right.y - 1;
+  return XC_OK;
+}
+
+xc_status xc_workspace_size(xc_mode mode, xc_dtype dtype, xc_method method, xc_size2 left, uint32_t n_left,
+                            xc_size2 right, uint32_t n_right, size_t* bytes) {
+  if (bytes == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "bytes is NULL");
+  XC_TRY(check_sizes(left, right));
+  PairMap pm;
+  uint64_t n_out;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out)) return fail(XC_ERR_INVALID_ARGUMENT, "invalid counts");
+  method = resolve(method, dtype);
+  switch (method) {
+    case XC_METHOD_DIRECT: *bytes = 0; return XC_OK;
+    case XC_METHOD_FFT: *bytes = fft_workspace_bytes(mode, dtype, left, n_left, right, n_right); return XC_OK;
+    case XC_METHOD_TC_BF16X3:
+      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split-BF16 tensor path is FP32 only");
+      *bytes = tc_workspace_size(make_geometry(left, right), pm);
+      return XC_OK;
+    default: return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
+  }
+}
+
+xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const void* d_left, xc_size2 left,
+                       uint32_t n_left, const void* d_right, xc_size2 right, uint32_t n_right, void* d_out,
+                       void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (d_left == nullptr || d_right == nullptr || d_out == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL device buffer");
+  if (dtype != XC_F32 && dtype != XC_F64) return fail(XC_ERR_INVALID_ARGUMENT, "unknown dtype");
+  XC_TRY(check_sizes(left, right));
+  PairMap pm;
+  uint64_t n_out;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out))
+    return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts for the mode");
+  const Geometry g = make_geometry(left, right);
+  method = resolve(method, dtype);
+  switch (method) {
+    case XC_METHOD_DIRECT: return direct_launch(dtype, d_left, d_right, d_out, g, pm, as_stream(stream), -1);
+    case XC_METHOD_FFT: {
+      FftPlanImpl* plan = nullptr;
+      XC_TRY(cached_plan(mode, dtype, left, n_left, right, n_right, &plan));
+      return fft_plan_execute(plan, d_left, d_right, d_out, 1, d_workspace, workspace_bytes, as_stream(stream));
+    }
+    case XC_METHOD_TC_BF16X3:
+      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split-BF16 tensor path is FP32 only");
+      return tc_correlate((const float*)d_left, (const float*)d_right, (float*)d_out, g, pm, d_workspace,
+                          workspace_bytes, as_stream(stream));
+    default: return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
+  }
+}
+
+xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
+                            uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
+                            void* stream) {
+  if (h_left == nullptr || h_right == nullptr || h_out == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL host buffer");
+  XC_TRY(check_sizes(left, right));
+  uint64_t n_out;
+  XC_TRY(xc_output_count(mode, n_left, n_right, &n_out));
+  const size_t es = elem_size(dtype);
+  const size_t lb = (size_t)left.x * left.y * n_left * es;
+  const size_t rb = (size_t)right.x * right.y * n_right * es;
+  const size_t ob = (size_t)(left.x + right.x - 1) * (left.y + right.y - 1) * n_out * es;
+  size_t wb = 0;
+  XC_TRY(xc_workspace_size(mode, dtype, method, left, n_left, right, n_right, &wb));
+  ThreadCache& c = cache();
+  auto grow = [](void** p, size_t* have, size_t need) -> xc_status {
+    if (need <= *have) return XC_OK;
+    cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+    XC_CUDA_TRY(cudaMalloc(p, need));
+    *have = need;
+    return XC_OK;
+  };
+  XC_TRY(grow(&c.d_left, &c.left_bytes, lb));
+  XC_TRY(grow(&c.d_right, &c.right_bytes, rb));
+  XC_TRY(grow(&c.d_out, &c.out_bytes, ob));
+  if (wb > 0) XC_TRY(grow(&c.d_ws, &c.ws_bytes, wb));
+  cudaStream_t s = as_stream(stream);
+  XC_CUDA_TRY(cudaMemcpyAsync(c.d_left, h_left, lb, cudaMemcpyHostToDevice, s));
+  XC_CUDA_TRY(cudaMemcpyAsync(c.d_right, h_right, rb, cudaMemcpyHostToDevice, s));
+  XC_TRY(xc_correlate(mode, dtype, method, c.d_left, left, n_left, c.d_right, right, n_right, c.d_out, c.d_ws,
+                      c.ws_bytes, stream));
+  XC_CUDA_TRY(cudaMemcpyAsync(h_out, c.d_out, ob, cudaMemcpyDeviceToHost, s));
+  XC_CUDA_TRY(cudaStreamSynchronize(s));
+  return check_device_flags(s);
+}
+
+void xc_release_thread_cache(void) { cache().release(); }
+
+// ---------------------------------------------------------------------------
+// Explicit FFT plans
+// ---------------------------------------------------------------------------
+struct xc_fft_plan_s {
+  FftPlanImpl* impl;
+};
+
+xc_status xc_fft_plan_create(xc_fft_plan* plan, xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left,
+                             xc_size2 right, uint32_t n_right, xc_size2 pad) {
+  if (plan == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "plan is NULL");
+  *plan = nullptr;
+  XC_TRY(check_sizes(left, right));
+  FftPlanImpl* impl = nullptr;
+  XC_TRY(fft_plan_create(&impl, mode, dtype, left, n_left, right, n_right, pad));
+  *plan = new xc_fft_plan_s{impl};
+  return XC_OK;
+}
+
+xc_status xc_fft_plan_workspace_size(xc_fft_plan plan, size_t* bytes) {
+  if (plan == nullptr || bytes == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  *bytes = fft_plan_workspace(plan->impl);
+  return XC_OK;
+}
+
+xc_status xc_fft_plan_pad_size(xc_fft_plan plan, xc_size2* pad) {
+  if (plan == nullptr || pad == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  *pad = fft_plan_pad(plan->impl);
+  return XC_OK;
+}
+
+xc_status xc_fft_execute(xc_fft_plan plan, const void* d_left, const void* d_right, void* d_out, int normalize,
+                         void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (plan == nullptr || d_left == nullptr || d_right == nullptr || d_out == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  return fft_plan_execute(plan->impl, d_left, d_right, d_out, normalize, d_workspace, workspace_bytes,
+                          as_stream(stream));
+}
+
+xc_status xc_fft_forward(xc_fft_plan plan, const void* d_left, const void* d_right, void* d_workspace,
+                         size_t workspace_bytes, void* stream) {
+  if (plan == nullptr || d_left == nullptr || d_right == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  return fft_plan_forward(plan->impl, d_left, d_right, d_workspace, workspace_bytes, as_stream(stream));
+}
+
+xc_status xc_fft_multiply(xc_fft_plan plan, void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (plan == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL plan");
+  return fft_plan_multiply(plan->impl, d_workspace, workspace_bytes, as_stream(stream));
+}
+
+xc_status xc_fft_inverse(xc_fft_plan plan, void* d_out, int normalize, void* d_workspace, size_t workspace_bytes,
+                         void* stream) {
+  if (plan == nullptr || d_out == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  return fft_plan_inverse(plan->impl, d_out, normalize, d_workspace, workspace_bytes, as_stream(stream));
+}
+
+xc_status xc_fft_plan_destroy(xc_fft_plan plan) {
+  if (plan == nullptr) return XC_OK;
+  fft_plan_destroy(plan->impl);
+  delete plan;
+  return XC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Drop-ins for the reference's run_* launchers (src/kernels.cuh).
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+xc_status check_search(xc_size2 matrix_size, xc_size2 search_size) {
+  if (search_size.x != 2 * matrix_size.x - 1 || search_size.y != 2 * matrix_size.y - 1)
+    return fail(XC_ERR_INVALID_ARGUMENT, "search_size must be 2*matrix_size-1 for equal-size inputs");
+  return check_sizes(matrix_size, matrix_size);
+}
+
+xc_status check_warps(uint32_t warps) {
+  // src/naive_shuffle.cu:461-463
+  if (warps == 0 || warps > 32)
+    return fail(XC_ERR_INVALID_ARGUMENT, "Too many warps per thread block: " + std::to_string(warps) + " (max 32)");
+  return XC_OK;
+}
+
+xc_status check_limit(uint32_t v, uint32_t lo, uint32_t hi, const char* what) {
+  if (v < lo || v > hi)
+    return fail(XC_ERR_INVALID_ARGUMENT, std::string("Invalid ") + what + ": " + std::to_string(v) + " [" +
+                                             std::to_string(lo) + "-" + std::to_string(hi) + "]");
+  return XC_OK;
+}
+
+template <typename T>
+xc_status run_mode(xc_mode mode, const T* left, const T* right, T* out, xc_size2 ms, uint32_t nl, uint32_t nr,
+                   void* stream) {
+  PairMap pm;
+  uint64_t n_out;
+  if (!make_pair_map(mode, nl, nr, &pm, &n_out)) return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts");
+  if (left == nullptr || right == nullptr || out == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");
+  return direct_launch(sizeof(T) == 4 ? XC_F32 : XC_F64, left, right, out, make_geometry(ms, ms), pm,
+                       as_stream(stream), -1);
+}
+
+}  // namespace
+
+extern "C" {
+
+#define XC_DEFINE_SHUFFLE(SUFFIX, T)                                                                             \
+  xc_status xc_run_ccn_shuffle_##SUFFIX(const T* left, const T* right, T* out, xc_size2 matrix_size,             \
+                                        xc_size2 search_size, uint32_t warps_per_thread_block, void* stream) {   \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_ONE, left, right, out, matrix_size, 1, 1, stream);                              \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_multimat_right_##SUFFIX(                                                          \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t right_matrices_per_thread,           \
+      void* stream) {                                                                                            \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(right_matrices_per_thread, 1, 8, "number of right matrices per thread"));                \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_MANY, left, right, out, matrix_size, 1, num_right_matrices, stream);            \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_##SUFFIX(                                \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t shifts_per_thread_right_matrix,      \
+      uint32_t right_matrices_per_thread, uint32_t left_rows_per_iteration, void* stream) {                      \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(shifts_per_thread_right_matrix, 0, 4, "shifts per thread in each right matrix"));         \
+    XC_TRY(check_limit(right_matrices_per_thread, 1, 4, "number of right matrices per thread"));                \
+    XC_TRY(check_limit(left_rows_per_iteration, 0, 4, "left rows per iteration"));                               \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_MANY, left, right, out, matrix_size, 1, num_right_matrices, stream);            \
+  }                                                                                                              \
+  xc_status xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_##SUFFIX(                                      \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,                  \
+      uint32_t shifts_per_thread_right_matrix, uint32_t left_matrices_per_thread,                                \
+      uint32_t right_matrices_per_thread, uint32_t left_rows_per_iteration, void* stream) {                      \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(shifts_per_thread_right_matrix, 0, 4, "shifts per thread per right matrix"));             \
+    XC_TRY(check_limit(left_matrices_per_thread, 1, 4, "left matrices per thread"));                             \
+    XC_TRY(check_limit(right_matrices_per_thread, 1, 4, "right matrices per thread"));                           \
+    XC_TRY(check_limit(left_rows_per_iteration, 0, 4, "left rows per iteration"));                              \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_N_TO_M, left, right, out, matrix_size, num_left_matrices, num_right_matrices, stream);  \
+  }
+
+XC_DEFINE_SHUFFLE(f32, float)
+XC_DEFINE_SHUFFLE(f64, double)
+
+#define XC_DEFINE_FFT_GLUE(CSUF, RSUF, DT, T)                                                                     \
+  xc_status xc_run_hadamard_original_##CSUF(const void* ref, void* deformed, xc_size2 subregion_size,            \
+                                            uint32_t subregions_per_pic, uint32_t batch_size,                    \
+                                            uint32_t threads_per_block, void* stream) {                          \
+    if (ref == nullptr || deformed == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");             \
+    const long long area = (long long)subregion_size.x * subregion_size.y * subregions_per_pic;                  \
+    return glue_hadamard_original(DT, ref, deformed, area, batch_size, (int)threads_per_block,                   \
+                                  as_stream(stream));                                                            \
+  }                                                                                                              \
+  xc_status xc_run_hadamard_n_to_m_over_output_##CSUF(const void* left, const void* right, void* out,            \
+                                                      xc_size2 matrix_size, uint32_t left_num, uint32_t right_num, \
+                                                      uint32_t threads_per_block, uint32_t min_items_per_thread,  \
+                                                      void* stream) {                                            \
+    (void)threads_per_block;                                                                                     \
+    (void)min_items_per_thread;                                                                                  \
+    if (left == nullptr || right == nullptr || out == nullptr)                                                   \
+      return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");                                                      \
+    if (left_num == 0 || right_num == 0) return fail(XC_ERR_INVALID_ARGUMENT, "empty batch");                    \
+    return glue_hadamard_n_to_m(DT, left, right, out, (long long)matrix_size.x * matrix_size.y, (int)left_num,   \
+                                (int)right_num, as_stream(stream));                                              \
+  }                                                                                                              \
+  xc_status xc_run_scatter_##RSUF(const T* src, T* dst, xc_size2 src_matrix_size, uint32_t src_num_matrices,     \
+                                  xc_size2 dst_matrix_size, xc_size2 dst_pos, uint32_t threads_per_block,        \
+                                  uint32_t items_per_thread, void* stream) {                                     \
+    (void)threads_per_block;                                                                                     \
+    (void)items_per_thread;                                                                                      \
+    if (src == nullptr || dst == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");                   \
+    if (dst_pos.x + src_matrix_size.x > dst_matrix_size.x || dst_pos.y + src_matrix_size.y > dst_matrix_size.y)  \
+      return fail(XC_ERR_INVALID_ARGUMENT, "source does not fit into the destination at dst_pos");               \
+    return glue_pad(DT, src, dst, (int)src_matrix_size.y, (int)src_matrix_size.x, (int)src_num_matrices,         \
+                    (int)dst_matrix_size.y, (int)dst_matrix_size.x, (int)dst_pos.y, (int)dst_pos.x,               \
+                    as_stream(stream));                                                                          \
+  }                                                                                                              \
+  xc_status xc_normalize_fft_results_##RSUF(const T* raw, T* norm, xc_size2 raw_size, uint32_t count,            \
+                                            void* stream) {                                                      \
+    if (raw == nullptr || norm == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");                 \
+    if (raw_size.x < 2 || raw_size.y < 2) return fail(XC_ERR_INVALID_ARGUMENT, "raw size must be at least 2x2"); \
+    /* The reference puts raw index 0 (shift 0) at norm index (size-1)/2       */                            \
+    /* (src/fft_helpers.hpp:222-226): the generic map with Hr-1 = (size-1)/2.  */                            \
+    const int Sy = (int)raw_size.y - 1, Sx = (int)raw_size.x - 1;                                                \
+    return glue_normalize(DT, raw, norm, (int)raw_size.y, (int)raw_size.x, (int)count, Sy / 2 + 1, Sx / 2 + 1,   \
+                          Sy, Sx, as_stream(stream));                                                            \
+  }
+
+XC_DEFINE_FFT_GLUE(c64, f32, XC_F32, float)
+XC_DEFINE_FFT_GLUE(c128, f64, XC_F64, double)
+
+}  // extern "C"

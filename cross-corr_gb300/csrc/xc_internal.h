@@ -1,0 +1,77 @@
+// xc_internal.h -- C++ interfaces shared between the library's translation
+// units (not part of the public C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "xcorr.h"
+
+namespace xc {
+
+// Mapping of (left l, k-th partner of l) to output and right indices:
+//   output o(l,k) = l*o_l + k*o_k,  right r(l,k) = l*r_l + k*r_k,  k < K.
+// one_to_one/one_to_many: (0,1,0,1); n_to_mn: (1,n,1,n); n_to_m: (M,1,0,1)
+// (src/validate.hpp:216-298).
+struct PairMap {
+  int n_left;
+  int K;
+  long long o_l, o_k, r_l, r_k;
+};
+
+bool make_pair_map(xc_mode mode, uint32_t n_left, uint32_t n_right, PairMap* pm, uint64_t* n_out);
+
+struct Geometry {
+  int Hl, Wl, Hr, Wr;  // left and right matrix sizes
+  int Sy, Sx;          // output size
+};
+
+inline Geometry make_geometry(xc_size2 left, xc_size2 right) {
+  Geometry g;
+  g.Hl = (int)left.y;
+  g.Wl = (int)left.x;
+  g.Hr = (int)right.y;
+  g.Wr = (int)right.x;
+  g.Sy = g.Hl + g.Hr - 1;
+  g.Sx = g.Wl + g.Wr - 1;
+  return g;
+}
+
+// Plain definition-based correlation (direct_simt.cu).
+xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
+                        const PairMap& pm, cudaStream_t stream, int force_loader /* -1 auto, 0 cp.async, 1 TMA */);
+
+// FFT pipeline (fft_pipeline.cu).
+struct FftPlanImpl;
+xc_status fft_plan_create(FftPlanImpl** plan, xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left,
+                          xc_size2 right, uint32_t n_right, xc_size2 pad);
+size_t fft_plan_workspace(const FftPlanImpl* plan);
+xc_size2 fft_plan_pad(const FftPlanImpl* plan);
+xc_status fft_plan_execute(FftPlanImpl* plan, const void* left, const void* right, void* out, int normalize,
+                           void* workspace, size_t ws_bytes, cudaStream_t stream);
+xc_status fft_plan_forward(FftPlanImpl* plan, const void* left, const void* right, void* workspace, size_t ws_bytes,
+                           cudaStream_t stream);
+xc_status fft_plan_multiply(FftPlanImpl* plan, void* workspace, size_t ws_bytes, cudaStream_t stream);
+xc_status fft_plan_inverse(FftPlanImpl* plan, void* out, int normalize, void* workspace, size_t ws_bytes,
+                           cudaStream_t stream);
+void fft_plan_destroy(FftPlanImpl* plan);
+
+// FFT glue kernels (fft_glue.cu).
+xc_status glue_pad(xc_dtype dtype, const void* src, void* dst, int rows, int cols, int count, int pad_rows,
+                   int pad_cols, int dst_y, int dst_x, cudaStream_t stream);
+xc_status glue_pad_pitched(xc_dtype dtype, const void* src, void* dst, int rows, int cols, int count, int pad_rows,
+                           int pad_cols, int dst_pitch, int dst_y, int dst_x, cudaStream_t stream);
+xc_status glue_normalize_pitched(xc_dtype dtype, const void* raw, void* out, int py, int px, int raw_pitch, int count,
+                                 int Hr, int Wr, int Sy, int Sx, bool rawcopy, cudaStream_t stream);
+xc_status glue_conj_multiply_pairs(xc_dtype dtype, const void* lspec, const void* rspec, void* out, long long bins,
+                                   const PairMap& pm, long long n_out, cudaStream_t stream);
+xc_status glue_normalize(xc_dtype dtype, const void* raw, void* out, int py, int px, int count, int Hr, int Wr,
+                         int Sy, int Sx, cudaStream_t stream);
+xc_status glue_hadamard_original(xc_dtype dtype, const void* ref, void* deformed, long long area_per_pic,
+                                 long long batch, int threads, cudaStream_t stream);
+xc_status glue_hadamard_n_to_m(xc_dtype dtype, const void* left, const void* right, void* out, long long area,
+                               int n_left, int n_right, cudaStream_t stream);
+
+}  // namespace xc

@@ -1,0 +1,152 @@
+// xc_runtime.cu -- host runtime pieces shared by every kernel family:
+// thread-local error messages, the TMA descriptor encoder and the per-device
+// flag word that bounded device waits report into.
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "xc_common.cuh"
+#include "xc_internal.h"
+
+namespace xc {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+xc_status fail(xc_status st, const std::string& msg) {
+  set_error(msg);
+  return st;
+}
+
+xc_status from_cuda(cudaError_t err, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorName(err) + " (" + cudaGetErrorString(err) + ")");
+  return XC_ERR_CUDA;
+}
+
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+// ---------------------------------------------------------------------------
+// TMA descriptor encoding through the runtime's driver entry point.
+// ---------------------------------------------------------------------------
+namespace {
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(ptr);
+  });
+  return fn;
+}
+}  // namespace
+
+bool encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
+                  const uint64_t* byte_strides, const uint32_t* box, CUtensorMapSwizzle swizzle) {
+  EncodeTiledFn fn = encode_fn();
+  if (fn == nullptr) {
+    set_error("cuTensorMapEncodeTiled is not available from the driver");
+    return false;
+  }
+  cuuint64_t d[5], s[4];
+  cuuint32_t b[5], e[5];
+  for (int i = 0; i < rank; ++i) {
+    d[i] = dims[i];
+    b[i] = box[i];
+    e[i] = 1;
+  }
+  for (int i = 0; i < rank - 1; ++i) s[i] = byte_strides[i];
+  CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void*>(base), d, s, b, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("cuTensorMapEncodeTiled failed with CUresult " + std::to_string((int)r));
+    return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Device flag word: a file-scope __device__ variable (no allocation).  Its
+// device address is looked up once per device with that device current.
+// ---------------------------------------------------------------------------
+__device__ DeviceFlags g_device_flags;
+
+namespace {
+std::mutex g_flag_mutex;
+DeviceFlags* g_flags[64] = {nullptr};
+}  // namespace
+
+DeviceFlags* device_flags() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_flag_mutex);
+  if (g_flags[dev] == nullptr) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_device_flags) != cudaSuccess) return nullptr;
+    g_flags[dev] = static_cast<DeviceFlags*>(ptr);
+  }
+  return g_flags[dev];
+}
+
+xc_status check_device_flags(cudaStream_t stream) {
+  DeviceFlags* f = device_flags();
+  if (f == nullptr) return XC_OK;
+  DeviceFlags h;
+  XC_CUDA_TRY(cudaMemcpyAsync(&h, f, sizeof(h), cudaMemcpyDeviceToHost, stream));
+  XC_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (h.timeout != 0) {
+    XC_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(DeviceFlags), stream));
+    return fail(XC_ERR_TIMEOUT, "a bounded device wait expired (site " + std::to_string(h.where) + ")");
+  }
+  return XC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Mode -> pair map (src/validate.hpp:216-298).
+// ---------------------------------------------------------------------------
+bool make_pair_map(xc_mode mode, uint32_t n_left, uint32_t n_right, PairMap* pm, uint64_t* n_out) {
+  if (n_left == 0 || n_right == 0) return false;
+  PairMap m;
+  m.n_left = (int)n_left;
+  switch (mode) {
+    case XC_ONE_TO_ONE:
+      if (n_left != 1 || n_right != 1) return false;
+      m.K = 1;
+      m.o_l = 0; m.o_k = 1; m.r_l = 0; m.r_k = 1;
+      *n_out = 1;
+      break;
+    case XC_ONE_TO_MANY:
+      if (n_left != 1) return false;
+      m.K = (int)n_right;
+      m.o_l = 0; m.o_k = 1; m.r_l = 0; m.r_k = 1;
+      *n_out = n_right;
+      break;
+    case XC_N_TO_MN:
+      if (n_right % n_left != 0) return false;
+      m.K = (int)(n_right / n_left);
+      m.o_l = 1; m.o_k = n_left; m.r_l = 1; m.r_k = n_left;
+      *n_out = n_right;
+      break;
+    case XC_N_TO_M:
+      m.K = (int)n_right;
+      m.o_l = n_right; m.o_k = 1; m.r_l = 0; m.r_k = 1;
+      *n_out = (uint64_t)n_left * n_right;
+      break;
+    default:
+      return false;
+  }
+  *pm = m;
+  return true;
+}
+
+}  // namespace xc

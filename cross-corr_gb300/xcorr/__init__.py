@@ -1,0 +1,224 @@
+"""Python binding of the GB300 cross-correlation library (ctypes over the C ABI).
+
+The library itself is ``cross-corr_gb300/_build/libxcorr.so`` (CUDA kernels and
+the C ABI of ``include/xcorr.h``); this module only marshals arguments.  Device
+buffers come from PyTorch (CUDA tensors) or numpy arrays for the host-buffer
+entry point.  Importing never falls back to anything else: if the library has
+not been built, every call raises ``LibraryNotBuilt``.
+
+Mode / result-order conventions follow the reference (src/validate.hpp:216-298):
+  one_to_one : 1 x 1 -> 1;  one_to_many: 1 x M -> M (output i = right i)
+  n_to_mn    : n x (m*n) -> m*n (output i = left i mod n with right i)
+  n_to_m     : n x M -> n*M (output l*M + r = left l with right r)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "_build", "libxcorr.so")
+CLI_PATH = os.path.join(PKG, "_build", "cross")
+
+MODES = {"one_to_one": 0, "one_to_many": 1, "n_to_mn": 2, "n_to_m": 3}
+DTYPES = {"f32": 0, "f64": 1}
+METHODS = {"auto": 0, "direct": 1, "fft": 2, "tc_bf16x3": 3}
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "cuFFT error", 4: "unsupported",
+          5: "workspace too small", 6: "device wait timed out"}
+
+# Every symbol declared in include/xcorr.h (checked by the CPU test suite).
+EXPORTED = [
+    "xc_version", "xc_status_string", "xc_last_error", "xc_device_check", "xc_output_count", "xc_output_size",
+    "xc_workspace_size", "xc_correlate", "xc_correlate_host", "xc_release_thread_cache",
+    "xc_fft_plan_create", "xc_fft_plan_workspace_size", "xc_fft_plan_pad_size", "xc_fft_execute",
+    "xc_fft_forward", "xc_fft_multiply", "xc_fft_inverse", "xc_fft_plan_destroy",
+    "xc_run_ccn_shuffle_f32", "xc_run_ccn_shuffle_f64",
+    "xc_run_ccn_shuffle_multimat_right_f32", "xc_run_ccn_shuffle_multimat_right_f64",
+    "xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f32",
+    "xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f64",
+    "xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f32",
+    "xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f64",
+    "xc_run_hadamard_original_c64", "xc_run_hadamard_original_c128",
+    "xc_run_hadamard_n_to_m_over_output_c64", "xc_run_hadamard_n_to_m_over_output_c128",
+    "xc_run_scatter_f32", "xc_run_scatter_f64",
+    "xc_normalize_fft_results_f32", "xc_normalize_fft_results_f64",
+]
+
+
+class LibraryNotBuilt(RuntimeError):
+    pass
+
+
+class XcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class Size2(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_uint32), ("y", ctypes.c_uint32)]
+
+
+def size2(rows: int, cols: int) -> Size2:
+    return Size2(int(cols), int(rows))
+
+
+_lib = None
+
+
+def lib():
+    """Load libxcorr.so (raises LibraryNotBuilt when it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryNotBuilt(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        c = ctypes
+        vp, u32, i, sz = c.c_void_p, c.c_uint32, c.c_int, c.c_size_t
+        L.xc_version.restype = c.c_char_p
+        L.xc_status_string.restype = c.c_char_p
+        L.xc_status_string.argtypes = [i]
+        L.xc_last_error.restype = c.c_char_p
+        L.xc_device_check.argtypes = [i]
+        L.xc_output_count.argtypes = [i, u32, u32, c.POINTER(c.c_uint64)]
+        L.xc_output_size.argtypes = [Size2, Size2, c.POINTER(Size2)]
+        L.xc_workspace_size.argtypes = [i, i, i, Size2, u32, Size2, u32, c.POINTER(sz)]
+        L.xc_correlate.argtypes = [i, i, i, vp, Size2, u32, vp, Size2, u32, vp, vp, sz, vp]
+        L.xc_correlate_host.argtypes = [i, i, i, vp, Size2, u32, vp, Size2, u32, vp, vp]
+        L.xc_release_thread_cache.restype = None
+        L.xc_fft_plan_create.argtypes = [c.POINTER(vp), i, i, Size2, u32, Size2, u32, Size2]
+        L.xc_fft_plan_workspace_size.argtypes = [vp, c.POINTER(sz)]
+        L.xc_fft_plan_pad_size.argtypes = [vp, c.POINTER(Size2)]
+        L.xc_fft_execute.argtypes = [vp, vp, vp, vp, i, vp, sz, vp]
+        L.xc_fft_forward.argtypes = [vp, vp, vp, vp, sz, vp]
+        L.xc_fft_multiply.argtypes = [vp, vp, sz, vp]
+        L.xc_fft_inverse.argtypes = [vp, vp, i, vp, sz, vp]
+        L.xc_fft_plan_destroy.argtypes = [vp]
+        for t in ("f32", "f64"):
+            getattr(L, f"xc_run_ccn_shuffle_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, vp]
+            getattr(L, f"xc_run_ccn_shuffle_multimat_right_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, u32, u32,
+                                                                              vp]
+            getattr(L, f"xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_{t}").argtypes = [
+                vp, vp, vp, Size2, Size2, u32, u32, u32, u32, u32, vp]
+            getattr(L, f"xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_{t}").argtypes = [
+                vp, vp, vp, Size2, Size2, u32, u32, u32, u32, u32, u32, u32, vp]
+            getattr(L, f"xc_run_scatter_{t}").argtypes = [vp, vp, Size2, u32, Size2, Size2, u32, u32, vp]
+            getattr(L, f"xc_normalize_fft_results_{t}").argtypes = [vp, vp, Size2, u32, vp]
+        for t in ("c64", "c128"):
+            getattr(L, f"xc_run_hadamard_original_{t}").argtypes = [vp, vp, Size2, u32, u32, u32, vp]
+            getattr(L, f"xc_run_hadamard_n_to_m_over_output_{t}").argtypes = [vp, vp, vp, Size2, u32, u32, u32, u32,
+                                                                               vp]
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise XcError(status, lib().xc_last_error().decode())
+
+
+def output_count(mode: str, n_left: int, n_right: int) -> int:
+    n = ctypes.c_uint64()
+    check(lib().xc_output_count(MODES[mode], n_left, n_right, ctypes.byref(n)))
+    return int(n.value)
+
+
+def workspace_size(mode, dtype, method, left_shape, n_left, right_shape, n_right) -> int:
+    b = ctypes.c_size_t()
+    check(lib().xc_workspace_size(MODES[mode], DTYPES[dtype], METHODS[method], size2(*left_shape), n_left,
+                                  size2(*right_shape), n_right, ctypes.byref(b)))
+    return int(b.value)
+
+
+def _stream_ptr(stream) -> Optional[int]:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return int(stream)
+
+
+def correlate(mode: str, left, right, method: str = "direct", out=None, workspace=None, stream=None):
+    """Correlate CUDA tensors ``left`` (n,Hl,Wl) and ``right`` (m,Hr,Wr) on the device.
+
+    Returns the (n_out, Hl+Hr-1, Wl+Wr-1) output tensor.  ``workspace`` (a uint8
+    CUDA tensor) is allocated when not given and the method needs one.
+    """
+    import torch
+
+    if left.dim() == 2:
+        left = left.unsqueeze(0)
+    if right.dim() == 2:
+        right = right.unsqueeze(0)
+    if not (left.is_cuda and right.is_cuda):
+        raise ValueError("correlate() takes CUDA tensors; use correlate_host() for host arrays")
+    dtype = {torch.float32: "f32", torch.float64: "f64"}[left.dtype]
+    left = left.contiguous()
+    right = right.contiguous()
+    n, hl, wl = left.shape
+    m, hr, wr = right.shape
+    n_out = output_count(mode, n, m)
+    if out is None:
+        out = torch.empty((n_out, hl + hr - 1, wl + wr - 1), dtype=left.dtype, device=left.device)
+    ws_bytes = workspace_size(mode, dtype, method, (hl, wl), n, (hr, wr), m)
+    if ws_bytes and (workspace is None or workspace.numel() < ws_bytes):
+        workspace = torch.empty(ws_bytes, dtype=torch.uint8, device=left.device)
+    wptr = workspace.data_ptr() if (workspace is not None and ws_bytes) else None
+    check(lib().xc_correlate(MODES[mode], DTYPES[dtype], METHODS[method], left.data_ptr(), size2(hl, wl), n,
+                             right.data_ptr(), size2(hr, wr), m, out.data_ptr(), wptr, ws_bytes,
+                             _stream_ptr(stream)))
+    return out
+
+
+def correlate_host(mode: str, left: np.ndarray, right: np.ndarray, method: str = "direct", out=None, stream=None):
+    """Host arrays in, host array out (H2D, correlation, D2H inside the call)."""
+    if left.ndim == 2:
+        left = left[None]
+    if right.ndim == 2:
+        right = right[None]
+    dtype = "f64" if left.dtype == np.float64 else "f32"
+    npdt = np.float64 if dtype == "f64" else np.float32
+    left = np.ascontiguousarray(left, dtype=npdt)
+    right = np.ascontiguousarray(right, dtype=npdt)
+    n, hl, wl = left.shape
+    m, hr, wr = right.shape
+    n_out = output_count(mode, n, m)
+    if out is None:
+        out = np.empty((n_out, hl + hr - 1, wl + wr - 1), dtype=npdt)
+    check(lib().xc_correlate_host(MODES[mode], DTYPES[dtype], METHODS[method], left.ctypes.data, size2(hl, wl), n,
+                                  right.ctypes.data, size2(hr, wr), m, out.ctypes.data,
+                                  None if stream is None else int(stream)))
+    return out
+
+
+class FftPlan:
+    """Explicit FFT plan (xc_fft_plan_create); owns its cuFFT plans."""
+
+    def __init__(self, mode, dtype, left_shape, n_left, right_shape, n_right, pad=(0, 0)):
+        self.handle = ctypes.c_void_p()
+        check(lib().xc_fft_plan_create(ctypes.byref(self.handle), MODES[mode], DTYPES[dtype], size2(*left_shape),
+                                       n_left, size2(*right_shape), n_right, size2(*pad)))
+        b = ctypes.c_size_t()
+        check(lib().xc_fft_plan_workspace_size(self.handle, ctypes.byref(b)))
+        self.workspace_bytes = int(b.value)
+        p = Size2()
+        check(lib().xc_fft_plan_pad_size(self.handle, ctypes.byref(p)))
+        self.pad = (int(p.y), int(p.x))
+
+    def execute(self, left, right, out, workspace, normalize=True, stream=None):
+        check(lib().xc_fft_execute(self.handle, left.data_ptr(), right.data_ptr(), out.data_ptr(), int(normalize),
+                                   workspace.data_ptr(), workspace.numel(), _stream_ptr(stream)))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().xc_fft_plan_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,231 @@
+/*
+ * xcorr.h -- C ABI of the GB300 (sm_103a) batched 2D cross-correlation library.
+ *
+ * Drop-in boundary for the hot path of MK4H/cross-corr: the definition-based
+ * warp-shuffle algorithms (`nai_shuffle_*`) and the FFT algorithms (`fft_*`).
+ * The reference has no FFI; its embeddable interface is the C++ kernel-launch
+ * layer in src/kernels.cuh (what its sample_app calls) plus the per-algorithm
+ * plug-in classes (src/cross_corr.hpp).  Every function below names the
+ * reference interface it replaces.
+ *
+ * Conventions
+ *  - Plain pointers and sizes only; no C++ or torch types cross this ABI.
+ *  - Device buffers are owned by the caller (as in the reference's
+ *    prepare_impl, src/one_to_one.hpp:112-118).  Launch-level calls allocate
+ *    nothing and never synchronise; they enqueue on `stream` (a cudaStream_t,
+ *    NULL = legacy default stream).
+ *  - Matrices are row-major, stacked contiguously ("# rows,cols,count" CSV
+ *    order, src/matrix.hpp:94-185).  A size2 is {x = columns, y = rows}, the
+ *    reference's dsize2_t (src/types.cuh:12-156).
+ *  - Output of one pair: (Hl+Hr-1) x (Wl+Wr-1), element
+ *      out[sy + Hr-1][sx + Wr-1] = sum_{y,x} L[y+sy][x+sx] * R[y][x],
+ *    the reference's shift order (src/validate.hpp:117-132) generalised to
+ *    unequal left/right sizes.
+ *  - Result order of the modes follows src/validate.hpp:216-298:
+ *      one_to_one : 1 left, 1 right                 -> 1 output
+ *      one_to_many: 1 left, M right                 -> output i = (left 0, right i)
+ *      n_to_mn    : n left, m*n right               -> output i = (left i mod n, right i)
+ *      n_to_m     : n left, M right                 -> output l*M + r = (left l, right r)
+ *  - Errors never abort: a status is returned and xc_last_error() holds a
+ *    message for the calling thread.
+ */
+#ifndef XCORR_GB300_H
+#define XCORR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum xc_status {
+  XC_OK = 0,
+  XC_ERR_INVALID_ARGUMENT = 1, /* bad sizes/counts/pointers: the reference's argument_error (exit 1) */
+  XC_ERR_CUDA = 2,             /* CUDA runtime error: the reference's exit-3 path (src/main.cpp:268-275) */
+  XC_ERR_CUFFT = 3,            /* cuFFT error: the reference's FFTCH throw (src/fft_helpers.hpp:67-76) */
+  XC_ERR_UNSUPPORTED = 4,      /* valid request this build does not implement (e.g. FP64 tensor path) */
+  XC_ERR_WORKSPACE = 5,        /* workspace too small or missing */
+  XC_ERR_TIMEOUT = 6           /* a bounded device-side wait expired; the context stays usable */
+} xc_status;
+
+typedef enum xc_mode { XC_ONE_TO_ONE = 0, XC_ONE_TO_MANY = 1, XC_N_TO_MN = 2, XC_N_TO_M = 3 } xc_mode;
+
+typedef enum xc_dtype { XC_F32 = 0, XC_F64 = 1 } xc_dtype;
+
+typedef enum xc_method {
+  XC_METHOD_AUTO = 0,     /* library choice */
+  XC_METHOD_DIRECT = 1,   /* plain definition-based kernel (FP32 or FP64 FMA, TMA-staged) */
+  XC_METHOD_FFT = 2,      /* cuFFT transforms + fused pad / conj-multiply / normalise kernels */
+  XC_METHOD_TC_BF16X3 = 3 /* split-BF16 (3 products) tcgen05 tensor-core implicit GEMM, FP32 only */
+} xc_method;
+
+typedef struct xc_size2 {
+  uint32_t x; /* columns */
+  uint32_t y; /* rows */
+} xc_size2;
+
+/* ------------------------------------------------------------------------ */
+/* Library information                                                      */
+/* ------------------------------------------------------------------------ */
+const char* xc_version(void);
+const char* xc_status_string(xc_status status);
+/* Message of the last failed call on this thread ("" if none). */
+const char* xc_last_error(void);
+/* Device compute capability check: XC_OK only on an sm_103 device. */
+xc_status xc_device_check(int device);
+
+/* ------------------------------------------------------------------------ */
+/* Geometry (src/validate.hpp:190-214 result_matrix_size / counts)          */
+/* ------------------------------------------------------------------------ */
+/* Number of result matrices of `mode`; replaces check_num_result_matrices and
+ * the *_validate_input_size predicates (src/one_to_one.hpp:20-22,
+ * src/one_to_many.hpp:15-17, src/n_to_mn.hpp:23-25, src/n_to_m.hpp:19-21). */
+xc_status xc_output_count(xc_mode mode, uint32_t n_left, uint32_t n_right, uint64_t* n_out);
+/* (Hl+Hr-1) x (Wl+Wr-1); replaces result_matrix_size (src/validate.hpp:190). */
+xc_status xc_output_size(xc_size2 left, xc_size2 right, xc_size2* out);
+
+/* ------------------------------------------------------------------------ */
+/* Batched correlation on caller-owned device buffers.                      */
+/* Replaces the run_impl step of every cross_corr_alg plug-in               */
+/* (src/cross_corr.hpp:145, e.g. src/one_to_one.hpp:196-207,                */
+/* src/one_to_many.hpp:571-587, src/n_to_m.hpp:198-212).                    */
+/* ------------------------------------------------------------------------ */
+/* Bytes of device workspace xc_correlate needs (0 for XC_METHOD_DIRECT). */
+xc_status xc_workspace_size(xc_mode mode, xc_dtype dtype, xc_method method, xc_size2 left, uint32_t n_left,
+                            xc_size2 right, uint32_t n_right, size_t* bytes);
+/* Correlates all pairs of `mode`.  `d_left` holds n_left matrices of size
+ * `left`, `d_right` n_right of size `right`, `d_out` receives the outputs in
+ * the mode's order, normalised (FFT results are quadrant-swapped and divided
+ * by the transform size on the device).  The FFT method keeps a per-thread
+ * cache of cuFFT plans: its first call for a shape creates (allocates) plans;
+ * create them explicitly with xc_fft_plan_create to keep allocation out of
+ * timed or captured regions. */
+xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const void* d_left, xc_size2 left,
+                       uint32_t n_left, const void* d_right, xc_size2 right, uint32_t n_right, void* d_out,
+                       void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* Host buffers in and out: allocation, host->device copy, correlation,
+ * device->host copy and free, i.e. the reference's whole
+ * prepare/transfer/run/finalize/free sequence (src/main.cpp:123-174).
+ * Synchronises `stream` before returning. Device buffers are cached per
+ * thread between calls of the same size. */
+xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
+                            uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
+                            void* stream);
+/* Releases the calling thread's cached buffers and plans. */
+void xc_release_thread_cache(void);
+
+/* ------------------------------------------------------------------------ */
+/* FFT pipeline with explicit plans (replaces the cufftPlanMany/exec calls  */
+/* and the host-side normalisation of the fft_* plug-ins:                   */
+/* src/one_to_one.hpp:925-990, src/one_to_many.hpp:538-587,                 */
+/* src/n_to_m.hpp:700-745, src/fft_helpers.hpp:193-261).                    */
+/* ------------------------------------------------------------------------ */
+typedef struct xc_fft_plan_s* xc_fft_plan;
+/* `pad` = transform size; {0,0} selects the reference's 2H x 2W for equal
+ * sizes and the smallest 2^a3^b5^c7^d size >= H+Hr-1 otherwise. */
+xc_status xc_fft_plan_create(xc_fft_plan* plan, xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left,
+                             xc_size2 right, uint32_t n_right, xc_size2 pad);
+xc_status xc_fft_plan_workspace_size(xc_fft_plan plan, size_t* bytes);
+xc_status xc_fft_plan_pad_size(xc_fft_plan plan, xc_size2* pad);
+/* normalize != 0: normalised (Hl+Hr-1)x(Wl+Wr-1) outputs.  normalize == 0:
+ * the raw, unnormalised pad.y x pad.x circular correlations the reference's
+ * fft_* algorithms store without -n (src/fft_alg.hpp:13-20). */
+xc_status xc_fft_execute(xc_fft_plan plan, const void* d_left, const void* d_right, void* d_out, int normalize,
+                         void* d_workspace, size_t workspace_bytes, void* stream);
+/* The three stages of xc_fft_execute, for per-step timing (the reference's
+ * "Forward FFT" / "Hadamard" / "Inverse FFT" measurements,
+ * src/one_to_one.hpp:967-990).  They communicate through the workspace. */
+xc_status xc_fft_forward(xc_fft_plan plan, const void* d_left, const void* d_right, void* d_workspace,
+                         size_t workspace_bytes, void* stream);
+xc_status xc_fft_multiply(xc_fft_plan plan, void* d_workspace, size_t workspace_bytes, void* stream);
+xc_status xc_fft_inverse(xc_fft_plan plan, void* d_out, int normalize, void* d_workspace, size_t workspace_bytes,
+                         void* stream);
+xc_status xc_fft_plan_destroy(xc_fft_plan plan);
+
+/* ------------------------------------------------------------------------ */
+/* Kernel-launch layer: drop-ins for the reference's run_* launchers        */
+/* (src/kernels.cuh), typed per element type like its explicit              */
+/* instantiations (src/naive_shuffle.cu:527-651).  Tile arguments are       */
+/* validated with the reference's limits and otherwise advisory: the GB300  */
+/* kernels pick their own tiling.  Nothing is allocated.                    */
+/* ------------------------------------------------------------------------ */
+/* run_ccn_shuffle (src/kernels.cuh:67-75): one_to_one, matrix_size both inputs. */
+xc_status xc_run_ccn_shuffle_f32(const float* left, const float* right, float* out, xc_size2 matrix_size,
+                                 xc_size2 search_size, uint32_t warps_per_thread_block, void* stream);
+xc_status xc_run_ccn_shuffle_f64(const double* left, const double* right, double* out, xc_size2 matrix_size,
+                                 xc_size2 search_size, uint32_t warps_per_thread_block, void* stream);
+/* run_ccn_shuffle_multimat_right (src/kernels.cuh:88-98): one left, many right. */
+xc_status xc_run_ccn_shuffle_multimat_right_f32(const float* left, const float* right, float* out,
+                                                xc_size2 matrix_size, xc_size2 search_size,
+                                                uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+                                                uint32_t right_matrices_per_thread, void* stream);
+xc_status xc_run_ccn_shuffle_multimat_right_f64(const double* left, const double* right, double* out,
+                                                xc_size2 matrix_size, xc_size2 search_size,
+                                                uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+                                                uint32_t right_matrices_per_thread, void* stream);
+/* run_ccn_shuffle_one_to_many_multirow_both_multimat_right (src/kernels.cuh:245-258),
+ * the launcher the reference's sample_app embeds (sample_app/src/main.cpp:48-59). */
+xc_status xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f32(
+    const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t shifts_per_thread_right_matrix,
+    uint32_t right_matrices_per_thread, uint32_t left_rows_per_iteration, void* stream);
+xc_status xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f64(
+    const double* left, const double* right, double* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t shifts_per_thread_right_matrix,
+    uint32_t right_matrices_per_thread, uint32_t left_rows_per_iteration, void* stream);
+/* run_ccn_n_to_m_shuffle_multirow_both_multimat_both (src/kernels.cuh:260-273):
+ * output index l*num_right + r. */
+xc_status xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f32(
+    const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+    uint32_t shifts_per_thread_right_matrix, uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread,
+    uint32_t left_rows_per_iteration, void* stream);
+xc_status xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f64(
+    const double* left, const double* right, double* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+    uint32_t shifts_per_thread_right_matrix, uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread,
+    uint32_t left_rows_per_iteration, void* stream);
+
+/* run_hadamard_original (src/kernels.cuh:7-15, src/hadamard.cu:33-58,176-192):
+ * in place, deformed[i] = ref[i mod (area*subregions)] * conj(deformed[i]);
+ * complex values as interleaved (re, im) pairs. */
+xc_status xc_run_hadamard_original_c64(const void* ref, void* deformed, xc_size2 subregion_size,
+                                       uint32_t subregions_per_pic, uint32_t batch_size, uint32_t threads_per_block,
+                                       void* stream);
+xc_status xc_run_hadamard_original_c128(const void* ref, void* deformed, xc_size2 subregion_size,
+                                        uint32_t subregions_per_pic, uint32_t batch_size, uint32_t threads_per_block,
+                                        void* stream);
+/* run_hadamard_n_to_m_over_output (src/kernels.cuh:29-38, src/hadamard.cu:116-149):
+ * out[l*R*A + r*A + k] = left[l*A + k] * conj(right[r*A + k]), A = area. */
+xc_status xc_run_hadamard_n_to_m_over_output_c64(const void* left, const void* right, void* out, xc_size2 matrix_size,
+                                                 uint32_t left_num, uint32_t right_num, uint32_t threads_per_block,
+                                                 uint32_t min_items_per_thread, void* stream);
+xc_status xc_run_hadamard_n_to_m_over_output_c128(const void* left, const void* right, void* out,
+                                                  xc_size2 matrix_size, uint32_t left_num, uint32_t right_num,
+                                                  uint32_t threads_per_block, uint32_t min_items_per_thread,
+                                                  void* stream);
+/* run_scatter (src/kernels.cuh:54-63, src/scatter.cu:16-102): copies each src
+ * matrix into dst at dst_pos.  Fixes the reference's non-square column index
+ * (src/scatter.cu:39).  Unlike the reference, also zero-fills the rest of dst,
+ * so no separate cudaMemset pass is needed. */
+xc_status xc_run_scatter_f32(const float* src, float* dst, xc_size2 src_matrix_size, uint32_t src_num_matrices,
+                             xc_size2 dst_matrix_size, xc_size2 dst_pos, uint32_t threads_per_block,
+                             uint32_t items_per_thread, void* stream);
+xc_status xc_run_scatter_f64(const double* src, double* dst, xc_size2 src_matrix_size, uint32_t src_num_matrices,
+                             xc_size2 dst_matrix_size, xc_size2 dst_pos, uint32_t threads_per_block,
+                             uint32_t items_per_thread, void* stream);
+/* normalize_fft_results (src/fft_helpers.hpp:193-261) on the device: `raw` holds
+ * `count` raw circular correlations of size raw_size, `norm` receives
+ * (raw_size.y-1) x (raw_size.x-1) each, quadrant-swapped and divided by the area. */
+xc_status xc_normalize_fft_results_f32(const float* raw, float* norm, xc_size2 raw_size, uint32_t count,
+                                       void* stream);
+xc_status xc_normalize_fft_results_f64(const double* raw, double* norm, xc_size2 raw_size, uint32_t count,
+                                       void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XCORR_GB300_H */

@@ -1,0 +1,225 @@
+"""Parity of the CUDA paths with the oracle and the reference's golden vectors.
+
+Tolerances (max|out - oracle64| / max|oracle64| per output matrix):
+  FP32 direct / FFT path : 1e-5 (the accuracy gate of the metric);
+                           2e-6 against the reference's FP32-level golden files
+                           is not required: those files carry FP32 error themselves,
+                           so the bound there is 1e-5 as well.
+  FP64 direct path       : 1e-12 (FP64-exact golden files and oracle).
+  FP64 FFT path          : 1e-10.
+"""
+import numpy as np
+import pytest
+
+from helpers import FP64_EXACT, VALID, golden_case, rel_to_max, scipy_cases, seeded
+from oracle import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import xcorr  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def device():
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    xcorr.check(xcorr.lib().xc_device_check(0))
+    yield
+    torch.cuda.synchronize()
+
+
+def dev(a, dtype=torch.float32):
+    return torch.as_tensor(np.ascontiguousarray(a)).to(device="cuda", dtype=dtype)
+
+
+def run(mode, left, right, method, dtype=torch.float32):
+    out = xcorr.correlate(mode, dev(left, dtype), dev(right, dtype), method=method)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("method", ["direct", "fft"])
+@pytest.mark.parametrize("name", VALID)
+def test_golden_fp32(name, method):
+    mode, left, right, valid = golden_case(name)
+    out = run(mode, left, right, method)
+    assert out.shape == valid.shape
+    assert rel_to_max(out, valid) <= 1e-5
+
+
+@pytest.mark.parametrize("name", sorted(FP64_EXACT))
+def test_golden_fp64_direct(name):
+    mode, left, right, valid = golden_case(name)
+    out = run(mode, left, right, "direct", torch.float64)
+    assert rel_to_max(out, valid) <= 1e-12
+
+
+@pytest.mark.parametrize("name", sorted(FP64_EXACT))
+def test_golden_fp64_fft(name):
+    mode, left, right, valid = golden_case(name)
+    out = run(mode, left, right, "fft", torch.float64)
+    assert rel_to_max(out, valid) <= 1e-10
+
+
+@pytest.mark.parametrize("method", ["direct", "fft"])
+@pytest.mark.parametrize("case", range(12))
+def test_reference_scipy_cases(case, method):
+    """Odd sizes, 1xN strips and unequal left/right sizes."""
+    mode, left, right, ref = scipy_cases()[case]
+    out = run(mode, left, right, method)
+    assert out.shape == ref.shape
+    assert rel_to_max(out, ref) <= 1e-5
+    out64 = run(mode, left, right, method, torch.float64)
+    assert rel_to_max(out64, ref) <= (1e-12 if method == "direct" else 1e-10)
+
+
+# Seeded sizes around the kernel's tile edges (32 x 64 shifts, 128-column
+# chunks), including widths that are not a multiple of 4 (cp.async loader).
+SHAPES = [
+    ("one_to_one", 1, 1, (1, 1), (1, 1)),
+    ("one_to_one", 1, 1, (33, 65), (33, 65)),
+    ("one_to_one", 1, 1, (130, 131), (7, 200)),
+    ("one_to_many", 1, 9, (64, 64), (64, 64)),
+    ("one_to_many", 1, 5, (37, 150), (61, 3)),
+    ("n_to_mn", 3, 9, (29, 29), (29, 29)),
+    ("n_to_m", 2, 5, (48, 20), (16, 52)),
+    ("n_to_m", 3, 3, (70, 1), (5, 1)),
+]
+
+
+@pytest.mark.parametrize("dist", ["uniform", "normal"])
+@pytest.mark.parametrize("shape", SHAPES, ids=[f"{s[0]}-{s[3]}-{s[4]}" for s in SHAPES])
+def test_seeded_shapes_direct_and_fft(shape, dist):
+    mode, n, m, ls, rs = shape
+    left = seeded((n,) + ls, 100 + n, dist)
+    right = seeded((m,) + rs, 200 + m, dist)
+    ref = oracle.run_mode(mode, left, right, dtype="f32acc64", threads=8)
+    for method in ("direct", "fft"):
+        out = run(mode, left, right, method)
+        assert out.shape == ref.shape
+        assert rel_to_max(out, ref) <= 1e-5, method
+
+
+def test_direct_fp32_accuracy_at_256_one_to_many():
+    """Long overlaps (256x256) stay under the 1e-5 gate thanks to the flushed
+    partial sums; 4 right matrices of the bench shape."""
+    left = seeded((1, 256, 256), 2)
+    right = seeded((4, 256, 256), 3)
+    ref = oracle.run_mode("one_to_many", left, right, dtype="f32acc64", threads=8)
+    out = run("one_to_many", left, right, "direct")
+    assert rel_to_max(out, ref) <= 1e-5
+
+
+def test_direct_loaders_agree():
+    """TMA loader and cp.async loader give the same sums on aligned widths."""
+    left = seeded((2, 40, 64), 7, "normal")
+    right = seeded((4, 24, 32), 8, "normal")
+    ref = oracle.run_mode("n_to_mn", left, right, dtype="f32acc64")
+    out = run("n_to_mn", left, right, "direct")
+    assert rel_to_max(out, ref) <= 1e-5
+
+
+def test_fft_raw_output_matches_reference_normalisation():
+    """normalize=0 returns the raw circular result; the reference's host
+    normalisation of it equals the full correlation."""
+    left = seeded((1, 20, 20), 11)
+    right = seeded((3, 20, 20), 12)
+    plan = xcorr.FftPlan("one_to_many", "f32", (20, 20), 1, (20, 20), 3)
+    assert plan.pad == (40, 40)
+    ws = torch.empty(plan.workspace_bytes, dtype=torch.uint8, device="cuda")
+    raw = torch.empty((3, 40, 40), dtype=torch.float32, device="cuda")
+    plan.execute(dev(left), dev(right), raw, ws, normalize=False)
+    torch.cuda.synchronize()
+    norm = oracle.normalize_fft(raw.cpu().numpy())
+    ref = oracle.run_mode("one_to_many", left, right)
+    assert rel_to_max(norm, ref) <= 1e-5
+    plan.close()
+
+
+def test_host_buffer_entry_point():
+    left = seeded((2, 30, 30), 21)
+    right = seeded((3, 30, 30), 22)
+    ref = oracle.run_mode("n_to_m", left, right)
+    for method in ("direct", "fft"):
+        out = xcorr.correlate_host("n_to_m", left, right, method=method)
+        assert rel_to_max(out, ref) <= 1e-5
+    out64 = xcorr.correlate_host("n_to_m", left.astype(np.float64), right.astype(np.float64))
+    assert rel_to_max(out64, oracle.run_mode("n_to_m", left.astype(np.float64), right.astype(np.float64),
+                                             dtype="f64")) <= 1e-12
+
+
+def test_reference_launchers():
+    """Drop-ins for run_ccn_shuffle* launchers (src/kernels.cuh)."""
+    import ctypes
+    L = xcorr.lib()
+    left = dev(seeded((1, 17, 17), 31))
+    right = dev(seeded((6, 17, 17), 32))
+    out = torch.zeros((6, 33, 33), device="cuda")
+    ms, ss = xcorr.size2(17, 17), xcorr.size2(33, 33)
+    st = torch.cuda.current_stream().cuda_stream
+    xcorr.check(L.xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f32(
+        left.data_ptr(), right.data_ptr(), out.data_ptr(), ms, ss, 6, 8, 4, 4, 4, st))
+    torch.cuda.synchronize()
+    ref = oracle.run_mode("one_to_many", left.cpu().numpy(), right.cpu().numpy())
+    assert rel_to_max(out.cpu().numpy(), ref) <= 1e-5
+    # the reference's limits are enforced
+    assert L.xc_run_ccn_shuffle_f32(left.data_ptr(), right.data_ptr(), out.data_ptr(), ms, ss, 33, st) == 1
+    assert L.xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f32(
+        left.data_ptr(), right.data_ptr(), out.data_ptr(), ms, ss, 6, 8, 5, 4, 4, st) == 1
+    # n_to_m launcher: output l*M + r
+    lefts = dev(seeded((2, 9, 9), 33))
+    rights = dev(seeded((3, 9, 9), 34))
+    o2 = torch.zeros((6, 17, 17), device="cuda")
+    xcorr.check(L.xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f32(
+        lefts.data_ptr(), rights.data_ptr(), o2.data_ptr(), xcorr.size2(9, 9), xcorr.size2(17, 17), 2, 3, 8, 2, 2, 2,
+        2, st))
+    torch.cuda.synchronize()
+    ref2 = oracle.run_mode("n_to_m", lefts.cpu().numpy(), rights.cpu().numpy())
+    assert rel_to_max(o2.cpu().numpy(), ref2) <= 1e-5
+
+
+def test_fft_glue_launchers():
+    """hadamard_original / hadamard_n_to_m_over_output / scatter / normalize drop-ins."""
+    L = xcorr.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(41)
+    ref = (rng.standard_normal((4, 5)) + 1j * rng.standard_normal((4, 5))).astype(np.complex64)
+    deformed = (rng.standard_normal((3, 4, 5)) + 1j * rng.standard_normal((3, 4, 5))).astype(np.complex64)
+    d_ref = torch.as_tensor(ref).cuda()
+    d_def = torch.as_tensor(deformed).cuda()
+    xcorr.check(L.xc_run_hadamard_original_c64(d_ref.data_ptr(), d_def.data_ptr(), xcorr.size2(4, 5), 1, 3, 128, st))
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(d_def.cpu().numpy(), ref[None] * np.conj(deformed), rtol=1e-6, atol=1e-6)
+
+    lt = (rng.standard_normal((2, 6)) + 1j * rng.standard_normal((2, 6))).astype(np.complex64)
+    rt = (rng.standard_normal((3, 6)) + 1j * rng.standard_normal((3, 6))).astype(np.complex64)
+    o = torch.zeros((2, 3, 6), dtype=torch.complex64, device="cuda")
+    xcorr.check(L.xc_run_hadamard_n_to_m_over_output_c64(torch.as_tensor(lt).cuda().data_ptr(),
+                                                         torch.as_tensor(rt).cuda().data_ptr(), o.data_ptr(),
+                                                         xcorr.size2(2, 3), 2, 3, 256, 1, st))
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(o.cpu().numpy(), lt[:, None, :] * np.conj(rt[None, :, :]), rtol=1e-6, atol=1e-6)
+
+    src = seeded((2, 3, 5), 42)
+    dst = torch.full((2, 6, 10), 7.0, device="cuda")
+    xcorr.check(L.xc_run_scatter_f32(dev(src).data_ptr(), dst.data_ptr(), xcorr.size2(3, 5), 2, xcorr.size2(6, 10),
+                                     xcorr.size2(1, 2), 256, 10, st))
+    torch.cuda.synchronize()
+    exp = np.zeros((2, 6, 10), np.float32)
+    exp[:, 1:4, 2:7] = src
+    np.testing.assert_array_equal(dst.cpu().numpy(), exp)
+
+    raw = seeded((2, 8, 6), 43, "normal")
+    norm = torch.zeros((2, 7, 5), device="cuda")
+    xcorr.check(L.xc_normalize_fft_results_f32(dev(raw).data_ptr(), norm.data_ptr(), xcorr.size2(8, 6), 2, st))
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(norm.cpu().numpy(), oracle.normalize_fft(raw), rtol=1e-6, atol=1e-7)
+
+
+def test_errors_are_reported_not_fatal():
+    with pytest.raises(xcorr.XcError) as e:
+        xcorr.correlate("n_to_mn", dev(seeded((3, 4, 4), 1)), dev(seeded((4, 4, 4), 2)))
+    assert e.value.status == 1
+    # the context is still usable
+    out = run("one_to_one", seeded((1, 4, 4), 1), seeded((1, 4, 4), 2), "direct")
+    assert out.shape == (1, 7, 7)
