@@ -1,19 +1,704 @@
-// tc_bf16x3.cu -- split-BF16 tensor-core correlation (tcgen05), FP32 in/out.
+// tc_bf16x3.cu -- split-BF16 tensor-core correlation on tcgen05 (sm_103a).
+//
+// FP32 inputs, FP32 outputs, three BF16 products per FP32 product:
+//   x = x_hi + x_lo, x_hi = bf16(x), x_lo = bf16(x - x_hi)
+//   L*R ~= L_hi*R_hi + L_hi*R_lo + L_lo*R_hi      (Henry, Tang & Heinecke 2019)
+//
+// Formulation (implicit GEMM).  For a left row a and a right row b the
+// contribution to output row sy = a - b + Hr - 1 is a 1D correlation, a
+// Toeplitz matrix-vector product.  One tcgen05.mma computes
+//     D[m][n] += sum_k A[m][k] * B[n][k]        (M=128, N<=64, K=16, BF16)
+// with
+//   m -> (partner matrix p, row shift dy): A[m][k] = R_p[a - dy][k0 + k]
+//        (right rows, staged by TMA with 128-byte swizzle, K-major);
+//   n -> column shift sx = c + 8n for a phase c in 0..7:
+//        B[n][k] = Lpad_a[c + 8n + k0 + k]
+//        where Lpad_a[j] = L[a][j - (Wr-1)] (zero outside the row).
+// B is a Toeplitz matrix.  It is read straight out of one shared-memory copy
+// of the (split) left row per phase c: a no-swizzle K-major descriptor whose
+// 8x16-byte core matrices overlap (leading byte offset 16 = 8 elements along
+// K, stride byte offset 128 = 64 elements along N) addresses element
+// 8n + k of the copy.  Nothing is materialised per shift; eight phase copies
+// of each left row cover every column shift.
+//
+// The accumulator tile is 128 lanes x (8 phases x N) FP32 columns of tensor
+// memory.  Every `flush_rows` left rows the epilogue warps drain it into the
+// output with FP32 reductions (red.global.add), so long row ranges can also
+// be split over several CTAs; the MMA warp waits during a drain.
+//
+// Accuracy.  Tensor-core FP32 accumulation drops low bits on every MMA with a
+// consistent sign, so the error of a long chain grows linearly with its
+// length and with the magnitude of the partial sums (measured on GB300:
+// ~1.2e-6 of max|out| per 48-MMA left row for uniform [0,1) data).  Each
+// matrix is therefore shifted by its mean before the split
+// (L' = L - mu_L, R' = R - mu_R): the tensor cores correlate the centred data,
+// whose partial sums are small random walks, and the exact remainder
+//   out = corr(L', R') + mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area
+// (S = sum of the centred matrix over the overlap of a shift, from FP64 2D
+// prefix sums) is written first by a correction kernel, which the tensor-core
+// drains then accumulate into.
+//
+// Warp roles (256 threads, one CTA per SM):
+//   warp 0    TMA producer of the right-row tiles (hi and lo planes)
+//   warp 1    TMEM allocation and the single-thread MMA issuer
+//   warps 2-3 build the eight phase copies of each split left row
+//   warps 4-7 epilogue (tcgen05.ld -> shared staging -> coalesced global)
+// All waits are bounded: an expired wait records a flag, the CTA winds down,
+// waits (bounded) for its own copies and MMAs, frees TMEM and returns.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstdlib>
+#include <string>
+
 #include "xc_common.cuh"
 #include "xc_internal.h"
 
 namespace xc {
 
+namespace {
+
+constexpr int kStages = 4;          // right-row tile pipeline depth
+constexpr int kTileBytes = 128 * 128;  // 128 rows x 64 bf16 (one plane)
+constexpr int kStageBytes = 2 * kTileBytes;
+constexpr int kThreads = 256;
+constexpr int kStgPitch = 65;       // epilogue staging row pitch (floats)
+// 15 mbarriers (120 B), the abort flag and the TMEM address slot
+constexpr int kBarBytes = 256;
+
+struct TcParams {
+  const float* left;
+  const float* mu_left;  // mean of every left matrix (the shift of the split)
+  float* out;
+  int Hl, Wl, Hr, Wr, Sy, Sx;
+  PairMap pm;
+  int P, DY;        // partners x row shifts per tile, P*DY = 128
+  int mats_mode;    // 1: one TMA box per row shift spans P partners; 0: one box per partner spans DY rows
+  int n_pgroups;    // ceil(K / P)
+  int n_dytiles;    // ceil(Sy / DY)
+  int N;            // B rows per phase (multiple of 16, 8N >= Sx)
+  int nkc;          // 64-column chunks of a right row
+  int buf_len;      // elements of one phase copy (multiple of 8)
+  int flush_rows;   // drain TMEM every this many left rows
+  int chunk_rows;   // left rows per CTA (a longer row range is split over CTAs)
+  int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
+  DeviceFlags* flags;
+};
+
+// ---------------------------------------------------------------------------
+// tcgen05 / descriptor helpers
+// ---------------------------------------------------------------------------
+// Shared-memory matrix descriptor (sm_100 family): start>>4 [0,14), LBO>>4
+// [16,30), SBO>>4 [32,46), version 1 at bit 46, layout type [61,64)
+// (0 = no swizzle, 2 = 128-byte swizzle).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo, uint32_t layout) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)(layout & 7u) << 61;
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D=F32 (bits 4-5 = 1), A=B=BF16 (bits 7-9,
+// 10-12 = 1), both K-major, N>>3 at bit 17, M>>4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void red_add(float* addr, float v) {
+  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v) : "memory");
+}
+
+// Bounded wait that also gives up as soon as another role aborted.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                              DeviceFlags* flags, unsigned where) {
+  for (uint32_t i = 0; i < (1u << 22); ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  record_timeout(flags, where);
+  return false;
+}
+
+// dy-tile visiting order: centre (heaviest overlap) first, then alternating
+// outwards, so long tiles start early.
+__device__ __forceinline__ int centre_out(int r, int n, int tc) {
+  const int below = tc, above = n - tc - 1;
+  const int m = min(below, above);
+  if (r == 0) return tc;
+  if (r <= 2 * m) return (r & 1) ? tc + (r + 1) / 2 : tc - r / 2;
+  const int extra = r - 2 * m;
+  return above > below ? tc + m + extra : tc - m - extra;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
+              const TcParams p) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* a_tiles = smem;                                   // kStages x (hi, lo) x 16 KB
+  __nv_bfloat16* b_bufs = reinterpret_cast<__nv_bfloat16*>(smem + kStages * kStageBytes);  // 2 x 8 x 2 x buf_len
+  const int b_slot_elems = 16 * p.buf_len;
+  float* stg = reinterpret_cast<float*>(b_bufs + 2 * b_slot_elems);  // 4 warps x 32 x kStgPitch
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stg + 4 * 32 * kStgPitch);
+  uint64_t* a_full = bars;
+  uint64_t* a_empty = bars + kStages;
+  uint64_t* b_full = bars + 2 * kStages;
+  uint64_t* b_empty = b_full + 2;
+  uint64_t* t_full = b_empty + 2;
+  uint64_t* t_empty = t_full + 1;
+  uint64_t* mma_done = t_empty + 1;
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 1);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 2);
+
+  // ---- tile of this CTA -------------------------------------------------
+  // blockIdx = (chunk * n_dytiles + rank) * per_rank + lp: all first chunks
+  // (centre tiles first) before any second chunk.
+  const int per_rank = p.pm.n_left * p.n_pgroups;
+  const int lp = blockIdx.x % per_rank;
+  const int rank = (blockIdx.x / per_rank) % p.n_dytiles;
+  const int chunk = blockIdx.x / (per_rank * p.n_dytiles);
+  const int l = lp / p.n_pgroups;
+  const int p0 = (lp % p.n_pgroups) * p.P;
+  const int t = centre_out(rank, p.n_dytiles, (p.Hr - 1) / p.DY);
+  const int dy0 = -(p.Hr - 1) + t * p.DY;
+  const int tile_lo = max(0, dy0);
+  const int tile_hi = min(p.Hl, dy0 + p.DY - 1 + p.Hr);
+  const int a_lo = tile_lo + chunk * p.chunk_rows;
+  const int a_hi = min(tile_hi, a_lo + p.chunk_rows);
+  const int n_rows = a_hi - a_lo;
+  if (n_rows <= 0) return;  // uniform over the CTA
+  const int n_drains = (n_rows + p.flush_rows - 1) / p.flush_rows;
+  const int rdim2 = p.pm.r_l != 0 ? l : 0;
+  const uint32_t ncols = 8u * (uint32_t)p.N <= 32 ? 32u : (8u * p.N <= 64 ? 64u : (8u * p.N <= 128 ? 128u : (8u * p.N <= 256 ? 256u : 512u)));
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&a_full[s], 1);
+      mbar_init(&a_empty[s], 1);
+    }
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&b_full[s], 64);
+      mbar_init(&b_empty[s], 1);
+    }
+    mbar_init(t_full, 1);
+    mbar_init(t_empty, 128);
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+    prefetch_tensormap(&map_hi);
+    prefetch_tensormap(&map_lo);
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int it = 0;
+      bool ok = true;
+      for (int ai = 0; ai < n_rows && ok; ++ai) {
+        const int a = a_lo + ai;
+        for (int kc = 0; kc < p.nkc && ok; ++kc, ++it) {
+          const int s = it % kStages;
+          if (!wait_or_abort(&a_empty[s], ((it / kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&a_full[s], kStageBytes);
+          unsigned char* hi = a_tiles + s * kStageBytes;
+          unsigned char* lo = hi + kTileBytes;
+          if (p.mats_mode) {
+            for (int d = 0; d < p.DY; ++d) {
+              const int b = a - (dy0 + d);
+              tma_load_4d(hi + d * p.P * 128, &map_hi, &a_full[s], kc * 64, b, rdim2, p0);
+              tma_load_4d(lo + d * p.P * 128, &map_lo, &a_full[s], kc * 64, b, rdim2, p0);
+            }
+          } else {
+            const int b0 = a - dy0 - (p.DY - 1);
+            for (int q = 0; q < p.P; ++q) {
+              tma_load_4d(hi + q * p.DY * 128, &map_hi, &a_full[s], kc * 64, b0, rdim2, p0 + q);
+              tma_load_4d(lo + q * p.DY * 128, &map_lo, &a_full[s], kc * 64, b0, rdim2, p0 + q);
+            }
+          }
+        }
+      }
+      if (!ok) {
+        // let the copies already issued land before the CTA exits
+        for (int q = max(0, it - kStages); q < it; ++q)
+          mbar_wait_bounded(&a_full[q % kStages], (q / kStages) & 1, 1u << 16);
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(128, p.N);
+      const uint32_t a_base = smem_u32(a_tiles);
+      const uint32_t b_base = smem_u32(b_bufs);
+      const uint32_t copy_bytes = (uint32_t)p.buf_len * 2;
+      int it = 0, drain = 0;
+      bool first = true, ok = true;
+      for (int ai = 0; ai < n_rows && ok; ++ai) {
+        const int bs = ai & 1;
+        if (!wait_or_abort(&b_full[bs], (ai >> 1) & 1, abort_flag, p.flags, 12)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t bslot = b_base + (uint32_t)bs * (uint32_t)b_slot_elems * 2;
+        for (int kc = 0; kc < p.nkc; ++kc, ++it) {
+          const int s = it % kStages;
+          if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a_hi_addr = a_base + (uint32_t)s * kStageBytes;
+          const uint32_t a_lo_addr = a_hi_addr + kTileBytes;
+#pragma unroll 1
+          for (int ks = 0; ks < 4; ++ks) {
+            const uint64_t ahi = smem_desc(a_hi_addr + ks * 32, 16, 1024, 2);
+            const uint64_t alo = smem_desc(a_lo_addr + ks * 32, 16, 1024, 2);
+            const uint32_t koff = (uint32_t)(kc * 64 + ks * 16) * 2;
+            const uint32_t acc0 = (first && kc == 0 && ks == 0) ? 0u : 1u;
+#pragma unroll 1
+            for (int c = 0; c < 8; ++c) {
+              const uint32_t bhi_addr = bslot + (uint32_t)c * 2 * copy_bytes + koff;
+              const uint64_t bhi = smem_desc(bhi_addr, 16, 128, 0);
+              const uint64_t blo = smem_desc(bhi_addr + copy_bytes, 16, 128, 0);
+              const uint32_t d = tmem_base + (uint32_t)(c * p.N);
+              mma_bf16(d, ahi, bhi, idesc, acc0);
+              mma_bf16(d, ahi, blo, idesc, 1u);
+              mma_bf16(d, alo, bhi, idesc, 1u);
+            }
+          }
+          mma_commit(&a_empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&b_empty[bs]);
+        first = false;
+        if ((ai + 1) % p.flush_rows == 0 || ai == n_rows - 1) {
+          mma_commit(t_full);
+          if (!wait_or_abort(t_empty, drain & 1, abort_flag, p.flags, 14)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          ++drain;
+          first = true;
+        }
+      }
+      // All MMAs issued by this thread must finish before TMEM is released.
+      mma_commit(mma_done);
+      mbar_wait_bounded(mma_done, 0, 1u << 22);
+    }
+  } else if (warp < 4) {
+    // ------------------------------------------------------------ B builders
+    const int bt = threadIdx.x - 64;  // 0..63
+    const float* lrow_base = p.left + (long long)l * p.Hl * p.Wl;
+    const float mu = p.mu_left[l];
+    const int nvec = p.buf_len / 8;
+    for (int ai = 0; ai < n_rows; ++ai) {
+      const int bs = ai & 1;
+      if (!wait_or_abort(&b_empty[bs], ((ai >> 1) & 1) ^ 1, abort_flag, p.flags, 15)) break;
+      const float* lrow = lrow_base + (long long)(a_lo + ai) * p.Wl;
+      __nv_bfloat16* slot = b_bufs + bs * b_slot_elems;
+      for (int item = bt; item < 8 * nvec; item += 64) {
+        const int c = item / nvec, jv = item % nvec;
+        const int j0 = jv * 8 + c - (p.Wr - 1);  // left column of element 0
+        __align__(16) __nv_bfloat16 hi[8];
+        __align__(16) __nv_bfloat16 lo[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          const int x = j0 + e;
+          const float v = (x >= 0 && x < p.Wl) ? __ldg(lrow + x) - mu : 0.0f;
+          const __nv_bfloat16 h = __float2bfloat16_rn(v);
+          hi[e] = h;
+          lo[e] = __float2bfloat16_rn(v - __bfloat162float(h));
+        }
+        __nv_bfloat16* dst = slot + (c * 2) * p.buf_len + jv * 8;
+        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(hi);
+        *reinterpret_cast<uint4*>(dst + p.buf_len) = *reinterpret_cast<const uint4*>(lo);
+      }
+      fence_proxy_async_shared();
+      mbar_arrive(&b_full[bs]);
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q = warp & 3;  // TMEM lane quadrant of this warp
+    float* st = stg + q * 32 * kStgPitch;
+    for (int d = 0; d < n_drains; ++d) {
+      if (!wait_or_abort(t_full, d & 1, abort_flag, p.flags, 16)) break;
+      tc_fence_after();
+      for (int n0 = 0; n0 < p.N; n0 += 8) {
+        float v[8][8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) tmem_ld8(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * p.N + n0), v[c]);
+        tmem_wait_ld();
+        // this thread's row: sx = 8*(n0 + j) + c
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+#pragma unroll
+          for (int c = 0; c < 8; ++c) st[lane * kStgPitch + j * 8 + c] = v[c][j];
+        __syncwarp();
+        // coalesced read-add-write of the 32 rows, 64 columns each
+        for (int r = 0; r < 32; ++r) {
+          const int mr = q * 32 + r;
+          int rp, rdy;
+          if (p.mats_mode) {
+            rp = mr % p.P;
+            rdy = dy0 + mr / p.P;
+          } else {
+            rp = mr / p.DY;
+            rdy = dy0 + (p.DY - 1) - (mr % p.DY);
+          }
+          const int rk = p0 + rp, rsy = rdy + p.Hr - 1;
+          if (rk >= p.pm.K || rsy < 0 || rsy >= p.Sy) continue;
+          float* orow = p.out + ((long long)l * p.pm.o_l + (long long)rk * p.pm.o_k) * p.Sy * p.Sx +
+                        (long long)rsy * p.Sx + 8 * n0;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int col = lane + 32 * h;
+            if (8 * n0 + col < p.Sx) red_add(orow + col, st[r * kStgPitch + col]);
+          }
+        }
+        __syncwarp();
+      }
+      tc_fence_before();
+      mbar_arrive(t_empty);
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(ncols) : "memory");
+  }
+}
+
+// Mean of every matrix (FP64 sum, FP32 result): one block per matrix.
+__global__ void mean_kernel(const float* __restrict__ left, long long left_area, int n_left,
+                            const float* __restrict__ right, long long right_area, float* __restrict__ mu) {
+  const int m = blockIdx.x;
+  const float* src = m < n_left ? left + (long long)m * left_area : right + (long long)(m - n_left) * right_area;
+  const long long area = m < n_left ? left_area : right_area;
+  double acc = 0.0;
+  for (long long i = threadIdx.x; i < area; i += blockDim.x) acc += (double)src[i];
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) mu[m] = (float)(acc / (double)area);
+  }
+}
+
+// 2D prefix sums (FP64) of the centred matrices fl32(x - mu): P[y][x] =
+// sum_{i<y, j<x}, (H+1) x (W+1) per matrix.  One block per matrix: rows are
+// scanned by threads, then columns.
+__global__ void prefix_kernel(const float* __restrict__ src, long long stride, int H, int W,
+                              const float* __restrict__ mu, double* __restrict__ P) {
+  const int m = blockIdx.x;
+  const float* a = src + (long long)m * stride;
+  const float mv = mu[m];
+  double* q = P + (long long)m * (H + 1) * (W + 1);
+  for (int x = threadIdx.x; x <= W; x += blockDim.x) q[x] = 0.0;
+  for (int y = threadIdx.x; y < H; y += blockDim.x) {
+    double acc = 0.0;
+    double* row = q + (long long)(y + 1) * (W + 1);
+    row[0] = 0.0;
+    for (int x = 0; x < W; ++x) {
+      acc += (double)(a[(long long)y * W + x] - mv);
+      row[x + 1] = acc;
+    }
+  }
+  __syncthreads();
+  for (int x = threadIdx.x; x <= W; x += blockDim.x) {
+    double acc = 0.0;
+    for (int y = 1; y <= H; ++y) {
+      acc += q[(long long)y * (W + 1) + x];
+      q[(long long)y * (W + 1) + x] = acc;
+    }
+  }
+}
+
+// Splits the centred right matrices fl32(R - mu_R) into BF16 hi/lo planes
+// with a padded pitch.
+__global__ void split_kernel(const float* __restrict__ src, const float* __restrict__ mu,
+                             __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, long long rows,
+                             int rows_per_matrix, int cols, int pitch) {
+  const long long total = rows * pitch;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long r = i / pitch;
+    const int c = (int)(i % pitch);
+    const float v = c < cols ? src[r * cols + c] - mu[r / rows_per_matrix] : 0.0f;
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    hi[i] = h;
+    lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
+}
+
+// out[o][sy][sx] = mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area over the
+// overlap of shift (sy, sx); one block per output row.
+__global__ void correction_kernel(float* __restrict__ out, const double* __restrict__ PL,
+                                  const double* __restrict__ PR, const float* __restrict__ mu_l,
+                                  const float* __restrict__ mu_r, int Hl, int Wl, int Hr, int Wr, int Sy, int Sx,
+                                  PairMap pm, long long n_out) {
+  const long long row = blockIdx.x;  // o * Sy + sy
+  const long long o = row / Sy;
+  const int sy = (int)(row % Sy);
+  // invert o = l*o_l + k*o_k for the three pair-map forms
+  long long l, k;
+  if (pm.o_l == 0) {  // one_to_one / one_to_many: o = k
+    l = 0;
+    k = o;
+  } else if (pm.o_k == 1 && pm.o_l == pm.K) {  // n_to_m: o = l*K + k
+    l = o / pm.K;
+    k = o % pm.K;
+  } else {  // n_to_mn: o = l + k*n
+    l = o % pm.n_left;
+    k = o / pm.n_left;
+  }
+  const long long r = l * pm.r_l + k * pm.r_k;
+  (void)n_out;
+  const int dy = sy - (Hr - 1);
+  const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
+  const double ml = mu_l[l], mr = mu_r[r];
+  const double* pl0 = PL + (l * (Hl + 1) + y0) * (long long)(Wl + 1);
+  const double* pl1 = PL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
+  const double* pr0 = PR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
+  const double* pr1 = PR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
+  float* orow = out + row * Sx;
+  for (int sx = threadIdx.x; sx < Sx; sx += blockDim.x) {
+    const int dx = sx - (Wr - 1);
+    const int x0 = max(0, dx), x1 = min(Wl, Wr + dx);
+    const double sl = pl1[x1] - pl0[x1] - pl1[x0] + pl0[x0];
+    const double sr = pr1[x1 - dx] - pr0[x1 - dx] - pr1[x0 - dx] + pr0[x0 - dx];
+    const double cnt = (double)(y1 - y0) * (double)(x1 - x0);
+    orow[sx] = (float)(mr * sl + ml * sr + ml * mr * cnt);
+  }
+}
+
+struct TcPlan {
+  int P, DY, mats_mode, N, nkc, buf_len, pitch;
+  int smem_bytes;
+};
+
+bool tc_plan(const Geometry& g, const PairMap& pm, TcPlan* t) {
+  if (g.Sx > 512 || g.Wr > 256) return false;  // 8 phases x N <= 512 TMEM columns
+  int P = 1;
+  while (P < 128 && P < pm.K) P *= 2;
+  t->P = P;
+  t->DY = 128 / P;
+  t->mats_mode = P >= 8 ? 1 : 0;
+  int N = (g.Sx + 7) / 8;
+  N = (N + 15) / 16 * 16;
+  if (N < 16) N = 16;
+  t->N = N;
+  t->nkc = (g.Wr + 63) / 64;
+  t->buf_len = t->nkc * 64 + 8 * N;
+  t->pitch = (g.Wr + 7) / 8 * 8;
+  t->smem_bytes = 1024 + kStages * kStageBytes + 2 * 16 * t->buf_len * 2 + 4 * 32 * kStgPitch * 4 + kBarBytes;
+  return t->smem_bytes <= 227 * 1024;
+}
+
+long long n_right_of(const PairMap& pm) {
+  // right matrices addressed by the pair map: r = l*r_l + k*r_k
+  return (long long)(pm.n_left - 1) * pm.r_l + (long long)(pm.K - 1) * pm.r_k + 1;
+}
+
+int env_int(const char* name, int def) {
+  const char* e = std::getenv(name);
+  const int v = e ? std::atoi(e) : 0;
+  return v > 0 ? v : def;
+}
+
+// Left rows accumulated in tensor memory between two drains: at most 192
+// MMAs (12 per 64-column chunk of a right row: 4 K-steps x 3 products) feed
+// one accumulator between drains, which keeps the truncation error of the
+// tensor-core accumulation (about 5e-8 of the partial sum per MMA, measured)
+// near 5e-8 x 192 ~ 1e-5 of the largest partial sum, even for zero-mean data
+// whose partial sums are as large as the result.
+// XC_TC_FLUSH_ROWS / XC_TC_CHUNK_ROWS override the defaults (studies).
+int flush_rows(int nkc) {
+  static const int v = env_int("XC_TC_FLUSH_ROWS", 0);
+  if (v > 0) return v;
+  return std::max(1, std::min(32, 192 / (12 * nkc)));
+}
+int chunk_rows() {
+  static int v = env_int("XC_TC_CHUNK_ROWS", 32);
+  return v;
+}
+
+// Workspace layout (each part 256-byte aligned).
+struct TcWs {
+  float* mu;        // n_left + n_right means
+  double* PL;       // n_left x (Hl+1)(Wl+1)
+  double* PR;       // n_right x (Hr+1)(Wr+1)
+  __nv_bfloat16* hi;  // n_right x Hr x pitch
+  __nv_bfloat16* lo;
+  size_t bytes;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t) {
+  const long long nr = n_right_of(pm);
+  const size_t plane = (size_t)nr * g.Hr * t.pitch;
+  size_t off = 0;
+  TcWs w;
+  char* b = reinterpret_cast<char*>(base);
+  auto take = [&](size_t bytes) {
+    char* ptr = b ? b + off : nullptr;
+    off += align256(bytes);
+    return ptr;
+  };
+  w.mu = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
+  w.PL = reinterpret_cast<double*>(take(sizeof(double) * (size_t)pm.n_left * (g.Hl + 1) * (g.Wl + 1)));
+  w.PR = reinterpret_cast<double*>(take(sizeof(double) * (size_t)nr * (g.Hr + 1) * (g.Wr + 1)));
+  w.hi = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * plane));
+  w.lo = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * plane));
+  w.bytes = off + 256;
+  return w;
+}
+
+}  // namespace
+
 size_t tc_workspace_size(const Geometry& g, const PairMap& pm) {
-  (void)g;
-  (void)pm;
-  return 0;
+  TcPlan t;
+  if (!tc_plan(g, pm, &t)) return 0;
+  return ws_layout(nullptr, g, pm, t).bytes;
 }
 
 xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
                        void* workspace, size_t ws_bytes, cudaStream_t stream) {
-  (void)left; (void)right; (void)out; (void)g; (void)pm; (void)workspace; (void)ws_bytes; (void)stream;
-  return fail(XC_ERR_UNSUPPORTED, "split-BF16 tensor-core path not built yet");
+  TcPlan t;
+  if (!tc_plan(g, pm, &t))
+    return fail(XC_ERR_UNSUPPORTED,
+                "split-BF16 tensor path supports outputs up to 512 columns and right widths up to 256");
+  const size_t need = ws_layout(nullptr, g, pm, t).bytes;
+  if (workspace == nullptr || ws_bytes < need)
+    return fail(XC_ERR_WORKSPACE, "split-BF16 path needs " + std::to_string(need) + " bytes of workspace");
+  const TcWs w = ws_layout(reinterpret_cast<void*>(((uintptr_t)workspace + 255) & ~uintptr_t(255)), g, pm, t);
+  const long long nr = n_right_of(pm);
+  const int nl = pm.n_left;
+  const uint64_t n_out = (uint64_t)((long long)(nl - 1) * pm.o_l + (long long)(pm.K - 1) * pm.o_k + 1);
+
+  // 1. per-matrix means, 2. FP64 prefix sums of the centred matrices
+  mean_kernel<<<(unsigned)(nl + nr), 256, 0, stream>>>(left, (long long)g.Hl * g.Wl, nl, right,
+                                                         (long long)g.Hr * g.Wr, w.mu);
+  XC_CUDA_TRY(cudaGetLastError());
+  prefix_kernel<<<(unsigned)nl, 256, 0, stream>>>(left, (long long)g.Hl * g.Wl, g.Hl, g.Wl, w.mu, w.PL);
+  XC_CUDA_TRY(cudaGetLastError());
+  prefix_kernel<<<(unsigned)nr, 256, 0, stream>>>(right, (long long)g.Hr * g.Wr, g.Hr, g.Wr, w.mu + nl, w.PR);
+  XC_CUDA_TRY(cudaGetLastError());
+  // 3. split of the centred right matrices
+  {
+    const long long rows = nr * g.Hr;
+    long long blocks = (rows * t.pitch + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    split_kernel<<<(unsigned)blocks, 256, 0, stream>>>(right, w.mu + nl, w.hi, w.lo, rows, g.Hr, g.Wr, t.pitch);
+    XC_CUDA_TRY(cudaGetLastError());
+  }
+  // 4. the mean terms initialise the output
+  correction_kernel<<<(unsigned)(n_out * g.Sy), 256, 0, stream>>>(out, w.PL, w.PR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr,
+                                                                  g.Wr, g.Sy, g.Sx, pm, (long long)n_out);
+  XC_CUDA_TRY(cudaGetLastError());
+
+  CUtensorMap mhi, mlo;
+  {
+    const uint64_t es = 2, mat = (uint64_t)t.pitch * g.Hr * es;
+    const uint64_t d2 = pm.r_l != 0 ? (uint64_t)pm.n_left : 1;
+    uint64_t dims[4] = {(uint64_t)t.pitch, (uint64_t)g.Hr, d2, (uint64_t)pm.K};
+    uint64_t strides[3] = {(uint64_t)t.pitch * es, mat * (uint64_t)(pm.r_l != 0 ? pm.r_l : 1), mat * (uint64_t)pm.r_k};
+    uint32_t box[4];
+    if (t.mats_mode) {
+      box[0] = 64; box[1] = 1; box[2] = 1; box[3] = (uint32_t)t.P;
+    } else {
+      box[0] = 64; box[1] = (uint32_t)t.DY; box[2] = 1; box[3] = 1;
+    }
+    if (!encode_tiled(&mhi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, w.hi, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
+      return XC_ERR_INVALID_ARGUMENT;
+    if (!encode_tiled(&mlo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, w.lo, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
+      return XC_ERR_INVALID_ARGUMENT;
+  }
+
+  TcParams prm;
+  prm.left = left;
+  prm.mu_left = w.mu;
+  prm.out = out;
+  prm.Hl = g.Hl;
+  prm.Wl = g.Wl;
+  prm.Hr = g.Hr;
+  prm.Wr = g.Wr;
+  prm.Sy = g.Sy;
+  prm.Sx = g.Sx;
+  prm.pm = pm;
+  prm.P = t.P;
+  prm.DY = t.DY;
+  prm.mats_mode = t.mats_mode;
+  prm.n_pgroups = div_up(pm.K, t.P);
+  prm.n_dytiles = div_up(g.Sy, t.DY);
+  prm.N = t.N;
+  prm.nkc = t.nkc;
+  prm.buf_len = t.buf_len;
+  prm.flush_rows = flush_rows(t.nkc);
+  prm.chunk_rows = chunk_rows();
+  prm.n_chunks = div_up(t.DY - 1 + std::min(g.Hl, g.Hr), prm.chunk_rows);
+  prm.flags = device_flags();
+
+  const long long blocks = (long long)prm.n_chunks * prm.n_dytiles * pm.n_left * prm.n_pgroups;
+  if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+  XC_CUDA_TRY(cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
+  tc_kernel<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
+  XC_CUDA_TRY(cudaGetLastError());
+  return XC_OK;
 }
 
 }  // namespace xc

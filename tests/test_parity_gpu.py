@@ -194,8 +194,9 @@ def test_fft_glue_launchers():
     lt = (rng.standard_normal((2, 6)) + 1j * rng.standard_normal((2, 6))).astype(np.complex64)
     rt = (rng.standard_normal((3, 6)) + 1j * rng.standard_normal((3, 6))).astype(np.complex64)
     o = torch.zeros((2, 3, 6), dtype=torch.complex64, device="cuda")
-    xcorr.check(L.xc_run_hadamard_n_to_m_over_output_c64(torch.as_tensor(lt).cuda().data_ptr(),
-                                                         torch.as_tensor(rt).cuda().data_ptr(), o.data_ptr(),
+    d_lt = torch.as_tensor(lt).cuda()
+    d_rt = torch.as_tensor(rt).cuda()
+    xcorr.check(L.xc_run_hadamard_n_to_m_over_output_c64(d_lt.data_ptr(), d_rt.data_ptr(), o.data_ptr(),
                                                          xcorr.size2(2, 3), 2, 3, 256, 1, st))
     torch.cuda.synchronize()
     np.testing.assert_allclose(o.cpu().numpy(), lt[:, None, :] * np.conj(rt[None, :, :]), rtol=1e-6, atol=1e-6)

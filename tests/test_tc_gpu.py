@@ -1,0 +1,72 @@
+"""Split-BF16 tensor-core path (tcgen05) against the oracle.
+
+Tolerance: max|out - oracle64| / max|oracle64| <= 1e-5 per output matrix,
+the accuracy gate of the headline metric.
+"""
+import numpy as np
+import pytest
+
+from helpers import VALID, golden_case, rel_to_max, seeded
+from oracle import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import xcorr  # noqa: E402
+
+
+def dev(a):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+
+
+def run_tc(mode, left, right):
+    out = xcorr.correlate(mode, dev(left), dev(right), method="tc_bf16x3")
+    torch.cuda.synchronize()
+    xcorr.check(xcorr.lib().xc_device_check(0))
+    return out.cpu().numpy()
+
+
+TC_SHAPES = [
+    # (mode, n_left, n_right, left, right, dist) -- partners per tile P = 1, 2, 4 use
+    # one TMA box per partner; P >= 8 one box per row shift
+    ("one_to_one", 1, 1, (17, 17), (17, 17), "uniform"),
+    ("one_to_many", 1, 2, (20, 24), (20, 24), "normal"),
+    ("one_to_many", 1, 4, (33, 40), (12, 9), "uniform"),
+    ("n_to_mn", 2, 6, (19, 19), (19, 19), "normal"),
+    ("one_to_many", 1, 9, (64, 64), (64, 64), "uniform"),
+    ("n_to_m", 2, 16, (30, 70), (30, 66), "signed"),
+    ("one_to_many", 1, 64, (40, 48), (40, 48), "uniform"),
+]
+
+
+@pytest.mark.parametrize("shape", TC_SHAPES, ids=[f"{s[0]}-{s[1]}x{s[2]}-{s[3]}-{s[4]}" for s in TC_SHAPES])
+def test_tc_matches_oracle(shape):
+    mode, n, m, ls, rs, dist = shape
+    left = seeded((n,) + ls, 300 + n, dist)
+    right = seeded((m,) + rs, 400 + m, dist)
+    ref = oracle.run_mode(mode, left, right, dtype="f32acc64", threads=8)
+    out = run_tc(mode, left, right)
+    assert out.shape == ref.shape
+    assert rel_to_max(out, ref) <= 1e-5
+
+
+@pytest.mark.parametrize("name", [v for v in VALID if "_10_10_" in v or "_64_64_" in v])
+def test_tc_golden(name):
+    mode, left, right, valid = golden_case(name)
+    out = run_tc(mode, left.astype(np.float32), right.astype(np.float32))
+    assert rel_to_max(out, valid) <= 1e-5
+
+
+def test_tc_bench_shape_accuracy():
+    """The benchmark's shape (256x256, 64 right matrices) on 8 of them."""
+    left = seeded((1, 256, 256), 2)
+    right = seeded((8, 256, 256), 3)
+    ref = oracle.run_mode("one_to_many", left, right, dtype="f32acc64", threads=16)
+    out = run_tc("one_to_many", left, right)
+    assert rel_to_max(out, ref) <= 1e-5
+
+
+def test_tc_rejects_unsupported_sizes():
+    with pytest.raises(xcorr.XcError) as e:
+        xcorr.correlate("one_to_one", dev(seeded((1, 8, 300), 1)), dev(seeded((1, 8, 300), 2)), method="tc_bf16x3")
+    assert e.value.status == 4
