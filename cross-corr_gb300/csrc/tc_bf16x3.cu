@@ -49,6 +49,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 #include <string>
 
 #include "xc_common.cuh"
@@ -701,4 +702,67 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   return XC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the split-BF16 path.
+//
+// Some callers cannot call cudaMalloc: hosts that hand a library a fixed
+// device-memory budget or their own pool (and forbid raw allocations), and
+// latency-critical loops where cudaMalloc/cudaFree may stall or synchronise
+// the device.  xc_correlate_tc_noalloc serves them with the scratch of this
+// path (means, FP64 prefix sums, BF16 planes) in the file-scope array below,
+// of fixed size XC_TC_NOALLOC_SCRATCH_BYTES.  Every GPU that loads the library
+// holds that array until the process exits.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_tc_noalloc_scratch[XC_TC_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of the scratch array for the current device, looked up once
+// per device (with that device current) and cached.
+xc_status noalloc_scratch(void** ptr) {
+  int dev = 0;
+  XC_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(XC_ERR_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    XC_CUDA_TRY(cudaGetSymbolAddress(&p, g_tc_noalloc_scratch));
+    g_noalloc_ptr[dev] = p;
+  }
+  *ptr = g_noalloc_ptr[dev];
+  return XC_OK;
+}
+}  // namespace
+
 }  // namespace xc
+
+extern "C" xc_status xc_correlate_tc_noalloc(xc_mode mode, const float* d_left, xc_size2 left, uint32_t n_left,
+                                             const float* d_right, xc_size2 right, uint32_t n_right, float* d_out,
+                                             void* stream) {
+  using namespace xc;
+  if (d_left == nullptr || d_right == nullptr || d_out == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL device buffer");
+  if (left.x == 0 || left.y == 0 || right.x == 0 || right.y == 0)
+    return fail(XC_ERR_INVALID_ARGUMENT, "matrix sizes must be positive");
+  PairMap pm;
+  uint64_t n_out = 0;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out))
+    return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts for the mode");
+  const Geometry g = make_geometry(left, right);
+  TcPlan t;
+  if (!tc_plan(g, pm, &t))
+    return fail(XC_ERR_UNSUPPORTED,
+                "split-BF16 tensor path supports outputs up to 512 columns and right widths up to 256");
+  const size_t need = ws_layout(nullptr, g, pm, t).bytes;
+  if (need > (size_t)XC_TC_NOALLOC_SCRATCH_BYTES)
+    return fail(XC_ERR_WORKSPACE, "xc_correlate_tc_noalloc: this problem needs " + std::to_string(need) +
+                                      " bytes of scratch, more than the fixed " +
+                                      std::to_string((size_t)XC_TC_NOALLOC_SCRATCH_BYTES) +
+                                      " bytes; use xc_correlate with a caller-owned workspace");
+  void* scratch = nullptr;
+  XC_TRY(noalloc_scratch(&scratch));
+  return tc_correlate(d_left, d_right, d_out, g, pm, scratch, (size_t)XC_TC_NOALLOC_SCRATCH_BYTES,
+                      reinterpret_cast<cudaStream_t>(stream));
+}

@@ -32,7 +32,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "cuFFT error", 4: 
 # Every symbol declared in include/xcorr.h (checked by the CPU test suite).
 EXPORTED = [
     "xc_version", "xc_status_string", "xc_last_error", "xc_device_check", "xc_output_count", "xc_output_size",
-    "xc_workspace_size", "xc_correlate", "xc_correlate_host", "xc_release_thread_cache",
+    "xc_workspace_size", "xc_correlate", "xc_correlate_host", "xc_release_thread_cache", "xc_correlate_tc_noalloc",
     "xc_fft_plan_create", "xc_fft_plan_workspace_size", "xc_fft_plan_pad_size", "xc_fft_execute",
     "xc_fft_forward", "xc_fft_multiply", "xc_fft_inverse", "xc_fft_plan_destroy",
     "xc_run_ccn_shuffle_f32", "xc_run_ccn_shuffle_f64",
@@ -89,6 +89,7 @@ def lib():
         L.xc_correlate.argtypes = [i, i, i, vp, Size2, u32, vp, Size2, u32, vp, vp, sz, vp]
         L.xc_correlate_host.argtypes = [i, i, i, vp, Size2, u32, vp, Size2, u32, vp, vp]
         L.xc_release_thread_cache.restype = None
+        L.xc_correlate_tc_noalloc.argtypes = [i, vp, Size2, u32, vp, Size2, u32, vp, vp]
         L.xc_fft_plan_create.argtypes = [c.POINTER(vp), i, i, Size2, u32, Size2, u32, Size2]
         L.xc_fft_plan_workspace_size.argtypes = [vp, c.POINTER(sz)]
         L.xc_fft_plan_pad_size.argtypes = [vp, c.POINTER(Size2)]

@@ -117,6 +117,33 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
 void xc_release_thread_cache(void);
 
 /* ------------------------------------------------------------------------ */
+/* Allocation-free split-BF16 correlation.  No counterpart in the reference. */
+/* ------------------------------------------------------------------------ */
+/* Size of the fixed scratch array xc_correlate_tc_noalloc works in (64 MiB).
+ * Every GPU that loads this library holds it until the process exits. */
+#define XC_TC_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+/* Same result as xc_correlate(mode, XC_F32, XC_METHOD_TC_BF16X3, ...), for
+ * callers that must not allocate device memory: hosts that own the device
+ * memory budget (a fixed arena or their own pool, no raw cudaMalloc) and
+ * latency-critical loops where cudaMalloc/cudaFree may block or synchronise
+ * the device.  Instead of a caller workspace it uses one file-scope device
+ * array of XC_TC_NOALLOC_SCRATCH_BYTES per GPU; it calls no cudaMalloc,
+ * cudaFree or allocating library routine.
+ *  - The first call on a device looks up that array's device address (with
+ *    the device current) and caches it; make that first call before any
+ *    stream capture.
+ *  - Problems whose scratch exceeds the array are rejected with
+ *    XC_ERR_WORKSPACE and a message giving both sizes.  (The 256x256 x 64
+ *    one_to_many problem needs about 51 MB.)
+ *  - All calls on a device share the array and nothing in it needs to start
+ *    at zero; calls whose work overlaps on the GPU (different streams, or
+ *    different host threads on one device) race on it and must be ordered by
+ *    the caller. */
+xc_status xc_correlate_tc_noalloc(xc_mode mode, const float* d_left, xc_size2 left, uint32_t n_left,
+                                  const float* d_right, xc_size2 right, uint32_t n_right, float* d_out,
+                                  void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* FFT pipeline with explicit plans (replaces the cufftPlanMany/exec calls  */
 /* and the host-side normalisation of the fft_* plug-ins:                   */
 /* src/one_to_one.hpp:925-990, src/one_to_many.hpp:538-587,                 */
