@@ -62,9 +62,10 @@ namespace {
 constexpr int kStages = 4;          // right-row tile pipeline depth
 constexpr int kTileBytes = 128 * 128;  // 128 rows x 64 bf16 (one plane)
 constexpr int kStageBytes = 2 * kTileBytes;
-constexpr int kThreads = 256;
-constexpr int kStgPitch = 65;       // epilogue staging row pitch (floats)
-// 15 mbarriers (120 B), the abort flag and the TMEM address slot
+constexpr int kEpiWarps = 8;        // epilogue warps (2 per TMEM lane quadrant)
+constexpr int kThreads = 32 * (4 + kEpiWarps);
+constexpr int kMaxLeftCols = 512;   // staged centred left row (Sx <= 512 on this path)
+// 17 mbarriers (136 B), the abort flag and the TMEM address slot
 constexpr int kBarBytes = 256;
 
 struct TcParams {
@@ -125,13 +126,16 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
 #pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -152,6 +156,20 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
   return false;
 }
 
+// OR-reduction over the threads of named barrier `id` (also a barrier).
+__device__ __forceinline__ bool bar_red_or(bool v, int id, int nthreads) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, %2, %3, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(nthreads)
+      : "memory");
+  return r != 0;
+}
+
 // dy-tile visiting order: centre (heaviest overlap) first, then alternating
 // outwards, so long tiles start early.
 __device__ __forceinline__ int centre_out(int r, int n, int tc) {
@@ -163,34 +181,39 @@ __device__ __forceinline__ int centre_out(int r, int n, int tc) {
   return above > below ? tc + m + extra : tc - m - extra;
 }
 
+template <int N>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
               const TcParams p) {
+  constexpr int kPhases = 4;            // column phases handled by this CTA
+  constexpr int kDCols = kPhases * N;   // TMEM columns of one accumulator buffer
+  constexpr int kAcc = 2 * N;           // accumulators per epilogue thread (2 phases)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* a_tiles = smem;                                   // kStages x (hi, lo) x 16 KB
-  __nv_bfloat16* b_bufs = reinterpret_cast<__nv_bfloat16*>(smem + kStages * kStageBytes);  // 2 x 8 x 2 x buf_len
-  const int b_slot_elems = 16 * p.buf_len;
-  float* stg = reinterpret_cast<float*>(b_bufs + 2 * b_slot_elems);  // 4 warps x 32 x kStgPitch
-  uint64_t* bars = reinterpret_cast<uint64_t*>(stg + 4 * 32 * kStgPitch);
+  unsigned char* a_tiles = smem;  // kStages x (hi, lo) x 16 KB
+  __nv_bfloat16* b_bufs = reinterpret_cast<__nv_bfloat16*>(smem + kStages * kStageBytes);
+  const int b_slot_elems = kPhases * 2 * p.buf_len;  // 4 phases x (hi, lo) per slot
+  float* lrows = reinterpret_cast<float*>(b_bufs + 2 * b_slot_elems);  // 2 x kMaxLeftCols
+  uint64_t* bars = reinterpret_cast<uint64_t*>(lrows + 2 * kMaxLeftCols);
   uint64_t* a_full = bars;
   uint64_t* a_empty = bars + kStages;
   uint64_t* b_full = bars + 2 * kStages;
   uint64_t* b_empty = b_full + 2;
-  uint64_t* t_full = b_empty + 2;
-  uint64_t* t_empty = t_full + 1;
-  uint64_t* mma_done = t_empty + 1;
+  uint64_t* t_full = b_empty + 2;   // [2]
+  uint64_t* t_empty = t_full + 2;   // [2]
+  uint64_t* mma_done = t_empty + 2;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 1);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 2);
 
-  // ---- tile of this CTA -------------------------------------------------
-  // blockIdx = (chunk * n_dytiles + rank) * per_rank + lp: all first chunks
-  // (centre tiles first) before any second chunk.
+  // ---- work item of this CTA ---------------------------------------------
+  // blockIdx = ((chunk * n_dytiles + rank) * per_rank + lp) * 2 + half
+  const int half = blockIdx.x & 1;
+  const int bid = blockIdx.x >> 1;
   const int per_rank = p.pm.n_left * p.n_pgroups;
-  const int lp = blockIdx.x % per_rank;
-  const int rank = (blockIdx.x / per_rank) % p.n_dytiles;
-  const int chunk = blockIdx.x / (per_rank * p.n_dytiles);
+  const int lp = bid % per_rank;
+  const int rank = (bid / per_rank) % p.n_dytiles;
+  const int chunk = bid / (per_rank * p.n_dytiles);
   const int l = lp / p.n_pgroups;
   const int p0 = (lp % p.n_pgroups) * p.P;
   const int t = centre_out(rank, p.n_dytiles, (p.Hr - 1) / p.DY);
@@ -203,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (n_rows <= 0) return;  // uniform over the CTA
   const int n_drains = (n_rows + p.flush_rows - 1) / p.flush_rows;
   const int rdim2 = p.pm.r_l != 0 ? l : 0;
-  const uint32_t ncols = 8u * (uint32_t)p.N <= 32 ? 32u : (8u * p.N <= 64 ? 64u : (8u * p.N <= 128 ? 128u : (8u * p.N <= 256 ? 256u : 512u)));
+  constexpr uint32_t ncols = 2 * kDCols <= 32 ? 32u : (2 * kDCols <= 64 ? 64u : (2 * kDCols <= 128 ? 128u : (2 * kDCols <= 256 ? 256u : 512u)));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -215,9 +238,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int s = 0; s < 2; ++s) {
       mbar_init(&b_full[s], 64);
       mbar_init(&b_empty[s], 1);
+      mbar_init(&t_full[s], 1);
+      mbar_init(&t_empty[s], 32 * kEpiWarps);
     }
-    mbar_init(t_full, 1);
-    mbar_init(t_empty, 128);
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     fence_mbar_init();
@@ -267,7 +290,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       if (!ok) {
-        // let the copies already issued land before the CTA exits
         for (int q = max(0, it - kStages); q < it; ++q)
           mbar_wait_bounded(&a_full[q % kStages], (q / kStages) & 1, 1u << 16);
       }
@@ -275,20 +297,29 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(128, p.N);
+      const uint32_t idesc = idesc_bf16_f32(128, N);
       const uint32_t a_base = smem_u32(a_tiles);
       const uint32_t b_base = smem_u32(b_bufs);
       const uint32_t copy_bytes = (uint32_t)p.buf_len * 2;
-      int it = 0, drain = 0;
-      bool first = true, ok = true;
+      int it = 0, buf = 0, rows_in = 0;
+      uint32_t uses[2] = {0u, 0u};
+      bool ok = true;
       for (int ai = 0; ai < n_rows && ok; ++ai) {
         const int bs = ai & 1;
         if (!wait_or_abort(&b_full[bs], (ai >> 1) & 1, abort_flag, p.flags, 12)) {
           ok = false;
           break;
         }
+        if (rows_in == 0) {
+          // the epilogue must have drained this buffer's previous use
+          if (!wait_or_abort(&t_empty[buf], (uses[buf] & 1) ^ 1, abort_flag, p.flags, 14)) {
+            ok = false;
+            break;
+          }
+        }
         tc_fence_after();
         const uint32_t bslot = b_base + (uint32_t)bs * (uint32_t)b_slot_elems * 2;
+        const uint32_t dbase = tmem_base + (uint32_t)(buf * kDCols);
         for (int kc = 0; kc < p.nkc; ++kc, ++it) {
           const int s = it % kStages;
           if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13)) {
@@ -303,13 +334,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t ahi = smem_desc(a_hi_addr + ks * 32, 16, 1024, 2);
             const uint64_t alo = smem_desc(a_lo_addr + ks * 32, 16, 1024, 2);
             const uint32_t koff = (uint32_t)(kc * 64 + ks * 16) * 2;
-            const uint32_t acc0 = (first && kc == 0 && ks == 0) ? 0u : 1u;
-#pragma unroll 1
-            for (int c = 0; c < 8; ++c) {
+            const uint32_t acc0 = (rows_in == 0 && kc == 0 && ks == 0) ? 0u : 1u;
+#pragma unroll
+            for (int c = 0; c < kPhases; ++c) {
               const uint32_t bhi_addr = bslot + (uint32_t)c * 2 * copy_bytes + koff;
               const uint64_t bhi = smem_desc(bhi_addr, 16, 128, 0);
               const uint64_t blo = smem_desc(bhi_addr + copy_bytes, 16, 128, 0);
-              const uint32_t d = tmem_base + (uint32_t)(c * p.N);
+              const uint32_t d = dbase + (uint32_t)(c * N);
               mma_bf16(d, ahi, bhi, idesc, acc0);
               mma_bf16(d, ahi, blo, idesc, 1u);
               mma_bf16(d, alo, bhi, idesc, 1u);
@@ -319,16 +350,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (!ok) break;
         mma_commit(&b_empty[bs]);
-        first = false;
-        if ((ai + 1) % p.flush_rows == 0 || ai == n_rows - 1) {
-          mma_commit(t_full);
-          if (!wait_or_abort(t_empty, drain & 1, abort_flag, p.flags, 14)) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          ++drain;
-          first = true;
+        ++rows_in;
+        if (rows_in == p.flush_rows || ai == n_rows - 1) {
+          mma_commit(&t_full[buf]);
+          ++uses[buf];
+          buf ^= 1;
+          rows_in = 0;
         }
       }
       // All MMAs issued by this thread must finish before TMEM is released.
@@ -343,23 +370,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int nvec = p.buf_len / 8;
     for (int ai = 0; ai < n_rows; ++ai) {
       const int bs = ai & 1;
-      if (!wait_or_abort(&b_empty[bs], ((ai >> 1) & 1) ^ 1, abort_flag, p.flags, 15)) break;
-      const float* lrow = lrow_base + (long long)(a_lo + ai) * p.Wl;
+      const bool ok = wait_or_abort(&b_empty[bs], ((ai >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
+      // the 64 builder threads leave together (they share a named barrier)
+      if (bar_red_or(!ok, 1, 64)) break;
+      // stage the centred left row (coalesced), then build the phase copies
+      float* lr = lrows + bs * kMaxLeftCols;
+      const float* src = lrow_base + (long long)(a_lo + ai) * p.Wl;
+      for (int x = bt; x < p.Wl; x += 64) lr[x] = __ldg(src + x) - mu;
+      asm volatile("bar.sync 1, 64;" ::: "memory");
       __nv_bfloat16* slot = b_bufs + bs * b_slot_elems;
-      for (int item = bt; item < 8 * nvec; item += 64) {
-        const int c = item / nvec, jv = item % nvec;
+      for (int item = bt; item < kPhases * nvec; item += 64) {
+        const int cl = item / nvec, jv = item % nvec;
+        const int c = half * kPhases + cl;
         const int j0 = jv * 8 + c - (p.Wr - 1);  // left column of element 0
         __align__(16) __nv_bfloat16 hi[8];
         __align__(16) __nv_bfloat16 lo[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
           const int x = j0 + e;
-          const float v = (x >= 0 && x < p.Wl) ? __ldg(lrow + x) - mu : 0.0f;
+          const float v = (x >= 0 && x < p.Wl) ? lr[x] : 0.0f;
           const __nv_bfloat16 h = __float2bfloat16_rn(v);
           hi[e] = h;
           lo[e] = __float2bfloat16_rn(v - __bfloat162float(h));
         }
-        __nv_bfloat16* dst = slot + (c * 2) * p.buf_len + jv * 8;
+        __nv_bfloat16* dst = slot + (cl * 2) * p.buf_len + jv * 8;
         *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(hi);
         *reinterpret_cast<uint4*>(dst + p.buf_len) = *reinterpret_cast<const uint4*>(lo);
       }
@@ -368,47 +402,55 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp & 3;  // TMEM lane quadrant of this warp
-    float* st = stg + q * 32 * kStgPitch;
+    // warps 4..11: lane quadrant q, column half e (phases 2e, 2e+1 of 4)
+    const int q = warp & 3;
+    const int e = (warp - 4) >> 2;
+    float acc[kAcc];
+#pragma unroll
+    for (int i = 0; i < kAcc; ++i) acc[i] = 0.0f;
+    bool ok = true;
     for (int d = 0; d < n_drains; ++d) {
-      if (!wait_or_abort(t_full, d & 1, abort_flag, p.flags, 16)) break;
+      const int b = d & 1;
+      if (!wait_or_abort(&t_full[b], (d >> 1) & 1, abort_flag, p.flags, 16)) {
+        ok = false;
+        break;
+      }
       tc_fence_after();
-      for (int n0 = 0; n0 < p.N; n0 += 8) {
-        float v[8][8];
+      const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kDCols + e * kAcc);
 #pragma unroll
-        for (int c = 0; c < 8; ++c) tmem_ld8(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * p.N + n0), v[c]);
+      for (int j = 0; j < kAcc / 16; ++j) {
+        float v[16];
+        tmem_ld16(col0 + (uint32_t)(16 * j), v);
         tmem_wait_ld();
-        // this thread's row: sx = 8*(n0 + j) + c
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-#pragma unroll
-          for (int c = 0; c < 8; ++c) st[lane * kStgPitch + j * 8 + c] = v[c][j];
-        __syncwarp();
-        // coalesced read-add-write of the 32 rows, 64 columns each
-        for (int r = 0; r < 32; ++r) {
-          const int mr = q * 32 + r;
-          int rp, rdy;
-          if (p.mats_mode) {
-            rp = mr % p.P;
-            rdy = dy0 + mr / p.P;
-          } else {
-            rp = mr / p.DY;
-            rdy = dy0 + (p.DY - 1) - (mr % p.DY);
-          }
-          const int rk = p0 + rp, rsy = rdy + p.Hr - 1;
-          if (rk >= p.pm.K || rsy < 0 || rsy >= p.Sy) continue;
-          float* orow = p.out + ((long long)l * p.pm.o_l + (long long)rk * p.pm.o_k) * p.Sy * p.Sx +
-                        (long long)rsy * p.Sx + 8 * n0;
-#pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            const int col = lane + 32 * h;
-            if (8 * n0 + col < p.Sx) red_add(orow + col, st[r * kStgPitch + col]);
-          }
-        }
-        __syncwarp();
+        for (int i = 0; i < 16; ++i) acc[16 * j + i] += v[i];
       }
       tc_fence_before();
-      mbar_arrive(t_empty);
+      mbar_arrive(&t_empty[b]);
+    }
+    if (ok) {
+      const int m = q * 32 + lane;
+      int pp, dy;
+      if (p.mats_mode) {
+        pp = m % p.P;
+        dy = dy0 + m / p.P;
+      } else {
+        pp = m / p.DY;
+        dy = dy0 + (p.DY - 1) - (m % p.DY);
+      }
+      const int k = p0 + pp, sy = dy + p.Hr - 1;
+      if (k < p.pm.K && sy >= 0 && sy < p.Sy) {
+        float* orow = p.out + ((long long)l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy * p.Sx + (long long)sy * p.Sx;
+        const int c0 = half * kPhases + 2 * e;
+#pragma unroll
+        for (int n = 0; n < N; ++n) {
+#pragma unroll
+          for (int cc = 0; cc < 2; ++cc) {
+            const int sx = c0 + cc + 8 * n;
+            if (sx < p.Sx) red_add(orow + sx, acc[cc * N + n]);
+          }
+        }
+      }
     }
   }
 
@@ -439,32 +481,49 @@ __global__ void mean_kernel(const float* __restrict__ left, long long left_area,
   }
 }
 
-// 2D prefix sums (FP64) of the centred matrices fl32(x - mu): P[y][x] =
-// sum_{i<y, j<x}, (H+1) x (W+1) per matrix.  One block per matrix: rows are
-// scanned by threads, then columns.
-__global__ void prefix_kernel(const float* __restrict__ src, long long stride, int H, int W,
-                              const float* __restrict__ mu, double* __restrict__ P) {
-  const int m = blockIdx.x;
-  const float* a = src + (long long)m * stride;
-  const float mv = mu[m];
-  double* q = P + (long long)m * (H + 1) * (W + 1);
-  for (int x = threadIdx.x; x <= W; x += blockDim.x) q[x] = 0.0;
-  for (int y = threadIdx.x; y < H; y += blockDim.x) {
-    double acc = 0.0;
-    double* row = q + (long long)(y + 1) * (W + 1);
-    row[0] = 0.0;
-    for (int x = 0; x < W; ++x) {
-      acc += (double)(a[(long long)y * W + x] - mv);
-      row[x + 1] = acc;
-    }
+// 2D prefix sums (FP64) of the centred matrices fl32(x - mu):
+// P[y][x] = sum_{i<y, j<x}, (H+1) x (W+1) per matrix.  Pass 1: one warp per
+// row scans it (warp shuffles); pass 2: one thread per column accumulates
+// down the rows.
+__global__ void prefix_rows_kernel(const float* __restrict__ src, int n_mats, int H, int W,
+                                   const float* __restrict__ mu, double* __restrict__ P) {
+  const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;  // (matrix, y) with y in [0, H]
+  const int lane = threadIdx.x & 31;
+  if (gw >= (long long)n_mats * (H + 1)) return;
+  const int m = (int)(gw / (H + 1));
+  const int y = (int)(gw % (H + 1));
+  double* row = P + ((long long)m * (H + 1) + y) * (W + 1);
+  if (y == 0) {
+    for (int x = lane; x <= W; x += 32) row[x] = 0.0;
+    return;
   }
-  __syncthreads();
-  for (int x = threadIdx.x; x <= W; x += blockDim.x) {
-    double acc = 0.0;
-    for (int y = 1; y <= H; ++y) {
-      acc += q[(long long)y * (W + 1) + x];
-      q[(long long)y * (W + 1) + x] = acc;
+  const float* a = src + ((long long)m * H + (y - 1)) * W;
+  const float mv = mu[m];
+  if (lane == 0) row[0] = 0.0;
+  double carry = 0.0;
+  for (int x0 = 0; x0 < W; x0 += 32) {
+    const int x = x0 + lane;
+    double v = x < W ? (double)(a[x] - mv) : 0.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
     }
+    if (x < W) row[x + 1] = carry + v;
+    carry += __shfl_sync(0xffffffffu, v, 31);
+  }
+}
+
+__global__ void prefix_cols_kernel(int n_mats, int H, int W, double* __restrict__ P) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= (long long)n_mats * (W + 1)) return;
+  const int m = (int)(t / (W + 1));
+  const int x = (int)(t % (W + 1));
+  double* q = P + (long long)m * (H + 1) * (W + 1) + x;
+  double acc = 0.0;
+  for (int y = 1; y <= H; ++y) {
+    acc += q[(long long)y * (W + 1)];
+    q[(long long)y * (W + 1)] = acc;
   }
 }
 
@@ -486,11 +545,15 @@ __global__ void split_kernel(const float* __restrict__ src, const float* __restr
 }
 
 // out[o][sy][sx] = mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area over the
-// overlap of shift (sy, sx); one block per output row.
+// overlap of shift (sy, sx); one block per output row.  The row band sums
+// Q[x] = P[y1][x] - P[y0][x] of both matrices are formed once per row in
+// shared memory (FP64); per element only the two band differences are FP64
+// and the products are FP32 (their rounding is ~6e-8 of max|out|).
 __global__ void correction_kernel(float* __restrict__ out, const double* __restrict__ PL,
                                   const double* __restrict__ PR, const float* __restrict__ mu_l,
                                   const float* __restrict__ mu_r, int Hl, int Wl, int Hr, int Wr, int Sy, int Sx,
-                                  PairMap pm, long long n_out) {
+                                  PairMap pm) {
+  extern __shared__ double qs[];  // (Wl + 1) + (Wr + 1)
   const long long row = blockIdx.x;  // o * Sy + sy
   const long long o = row / Sy;
   const int sy = (int)(row % Sy);
@@ -507,22 +570,27 @@ __global__ void correction_kernel(float* __restrict__ out, const double* __restr
     k = o / pm.n_left;
   }
   const long long r = l * pm.r_l + k * pm.r_k;
-  (void)n_out;
   const int dy = sy - (Hr - 1);
   const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
-  const double ml = mu_l[l], mr = mu_r[r];
   const double* pl0 = PL + (l * (Hl + 1) + y0) * (long long)(Wl + 1);
   const double* pl1 = PL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
   const double* pr0 = PR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
   const double* pr1 = PR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
+  double* ql = qs;
+  double* qr = qs + (Wl + 1);
+  for (int x = threadIdx.x; x <= Wl; x += blockDim.x) ql[x] = pl1[x] - pl0[x];
+  for (int x = threadIdx.x; x <= Wr; x += blockDim.x) qr[x] = pr1[x] - pr0[x];
+  __syncthreads();
+  const float ml = mu_l[l], mr = mu_r[r];
+  const float mlr = ml * mr;
+  const float rows = (float)(y1 - y0);
   float* orow = out + row * Sx;
   for (int sx = threadIdx.x; sx < Sx; sx += blockDim.x) {
     const int dx = sx - (Wr - 1);
     const int x0 = max(0, dx), x1 = min(Wl, Wr + dx);
-    const double sl = pl1[x1] - pl0[x1] - pl1[x0] + pl0[x0];
-    const double sr = pr1[x1 - dx] - pr0[x1 - dx] - pr1[x0 - dx] + pr0[x0 - dx];
-    const double cnt = (double)(y1 - y0) * (double)(x1 - x0);
-    orow[sx] = (float)(mr * sl + ml * sr + ml * mr * cnt);
+    const float sl = (float)(ql[x1] - ql[x0]);
+    const float sr = (float)(qr[x1 - dx] - qr[x0 - dx]);
+    orow[sx] = fmaf(mr, sl, fmaf(ml, sr, mlr * (rows * (float)(x1 - x0))));
   }
 }
 
@@ -545,7 +613,7 @@ bool tc_plan(const Geometry& g, const PairMap& pm, TcPlan* t) {
   t->nkc = (g.Wr + 63) / 64;
   t->buf_len = t->nkc * 64 + 8 * N;
   t->pitch = (g.Wr + 7) / 8 * 8;
-  t->smem_bytes = 1024 + kStages * kStageBytes + 2 * 16 * t->buf_len * 2 + 4 * 32 * kStgPitch * 4 + kBarBytes;
+  t->smem_bytes = 1024 + kStages * kStageBytes + 2 * 4 * 2 * t->buf_len * 2 + 2 * kMaxLeftCols * 4 + kBarBytes;
   return t->smem_bytes <= 227 * 1024;
 }
 
@@ -635,10 +703,19 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   mean_kernel<<<(unsigned)(nl + nr), 256, 0, stream>>>(left, (long long)g.Hl * g.Wl, nl, right,
                                                          (long long)g.Hr * g.Wr, w.mu);
   XC_CUDA_TRY(cudaGetLastError());
-  prefix_kernel<<<(unsigned)nl, 256, 0, stream>>>(left, (long long)g.Hl * g.Wl, g.Hl, g.Wl, w.mu, w.PL);
-  XC_CUDA_TRY(cudaGetLastError());
-  prefix_kernel<<<(unsigned)nr, 256, 0, stream>>>(right, (long long)g.Hr * g.Wr, g.Hr, g.Wr, w.mu + nl, w.PR);
-  XC_CUDA_TRY(cudaGetLastError());
+  {
+    auto prefix = [&](const float* src, int n, int H, int W, const float* mu, double* P) -> xc_status {
+      const long long warps = (long long)n * (H + 1);
+      prefix_rows_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, stream>>>(src, n, H, W, mu, P);
+      XC_CUDA_TRY(cudaGetLastError());
+      const long long cols = (long long)n * (W + 1);
+      prefix_cols_kernel<<<(unsigned)((cols + 255) / 256), 256, 0, stream>>>(n, H, W, P);
+      XC_CUDA_TRY(cudaGetLastError());
+      return XC_OK;
+    };
+    XC_TRY(prefix(left, nl, g.Hl, g.Wl, w.mu, w.PL));
+    XC_TRY(prefix(right, (int)nr, g.Hr, g.Wr, w.mu + nl, w.PR));
+  }
   // 3. split of the centred right matrices
   {
     const long long rows = nr * g.Hr;
@@ -648,8 +725,8 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
     XC_CUDA_TRY(cudaGetLastError());
   }
   // 4. the mean terms initialise the output
-  correction_kernel<<<(unsigned)(n_out * g.Sy), 256, 0, stream>>>(out, w.PL, w.PR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr,
-                                                                  g.Wr, g.Sy, g.Sx, pm, (long long)n_out);
+  correction_kernel<<<(unsigned)(n_out * g.Sy), 256, sizeof(double) * (g.Wl + g.Wr + 2), stream>>>(
+      out, w.PL, w.PR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, pm);
   XC_CUDA_TRY(cudaGetLastError());
 
   CUtensorMap mhi, mlo;
@@ -694,12 +771,20 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.n_chunks = div_up(t.DY - 1 + std::min(g.Hl, g.Hr), prm.chunk_rows);
   prm.flags = device_flags();
 
-  const long long blocks = (long long)prm.n_chunks * prm.n_dytiles * pm.n_left * prm.n_pgroups;
+  const long long blocks = 2LL * prm.n_chunks * prm.n_dytiles * pm.n_left * prm.n_pgroups;
   if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
-  XC_CUDA_TRY(cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
-  tc_kernel<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
-  XC_CUDA_TRY(cudaGetLastError());
-  return XC_OK;
+  auto launch = [&](auto kern) -> xc_status {
+    XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
+    kern<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
+    XC_CUDA_TRY(cudaGetLastError());
+    return XC_OK;
+  };
+  switch (t.N) {
+    case 16: return launch(tc_kernel<16>);
+    case 32: return launch(tc_kernel<32>);
+    case 48: return launch(tc_kernel<48>);
+    default: return launch(tc_kernel<64>);
+  }
 }
 
 // ---------------------------------------------------------------------------
