@@ -153,6 +153,13 @@ xc_status xc_device_check(int device) {
   return XC_OK;
 }
 
+xc_status xc_check_device(void* stream) { return check_device_flags(as_stream(stream)); }
+
+xc_status xc_debug_expire_wait(uint32_t polls, void* stream) {
+  if (polls == 0 || polls > (1u << 24)) return fail(XC_ERR_INVALID_ARGUMENT, "polls must be in [1, 2^24]");
+  return debug_expire_wait(polls, as_stream(stream));
+}
+
 xc_status xc_output_count(xc_mode mode, uint32_t n_left, uint32_t n_right, uint64_t* n_out) {
   PairMap pm;
   if (n_out == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "n_out is NULL");

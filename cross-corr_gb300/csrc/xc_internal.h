@@ -39,6 +39,8 @@ inline Geometry make_geometry(xc_size2 left, xc_size2 right) {
   return g;
 }
 
+xc_status debug_expire_wait(uint32_t polls, cudaStream_t stream);
+
 // Plain definition-based correlation (direct_simt.cu).
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
                         const PairMap& pm, cudaStream_t stream, int force_loader /* -1 auto, 0 cp.async, 1 TMA */);

@@ -112,6 +112,28 @@ xc_status check_device_flags(cudaStream_t stream) {
 }
 
 // ---------------------------------------------------------------------------
+// Bounded-wait test hook: an mbarrier with one expected arrival that never
+// comes; the wait gives up after `polls` polls and records site 99.
+// ---------------------------------------------------------------------------
+__global__ void expire_wait_kernel(DeviceFlags* flags, uint32_t polls) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !mbar_wait_bounded(&bar, 0, polls)) record_timeout(flags, 99);
+}
+
+xc_status debug_expire_wait(uint32_t polls, cudaStream_t stream) {
+  DeviceFlags* f = device_flags();
+  if (f == nullptr) return fail(XC_ERR_CUDA, "device flag word unavailable");
+  expire_wait_kernel<<<1, 32, 0, stream>>>(f, polls);
+  XC_CUDA_TRY(cudaGetLastError());
+  return XC_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Mode -> pair map (src/validate.hpp:216-298).
 // ---------------------------------------------------------------------------
 bool make_pair_map(xc_mode mode, uint32_t n_left, uint32_t n_right, PairMap* pm, uint64_t* n_out) {

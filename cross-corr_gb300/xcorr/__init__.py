@@ -31,7 +31,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "cuFFT error", 4: 
 
 # Every symbol declared in include/xcorr.h (checked by the CPU test suite).
 EXPORTED = [
-    "xc_version", "xc_status_string", "xc_last_error", "xc_device_check", "xc_output_count", "xc_output_size",
+    "xc_version", "xc_status_string", "xc_last_error", "xc_device_check", "xc_check_device",
+    "xc_debug_expire_wait", "xc_output_count", "xc_output_size",
     "xc_workspace_size", "xc_correlate", "xc_correlate_host", "xc_release_thread_cache", "xc_correlate_tc_noalloc",
     "xc_fft_plan_create", "xc_fft_plan_workspace_size", "xc_fft_plan_pad_size", "xc_fft_execute",
     "xc_fft_forward", "xc_fft_multiply", "xc_fft_inverse", "xc_fft_plan_destroy",
@@ -83,6 +84,8 @@ def lib():
         L.xc_status_string.argtypes = [i]
         L.xc_last_error.restype = c.c_char_p
         L.xc_device_check.argtypes = [i]
+        L.xc_check_device.argtypes = [vp]
+        L.xc_debug_expire_wait.argtypes = [u32, vp]
         L.xc_output_count.argtypes = [i, u32, u32, c.POINTER(c.c_uint64)]
         L.xc_output_size.argtypes = [Size2, Size2, c.POINTER(Size2)]
         L.xc_workspace_size.argtypes = [i, i, i, Size2, u32, Size2, u32, c.POINTER(sz)]

@@ -74,6 +74,15 @@ const char* xc_status_string(xc_status status);
 const char* xc_last_error(void);
 /* Device compute capability check: XC_OK only on an sm_103 device. */
 xc_status xc_device_check(int device);
+/* Synchronises `stream`, then reports XC_ERR_TIMEOUT if a bounded device-side
+ * wait of an earlier launch on this device gave up (and clears that record).
+ * The reference has no device-side waits; it surfaces asynchronous errors
+ * the same way, after a synchronisation (src/main.cpp:268-275). */
+xc_status xc_check_device(void* stream);
+/* Test hook for the bounded waits (new, no reference counterpart): launches
+ * one block that waits on a shared-memory mbarrier nothing completes, gives up
+ * after `polls` polls, records the expiry and returns.  No fault, no hang. */
+xc_status xc_debug_expire_wait(uint32_t polls, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Geometry (src/validate.hpp:190-214 result_matrix_size / counts)          */
