@@ -327,6 +327,53 @@ xc_status xc_fft_plan_destroy(xc_fft_plan plan) {
 }
 
 // ---------------------------------------------------------------------------
+// Ragged batches
+// ---------------------------------------------------------------------------
+struct xc_ragged_plan_s {
+  RaggedPlanImpl* impl;
+};
+
+xc_status xc_ragged_plan_create(xc_ragged_plan* plan, xc_dtype dtype, const void* d_left,
+                                const xc_matrix_desc* lefts, uint32_t n_left, const void* d_right,
+                                const xc_matrix_desc* rights, uint32_t n_right, const xc_pair_desc* pairs,
+                                uint32_t n_pairs, void* d_out) {
+  if (plan == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "plan is NULL");
+  *plan = nullptr;
+  RaggedPlanImpl* impl = nullptr;
+  XC_TRY(ragged_plan_create(&impl, dtype, d_left, lefts, n_left, d_right, rights, n_right, pairs, n_pairs, d_out));
+  *plan = new xc_ragged_plan_s{impl};
+  return XC_OK;
+}
+
+xc_status xc_ragged_autotune(xc_ragged_plan plan, void* stream, int* chosen_shape, double* best_ms) {
+  if (plan == nullptr || chosen_shape == nullptr || best_ms == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  return ragged_autotune(plan->impl, as_stream(stream), chosen_shape, best_ms);
+}
+
+xc_status xc_ragged_execute(xc_ragged_plan plan, void* stream) {
+  if (plan == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "plan is NULL");
+  return ragged_execute(plan->impl, as_stream(stream));
+}
+
+xc_status xc_ragged_plan_destroy(xc_ragged_plan plan) {
+  if (plan == nullptr) return XC_OK;
+  ragged_plan_destroy(plan->impl);
+  delete plan;
+  return XC_OK;
+}
+
+xc_status xc_correlate_pairs(xc_dtype dtype, const void* d_left, const xc_matrix_desc* lefts, uint32_t n_left,
+                             const void* d_right, const xc_matrix_desc* rights, uint32_t n_right,
+                             const xc_pair_desc* pairs, uint32_t n_pairs, void* d_out, void* stream) {
+  if (d_left == nullptr || d_right == nullptr || d_out == nullptr || lefts == nullptr || rights == nullptr ||
+      pairs == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  return correlate_pairs(dtype, d_left, lefts, n_left, d_right, rights, n_right, pairs, n_pairs, d_out,
+                         as_stream(stream));
+}
+
+// ---------------------------------------------------------------------------
 // Drop-ins for the reference's run_* launchers (src/kernels.cuh).
 // ---------------------------------------------------------------------------
 }  // extern "C"

@@ -1,34 +1,40 @@
 // direct_simt.cu -- plain definition-based full 2D cross-correlation on the
-// FP32/FP64 FMA pipes of GB300 (sm_103a).
+// FP32/FP64 FMA pipes of GB300 (sm_103a), for uniform batches (the four
+// modes) and for ragged batches of pairs of any sizes.
 //
 // Replaces the reference's warp-shuffle kernel family (src/naive_shuffle*.cu,
 // e.g. ccn_shuffle src/naive_shuffle.cu:86-267 and the best one_to_many kernel
 // src/naive_shuffle_one_to_many_multirow_both_multimat_right.cu:91-535).
 // Same result and shift order, different design:
 //
-//  * A CTA owns an output tile of BSY x BSX shifts for G right matrices that
-//    share one left matrix (the reference's "multimat right" reuse).
-//  * Work is streamed in stages (x-chunk of XC right columns) x (one right row
-//    y).  Each stage's left window (BSY rows x XC+BSX columns) and right rows
-//    (G matrices x XC columns) are staged in shared memory by TMA
-//    (cp.async.bulk.tensor), whose out-of-bounds zero fill replaces every
-//    bounds check of the reference (src/bound_checked_loads.cuh:22-39).  Row
-//    pitches TMA cannot describe (not a multiple of 16 bytes) fall back to
-//    cp.async with zero fill.
-//  * Each thread accumulates TSY x TSX shifts x TG matrices in registers.  The
-//    left values of its TSX consecutive shifts form a sliding window carried
-//    in registers across x steps; every 4 columns it loads one new 128-bit
-//    vector per left row and one broadcast 128-bit vector per right matrix,
-//    so an x step issues TSY*TSX*TG*4 FMAs per (TSY+TG) vector loads.  The
-//    register carry replaces the reference's per-FMA shuffle rotation
+//  * Work is cut into tiles: BSY x BSX shifts for up to G right matrices that
+//    share one left matrix (the reference's "multimat right" reuse).  A tile
+//    is streamed in stages of (XC right columns) x (one right row y); a
+//    stage's left window (BSY rows x XC+BSX columns) and right rows (G x XC)
+//    land in shared memory by TMA (cp.async.bulk.tensor).  TMA's zero fill
+//    of out-of-bounds elements replaces every bounds check of the reference
+//    (src/bound_checked_loads.cuh:22-39).  Row pitches TMA cannot describe
+//    (not a multiple of 16 bytes) are loaded with cp.async + zero fill.
+//  * One producer warp issues the loads into a ring of STAGES slots; the
+//    consumer warps wait on per-slot "full" mbarriers and release slots with
+//    per-slot "empty" mbarriers, so no CTA-wide barrier is taken per stage.
+//    The producer also publishes each stage's tile geometry in shared memory,
+//    which lets the same kernel run persistently over a queue of tiles.
+//  * Each consumer thread accumulates TSY x TSX shifts x TG matrices in
+//    registers.  The left values of its TSX consecutive shifts form a sliding
+//    window held in three 4-element register buffers that rotate through a
+//    3x unrolled column loop (no register moves); every 4 columns it loads
+//    one 128-bit vector per left row and one broadcast vector per right
+//    matrix.  This replaces the reference's per-FMA shuffle rotation
 //    (src/naive_shuffle.cu:134-148), which made it shuffle-issue bound.
 //  * FP32 partial sums are flushed into the output every FLUSH_STAGES stages
 //    (store first, then add), so no FP32 accumulation chain exceeds
 //    FLUSH_STAGES*XC products: serial FP32 sums over 256x256 overlaps would
 //    otherwise drift past 1e-5 of max|out|.
-//  * Bounded mbarrier waits: a wait that expires records a flag and the whole
-//    CTA returns (no trap, no hang).
+//  * Bounded mbarrier waits: an expired wait records a flag and the CTA
+//    winds down (no trap, no hang).
 #include <algorithm>
+#include <cstring>
 
 #include "xc_common.cuh"
 #include "xc_internal.h"
@@ -58,28 +64,67 @@ __device__ __forceinline__ V4<double> lds4<double>(const double* p) {
   return V4<double>{{a.x, a.y, b.x, b.y}};
 }
 
+// Geometry of one tile as the producer publishes it with every stage.
+struct TileInfo {
+  int Hl, Wl, Hr, Wr, Sy, Sx;
+  int SY0, SX0;
+  int nmat;              // right matrices of the tile that exist (<= G)
+  int lc;                // left TMA coordinate (matrix index within its map)
+  int rc2, rc3;          // right TMA coordinates of dims 2 and 3
+  long long out0;        // element offset of the first matrix's output
+  long long ostride;     // element offset between consecutive matrices' outputs
+  long long lsrc;        // element offset of the left matrix (cp.async loader)
+  long long rsrc0;       // element offset of the first right matrix (cp.async loader)
+  long long rstride;     // element offset between the tile's right matrices (cp.async loader)
+  const void* lmap;      // tensor maps (TMA loader)
+  const void* rmap;
+};
+
+struct StageMeta {
+  TileInfo ti;
+  int y, xc_start;
+  int first, last, end;
+};
+
+// Uniform batches: the four modes over equal-size matrices.
 template <typename T>
-struct DirectParams {
-  const T* left;
-  const T* right;
-  T* out;
+struct Uniform {
   int Hl, Wl, Hr, Wr, Sy, Sx;
   PairMap pm;
   int tiles_sx, tiles_sy, kgroups;
   int sx_origin;  // first tile's sx (<= 0) so that every tile's left x origin is 16-byte aligned
+};
+
+// Ragged batches: one tile queue over pairs of arbitrary sizes.
+struct RaggedView {
+  const RaggedTile* tiles;
+  const RaggedPairDev* pairs;
+  const CUtensorMap* lmaps;  // per left matrix (padded copies)
+  const CUtensorMap* rmaps;  // per right matrix
+  unsigned int* queue;       // next tile to hand out
+  int n_tiles;
+};
+
+template <typename T>
+struct DirectArgs {
+  const T* left;
+  const T* right;
+  T* out;
+  Uniform<T> u;
+  RaggedView rg;  // rg.tiles == nullptr for uniform batches
   DeviceFlags* flags;
 };
 
 // Tile configuration.
-//  lanes: 4 (sy) x 8 (sx) per warp; warps: WY x WX x WG per CTA.
-template <typename T, int TSY_, int TSX_, int TG_, int WY_, int WX_, int WG_, int XC_, int STAGES_, int MINB_>
+//  lanes: 4 (sy) x 8 (sx) per warp; consumer warps: WY x WX x WG; one producer warp.
+template <typename T, int TSY_, int TG_, int WY_, int WX_, int WG_, int XC_, int STAGES_, int MINB_>
 struct Cfg {
   using type = T;
-  static constexpr int TSY = TSY_, TSX = TSX_, TG = TG_, WY = WY_, WX = WX_, WG = WG_;
+  static constexpr int TSY = TSY_, TSX = 8, TG = TG_, WY = WY_, WX = WX_, WG = WG_;
   static constexpr int XC = XC_, STAGES = STAGES_, MINB = MINB_;
   static constexpr int LANES_Y = 4, LANES_X = 8;
-  static constexpr int NWARPS = WY * WX * WG;
-  static constexpr int NT = NWARPS * 32;
+  static constexpr int NW = WY * WX * WG;  // consumer warps
+  static constexpr int NT = (NW + 1) * 32;
   static constexpr int WSY = LANES_Y * TSY;  // sy rows per warp
   static constexpr int WSX = LANES_X * TSX;  // sx columns per warp
   static constexpr int BSY = WY * WSY;
@@ -90,279 +135,379 @@ struct Cfg {
   static constexpr int L_ELEMS = BSY * LW;
   static constexpr int R_ELEMS = G * XC;
   static constexpr int STAGE_BYTES = ((L_ELEMS + R_ELEMS) * (int)sizeof(T) + 127) / 128 * 128;
-  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 128;
+  static constexpr int META_BYTES = (STAGES * (int)sizeof(StageMeta) + 127) / 128 * 128;
+  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + META_BYTES + 2 * STAGES * 8 + 128;
   // FP32 chains are capped at 4096 products per flush; FP64 needs no flush.
   static constexpr int FLUSH_STAGES = sizeof(T) == 4 ? (4096 / XC) : (1 << 30);
-  static_assert(TSX % 4 == 0, "TSX must be a multiple of 4");
   static_assert(LW <= 256 && BSY <= 256 && XC <= 256 && G <= 256, "TMA box dimensions are limited to 256");
   static_assert((LW * (int)sizeof(T)) % 16 == 0 && (XC * (int)sizeof(T)) % 16 == 0, "TMA inner box must be 16B");
+  static_assert(XC % 4 == 0, "column chunks are walked 4 at a time");
+};
+
+// Stage count and column range of a tile.
+struct TileSpan {
+  int y_lo, ny, x_lo, nxc;
 };
 
 template <typename C>
+__device__ __forceinline__ TileSpan tile_span(const TileInfo& ti) {
+  TileSpan s;
+  s.y_lo = max(0, ti.Hr - 1 - (ti.SY0 + C::BSY - 1));
+  const int y_hi = min(ti.Hr, ti.Hl + ti.Hr - 1 - ti.SY0);
+  s.x_lo = max(0, ti.Wr - 1 - (ti.SX0 + C::BSX - 1)) & ~(C::VEC - 1);
+  const int x_hi = min(ti.Wr, ti.Wl + ti.Wr - 1 - ti.SX0);
+  s.ny = max(0, y_hi - s.y_lo);
+  s.nxc = x_hi > s.x_lo ? (x_hi - s.x_lo + C::XC - 1) / C::XC : 0;
+  return s;
+}
+
+template <typename C>
 __global__ void __launch_bounds__(C::NT, C::MINB)
-    direct_kernel(const __grid_constant__ CUtensorMap lmap, const __grid_constant__ CUtensorMap rmap,
-                  const DirectParams<typename C::type> p, const bool use_tma) {
+    direct_kernel(const __grid_constant__ CUtensorMap lmap_u, const __grid_constant__ CUtensorMap rmap_u,
+                  const DirectArgs<typename C::type> p, const bool use_tma) {
   using T = typename C::type;
   constexpr int TSY = C::TSY, TSX = C::TSX, TG = C::TG, XC = C::XC, S = C::STAGES;
   constexpr int BSY = C::BSY, BSX = C::BSX, G = C::G, LW = C::LW;
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + S * C::STAGE_BYTES);
-
-  // ---- decode the CTA's tile --------------------------------------------
-  const int nlk = p.pm.n_left * p.kgroups;
-  int bid = blockIdx.x;
-  const int lk = bid % nlk;
-  bid /= nlk;
-  const int tx = bid % p.tiles_sx;
-  const int ty = bid / p.tiles_sx;
-  const int l = lk / p.kgroups;
-  const int k0 = (lk % p.kgroups) * G;
-  const int SY0 = ty * BSY;
-  const int SX0 = p.sx_origin + tx * BSX;
-
-  // Right rows / columns that meet any shift of the tile.
-  const int y_lo = max(0, p.Hr - 1 - (SY0 + BSY - 1));
-  const int y_hi = min(p.Hr, p.Hl + p.Hr - 1 - SY0);
-  const int x_lo = max(0, p.Wr - 1 - (SX0 + BSX - 1)) & ~(C::VEC - 1);
-  const int x_hi = min(p.Wr, p.Wl + p.Wr - 1 - SX0);
-  if (y_lo >= y_hi || x_lo >= x_hi) return;  // uniform over the CTA
-  const int ny = y_hi - y_lo;
-  const int nxc = (x_hi - x_lo + XC - 1) / XC;
-  const int nst = ny * nxc;
+  StageMeta* meta = reinterpret_cast<StageMeta*>(smem + S * C::STAGE_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * C::STAGE_BYTES + C::META_BYTES);
+  uint64_t* empty = full + S;
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
+  const bool ragged = p.rg.tiles != nullptr;
+
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      // TMA: the producer's arrive.expect_tx; cp.async: one asynchronous
+      // arrival per producer lane plus lane 0's release arrival after it
+      // wrote the stage's metadata
+      mbar_init(&full[s], use_tma ? 1 : 33);
+      mbar_init(&empty[s], C::NW);
+    }
+    fence_mbar_init();
+    if (use_tma && !ragged) {
+      prefetch_tensormap(&lmap_u);
+      prefetch_tensormap(&rmap_u);
+    }
+  }
+  __syncthreads();
+
+  auto stage_L = [&](int slot) { return reinterpret_cast<T*>(smem + slot * C::STAGE_BYTES); };
+  auto stage_R = [&](int slot) { return reinterpret_cast<T*>(smem + slot * C::STAGE_BYTES) + C::L_ELEMS; };
+
+  if (warp == C::NW) {
+    // ================================================================ producer
+    int j = 0;
+    bool ok = true;
+    for (int iter = 0; ok; ++iter) {
+      TileInfo ti;
+      if (!ragged) {
+        if (iter > 0) break;
+        const Uniform<T>& u = p.u;
+        const int nlk = u.pm.n_left * u.kgroups;
+        int bid = blockIdx.x;
+        const int lk = bid % nlk;
+        bid /= nlk;
+        const int tx = bid % u.tiles_sx;
+        const int ty = bid / u.tiles_sx;
+        const int l = lk / u.kgroups;
+        const int k0 = (lk % u.kgroups) * G;
+        ti.Hl = u.Hl; ti.Wl = u.Wl; ti.Hr = u.Hr; ti.Wr = u.Wr; ti.Sy = u.Sy; ti.Sx = u.Sx;
+        ti.SY0 = ty * BSY;
+        ti.SX0 = u.sx_origin + tx * BSX;
+        ti.nmat = min(G, u.pm.K - k0);
+        ti.lc = l;
+        ti.rc2 = u.pm.r_l != 0 ? l : 0;
+        ti.rc3 = k0;
+        ti.out0 = ((long long)l * u.pm.o_l + (long long)k0 * u.pm.o_k) * u.Sy * u.Sx;
+        ti.ostride = u.pm.o_k * (long long)u.Sy * u.Sx;
+        ti.lsrc = (long long)l * u.Hl * u.Wl;
+        ti.rsrc0 = ((long long)l * u.pm.r_l + (long long)k0 * u.pm.r_k) * u.Hr * u.Wr;
+        ti.rstride = u.pm.r_k * (long long)u.Hr * u.Wr;
+        ti.lmap = &lmap_u;
+        ti.rmap = &rmap_u;
+      } else {
+        unsigned int t = 0;
+        if (lane == 0) t = atomicAdd(p.rg.queue, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= (unsigned)p.rg.n_tiles) break;
+        const RaggedTile rt = p.rg.tiles[t];
+        const RaggedPairDev pr = p.rg.pairs[rt.pair];
+        ti.Hl = pr.Hl; ti.Wl = pr.Wl; ti.Hr = pr.Hr; ti.Wr = pr.Wr;
+        ti.Sy = pr.Hl + pr.Hr - 1;
+        ti.Sx = pr.Wl + pr.Wr - 1;
+        ti.SY0 = rt.sy0;
+        ti.SX0 = rt.sx0;
+        ti.nmat = 1;
+        ti.lc = 0;
+        ti.rc2 = 0;
+        ti.rc3 = 0;
+        ti.out0 = (long long)pr.out_off;
+        ti.ostride = 0;
+        ti.lsrc = 0;
+        ti.rsrc0 = 0;
+        ti.rstride = 0;
+        ti.lmap = p.rg.lmaps + pr.left;
+        ti.rmap = p.rg.rmaps + pr.right;
+      }
+      const TileSpan sp = tile_span<C>(ti);
+      const int nst = sp.ny * sp.nxc;
+      for (int st = 0; st < nst; ++st, ++j) {
+        const int slot = j % S;
+        bool w = true;
+        if (lane == 0) w = mbar_wait_bounded(&empty[slot], ((j / S) & 1) ^ 1);
+        if (!__shfl_sync(0xffffffffu, (int)w, 0)) {
+          if (lane == 0) record_timeout(p.flags, 2);
+          ok = false;
+          break;
+        }
+        const int xc_start = sp.x_lo + (st / sp.ny) * XC;
+        const int y = sp.y_lo + (st % sp.ny);
+        if (lane == 0) {
+          StageMeta& m = meta[slot];
+          m.ti = ti;
+          m.y = y;
+          m.xc_start = xc_start;
+          m.first = st == 0;
+          m.last = st == nst - 1;
+          m.end = 0;
+        }
+        const int lx0 = xc_start + ti.SX0 - (ti.Wr - 1);
+        const int ly0 = y + ti.SY0 - (ti.Hr - 1);
+        T* sL = stage_L(slot);
+        T* sR = stage_R(slot);
+        if (use_tma) {
+          if (lane == 0) {
+            mbar_arrive_expect_tx(&full[slot], (uint32_t)((C::L_ELEMS + C::R_ELEMS) * sizeof(T)));
+            tma_load_3d(sL, reinterpret_cast<const CUtensorMap*>(ti.lmap), &full[slot], lx0, ly0, ti.lc);
+            tma_load_4d(sR, reinterpret_cast<const CUtensorMap*>(ti.rmap), &full[slot], xc_start, y, ti.rc2,
+                        ti.rc3);
+          }
+        } else {
+          const T* Lm = p.left + ti.lsrc;
+          for (int e = lane; e < C::L_ELEMS; e += 32) {
+            const int r = e / LW, c = e % LW;
+            const int gy = ly0 + r, gx = lx0 + c;
+            const bool okk = gy >= 0 && gy < ti.Hl && gx >= 0 && gx < ti.Wl;
+            cp_async_zfill<sizeof(T)>(sL + e, okk ? Lm + (long long)gy * ti.Wl + gx : p.left, okk);
+          }
+          for (int e = lane; e < C::R_ELEMS; e += 32) {
+            const int g = e / XC, c = e % XC;
+            const int gx = xc_start + c;
+            const bool okk = g < ti.nmat && gx < ti.Wr;
+            const T* src = p.right + ti.rsrc0 + (long long)g * ti.rstride + (long long)y * ti.Wr + gx;
+            cp_async_zfill<sizeof(T)>(sR + e, okk ? src : p.right, okk);
+          }
+          cp_async_mbar_arrive(&full[slot]);
+          if (lane == 0) mbar_arrive(&full[slot]);
+        }
+      }
+    }
+    if (ok) {
+      // end-of-work sentinel
+      const int slot = j % S;
+      bool w = true;
+      if (lane == 0) w = mbar_wait_bounded(&empty[slot], ((j / S) & 1) ^ 1);
+      if (__shfl_sync(0xffffffffu, (int)w, 0)) {
+        if (lane == 0) {
+          meta[slot].end = 1;
+          mbar_arrive_count(&full[slot], use_tma ? 1u : 33u);
+        }
+      } else if (lane == 0) {
+        record_timeout(p.flags, 3);
+      }
+    }
+    return;
+  }
+
+  // ================================================================== consumers
   const int wg = warp % C::WG;
   const int wx = (warp / C::WG) % C::WX;
   const int wy = warp / (C::WG * C::WX);
   const int lyy = lane >> 3, lxx = lane & 7;
   const int row0 = wy * C::WSY + lyy * TSY;  // first local sy row of this thread
   const int col0 = wx * C::WSX + lxx * TSX;  // first local sx column of this thread
-  const int wsy0 = SY0 + wy * C::WSY, wsx0 = SX0 + wx * C::WSX;
-
-  const int rdim2 = p.pm.r_l != 0 ? l : 0;
-
-  if (use_tma && tid == 0) {
-    prefetch_tensormap(&lmap);
-    prefetch_tensormap(&rmap);
-    for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-
-  auto stage_ptrL = [&](int slot) { return reinterpret_cast<T*>(smem + slot * C::STAGE_BYTES); };
-  auto stage_ptrR = [&](int slot) { return reinterpret_cast<T*>(smem + slot * C::STAGE_BYTES) + C::L_ELEMS; };
-
-  // Issue the loads of stage j into its slot.
-  auto issue = [&](int j) {
-    if (j >= nst) {
-      if (!use_tma) cp_async_commit();
-      return;
-    }
-    const int slot = j % S;
-    const int xc_start = x_lo + (j / ny) * XC;
-    const int y = y_lo + (j % ny);
-    const int lx0 = xc_start + SX0 - (p.Wr - 1);
-    const int ly0 = y + SY0 - (p.Hr - 1);
-    T* sL = stage_ptrL(slot);
-    T* sR = stage_ptrR(slot);
-    if (use_tma) {
-      if (tid == 0) {
-        mbar_arrive_expect_tx(&bars[slot], (uint32_t)((C::L_ELEMS + C::R_ELEMS) * sizeof(T)));
-        tma_load_3d(sL, &lmap, &bars[slot], lx0, ly0, l);
-        tma_load_4d(sR, &rmap, &bars[slot], xc_start, y, rdim2, k0);
-      }
-    } else {
-      const T* Lm = p.left + (long long)l * p.Hl * p.Wl;
-      for (int e = tid; e < C::L_ELEMS; e += C::NT) {
-        const int r = e / LW, c = e % LW;
-        const int gy = ly0 + r, gx = lx0 + c;
-        const bool ok = gy >= 0 && gy < p.Hl && gx >= 0 && gx < p.Wl;
-        cp_async_zfill<sizeof(T)>(sL + e, ok ? Lm + (long long)gy * p.Wl + gx : p.left, ok);
-      }
-      for (int e = tid; e < C::R_ELEMS; e += C::NT) {
-        const int g = e / XC, c = e % XC;
-        const int k = k0 + g, gx = xc_start + c;
-        const bool ok = k < p.pm.K && gx < p.Wr;
-        const long long r = ok ? (long long)l * p.pm.r_l + (long long)k * p.pm.r_k : 0;
-        cp_async_zfill<sizeof(T)>(sR + e, ok ? p.right + (r * p.Hr + y) * p.Wr + gx : p.right, ok);
-      }
-      cp_async_commit();
-    }
-  };
 
   T acc[TSY][TSX][TG];
-#pragma unroll
-  for (int t = 0; t < TSY; ++t)
-#pragma unroll
-    for (int j = 0; j < TSX; ++j)
-#pragma unroll
-      for (int i = 0; i < TG; ++i) acc[t][j][i] = T(0);
   bool flushed = false;
+  int since = 0;
+  // tile state kept across its stages
+  int t_Sy = 0, t_Sx = 0, t_SY0 = 0, t_SX0 = 0, t_nmat = 0;
+  long long t_out0 = 0, t_ostride = 0;
+  int yw_lo = 0, yw_hi = 0, xw_lo = 0, xw_hi = 0;
 
-  // The empty asm keeps the compiler from hoisting the 4*TSY*TSX*TG output
-  // addresses out of the stage loop (they would pin ~100 registers).
+  auto zero = [&]() {
+#pragma unroll
+    for (int t = 0; t < TSY; ++t)
+#pragma unroll
+      for (int q = 0; q < TSX; ++q)
+#pragma unroll
+        for (int i = 0; i < TG; ++i) acc[t][q][i] = T(0);
+  };
+
+  // The empty asm keeps the compiler from hoisting the output addresses out of
+  // the stage loop (they would pin many registers).
   auto flush = [&]() {
-    int sy_base = SY0 + row0, sx_base = SX0 + col0, kb = k0 + wg * TG;
-    asm volatile("" : "+r"(sy_base), "+r"(sx_base), "+r"(kb));
+    int sy_base = t_SY0 + row0, sx_base = t_SX0 + col0, gb = wg * TG;
+    asm volatile("" : "+r"(sy_base), "+r"(sx_base), "+r"(gb));
 #pragma unroll
     for (int i = 0; i < TG; ++i) {
-      const int k = kb + i;
-      if (k >= p.pm.K) continue;
-      T* o = p.out + ((long long)l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy * p.Sx;
+      if (gb + i >= t_nmat) continue;
+      T* o = p.out + t_out0 + (long long)(gb + i) * t_ostride;
 #pragma unroll
       for (int t = 0; t < TSY; ++t) {
         const int sy = sy_base + t;
-        if (sy >= p.Sy) continue;
+        if (sy >= t_Sy) continue;
 #pragma unroll
-        for (int j = 0; j < TSX; ++j) {
-          const int sx = sx_base + j;
-          if (sx < 0 || sx >= p.Sx) continue;
-          T* dst = o + (long long)sy * p.Sx + sx;
-          *dst = flushed ? *dst + acc[t][j][i] : acc[t][j][i];
-          acc[t][j][i] = T(0);
+        for (int q = 0; q < TSX; ++q) {
+          const int sx = sx_base + q;
+          if (sx < 0 || sx >= t_Sx) continue;
+          T* dst = o + (long long)sy * t_Sx + sx;
+          *dst = flushed ? *dst + acc[t][q][i] : acc[t][q][i];
+          acc[t][q][i] = T(0);
         }
       }
     }
     flushed = true;
   };
 
-  for (int s = 0; s < S - 1; ++s) issue(s);
-
-  for (int j = 0; j < nst; ++j) {
-    issue(j + S - 1);
+  zero();
+  for (int j = 0;; ++j) {
     const int slot = j % S;
-    if (use_tma) {
-      const bool ok = mbar_wait_bounded(&bars[slot], (uint32_t)((j / S) & 1));
-      if (__syncthreads_or(!ok)) {
-        if (tid == 0) {
-          record_timeout(p.flags, 1);
-          // Give copies still in flight a bounded chance to land before exit.
-          for (int q = j; q < min(nst, j + S); ++q) mbar_wait_bounded(&bars[q % S], (uint32_t)((q / S) & 1), 1u << 16);
-        }
-        return;
-      }
-    } else {
-      cp_async_wait<S - 1>();
-      __syncthreads();
+    if (!mbar_wait_bounded(&full[slot], (j / S) & 1)) {
+      if (lane == 0) record_timeout(p.flags, 1);
+      break;
     }
-
-    const int xc_start = x_lo + (j / ny) * XC;
-    const int y = y_lo + (j % ny);
-    // Does this warp's 16-row band of shifts meet right row y?
-    const bool y_ok = (y >= p.Hr - 1 - (wsy0 + C::WSY - 1)) && (y < p.Hl + p.Hr - 1 - wsy0);
-    // Columns of this chunk that meet the warp's shifts, in 4-column steps.
-    int xs = max(0, p.Wr - 1 - (wsx0 + C::WSX - 1)) - xc_start;
-    int xe = min(p.Wr, p.Wl + p.Wr - 1 - wsx0) - xc_start;
-    xs = max(xs, 0) & ~3;
-    xe = min(xe, XC);
-    if (y_ok && xs < xe) {
-      const T* sL = stage_ptrL(slot) + row0 * LW + col0;
-      const T* sR = stage_ptrR(slot) + (wg * TG) * XC;
-      T cur[TSY][TSX];
+    const StageMeta& m = meta[slot];
+    if (m.end) break;
+    const int y = m.y, xc_start = m.xc_start;
+    const int last = m.last;
+    if (m.first) {
+      const TileInfo& ti = m.ti;
+      t_Sy = ti.Sy;
+      t_Sx = ti.Sx;
+      t_SY0 = ti.SY0;
+      t_SX0 = ti.SX0;
+      t_nmat = ti.nmat;
+      t_out0 = ti.out0;
+      t_ostride = ti.ostride;
+      const int wsy0 = ti.SY0 + wy * C::WSY, wsx0 = ti.SX0 + wx * C::WSX;
+      // right rows / columns that meet this warp's band of shifts
+      yw_lo = ti.Hr - 1 - (wsy0 + C::WSY - 1);
+      yw_hi = ti.Hl + ti.Hr - 1 - wsy0;
+      xw_lo = max(0, ti.Wr - 1 - (wsx0 + C::WSX - 1));
+      xw_hi = min(ti.Wr, ti.Wl + ti.Wr - 1 - wsx0);
+      flushed = false;
+      since = 0;
+    }
+    int xs = max(xw_lo - xc_start, 0) & ~3;
+    int xe = min(xw_hi - xc_start, XC);
+    if (y >= yw_lo && y < yw_hi && xs < xe) {
+      const T* sL = stage_L(slot) + row0 * LW + col0;
+      const T* sR = stage_R(slot) + (wg * TG) * XC;
+      // three rotating 4-column buffers per left row: window = 12 columns
+      V4<T> P[TSY], Q[TSY], R[TSY];
 #pragma unroll
       for (int t = 0; t < TSY; ++t) {
-#pragma unroll
-        for (int q = 0; q < TSX / 4; ++q) {
-          V4<T> v = lds4<T>(sL + t * LW + xs + 4 * q);
-          cur[t][4 * q + 0] = v.v[0];
-          cur[t][4 * q + 1] = v.v[1];
-          cur[t][4 * q + 2] = v.v[2];
-          cur[t][4 * q + 3] = v.v[3];
-        }
+        P[t] = lds4<T>(sL + t * LW + xs);
+        Q[t] = lds4<T>(sL + t * LW + xs + 4);
       }
-#pragma unroll 1
-      for (int xo = xs; xo < xe; xo += 4) {
+      // one 4-column step over the window (A | B | C), C freshly loaded
+      auto step = [&](V4<T>* A, V4<T>* B, V4<T>* Cn, int x) {
         V4<T> rv[TG];
 #pragma unroll
-        for (int i = 0; i < TG; ++i) rv[i] = lds4<T>(sR + i * XC + xo);
+        for (int i = 0; i < TG; ++i) rv[i] = lds4<T>(sR + i * XC + x);
 #pragma unroll
         for (int t = 0; t < TSY; ++t) {
-          const V4<T> nw = lds4<T>(sL + t * LW + xo + TSX);
-          T win[TSX + 4];
-#pragma unroll
-          for (int q = 0; q < TSX; ++q) win[q] = cur[t][q];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) win[TSX + q] = nw.v[q];
+          Cn[t] = lds4<T>(sL + t * LW + x + 8);
 #pragma unroll
           for (int xx = 0; xx < 4; ++xx)
 #pragma unroll
-            for (int jj = 0; jj < TSX; ++jj)
+            for (int q = 0; q < TSX; ++q) {
+              const int w = xx + q;
+              const T lv = w < 4 ? A[t].v[w] : (w < 8 ? B[t].v[w - 4] : Cn[t].v[w - 8]);
 #pragma unroll
-              for (int i = 0; i < TG; ++i) acc[t][jj][i] = fma(win[xx + jj], rv[i].v[xx], acc[t][jj][i]);
-#pragma unroll
-          for (int q = 0; q < TSX; ++q) cur[t][q] = win[q + 4];
+              for (int i = 0; i < TG; ++i) acc[t][q][i] = fma(lv, rv[i].v[xx], acc[t][q][i]);
+            }
         }
+      };
+#pragma unroll 1
+      for (int xo = xs; xo < xe; xo += 12) {
+        step(P, Q, R, xo);
+        if (xo + 4 >= xe) break;
+        step(Q, R, P, xo + 4);
+        if (xo + 8 >= xe) break;
+        step(R, P, Q, xo + 8);
       }
     }
-    if ((j + 1) % C::FLUSH_STAGES == 0) flush();
-    __syncthreads();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[slot]);
+    if (++since == C::FLUSH_STAGES || last) {
+      flush();
+      since = 0;
+    }
   }
-  flush();
 }
 
-using CfgF32Multi = Cfg<float, 4, 4, 4, 2, 2, 2, 128, 3, 2>;   // 32 sy x 64 sx x 8 mats, 256 threads
-using CfgF32Single = Cfg<float, 4, 8, 1, 4, 1, 1, 128, 2, 2>;  // 64 sy x 64 sx x 1 mat, 128 threads
-using CfgF64Multi = Cfg<double, 4, 4, 2, 2, 2, 2, 64, 3, 1>;   // 32 x 64 x 4 mats
-using CfgF64Single = Cfg<double, 4, 4, 1, 2, 2, 1, 64, 3, 2>;  // 32 x 64 x 1 mat
+// Tile shapes.  Cfg<T, TSY, TG, WY, WX, WG, XC, STAGES, MINB>.
+using CfgF32Multi = Cfg<float, 2, 4, 4, 1, 2, 128, 4, 1>;   // 32 sy x 64 sx x 8 mats, 8+1 warps
+using CfgF32Single = Cfg<float, 4, 1, 4, 1, 1, 128, 2, 2>;  // 64 sy x 64 sx x 1 mat, 4+1 warps
+using CfgF32Small = Cfg<float, 2, 1, 4, 1, 1, 128, 3, 3>;   // 32 sy x 64 sx x 1 mat, 4+1 warps
+using CfgF64Multi = Cfg<double, 2, 2, 4, 1, 2, 64, 3, 1>;   // 32 x 64 x 4 mats
+using CfgF64Single = Cfg<double, 2, 1, 4, 1, 1, 64, 3, 2>;  // 32 x 64 x 1 mat
 
 template <typename C>
-xc_status launch_cfg(const typename C::type* left, const typename C::type* right, typename C::type* out,
-                     const Geometry& g, const PairMap& pm, cudaStream_t stream, int force_loader) {
+xc_status launch_uniform(const typename C::type* left, const typename C::type* right, typename C::type* out,
+                         const Geometry& g, const PairMap& pm, cudaStream_t stream, int force_loader) {
   using T = typename C::type;
-  DirectParams<T> p;
+  DirectArgs<T> p;
+  std::memset(&p, 0, sizeof(p));
   p.left = left;
   p.right = right;
   p.out = out;
-  p.Hl = g.Hl;
-  p.Wl = g.Wl;
-  p.Hr = g.Hr;
-  p.Wr = g.Wr;
-  p.Sy = g.Sy;
-  p.Sx = g.Sx;
-  p.pm = pm;
+  Uniform<T>& u = p.u;
+  u.Hl = g.Hl;
+  u.Wl = g.Wl;
+  u.Hr = g.Hr;
+  u.Wr = g.Wr;
+  u.Sy = g.Sy;
+  u.Sx = g.Sx;
+  u.pm = pm;
   const int rem = (g.Wr - 1) % C::VEC;
-  p.sx_origin = rem == 0 ? 0 : rem - C::VEC;
-  p.tiles_sx = div_up(g.Sx - p.sx_origin, C::BSX);
-  p.tiles_sy = div_up(g.Sy, C::BSY);
-  p.kgroups = div_up(pm.K, C::G);
+  u.sx_origin = rem == 0 ? 0 : rem - C::VEC;
+  u.tiles_sx = div_up(g.Sx - u.sx_origin, C::BSX);
+  u.tiles_sy = div_up(g.Sy, C::BSY);
+  u.kgroups = div_up(pm.K, C::G);
   p.flags = device_flags();
 
-  const long long blocks = (long long)p.tiles_sx * p.tiles_sy * pm.n_left * p.kgroups;
+  const long long blocks = (long long)u.tiles_sx * u.tiles_sy * pm.n_left * u.kgroups;
   if (blocks <= 0) return XC_OK;
   if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
 
   // TMA needs 16-byte aligned bases and row/matrix pitches.
   const size_t es = sizeof(T);
-  bool tma_ok = ((uintptr_t)left % 16 == 0) && ((uintptr_t)right % 16 == 0) && ((size_t)g.Wl * es % 16 == 0) &&
-                ((size_t)g.Wr * es % 16 == 0);
-  bool use_tma = force_loader < 0 ? tma_ok : (force_loader == 1);
+  const bool tma_ok = ((uintptr_t)left % 16 == 0) && ((uintptr_t)right % 16 == 0) && ((size_t)g.Wl * es % 16 == 0) &&
+                      ((size_t)g.Wr * es % 16 == 0);
+  const bool use_tma = force_loader < 0 ? tma_ok : (force_loader == 1);
   if (use_tma && !tma_ok) return fail(XC_ERR_INVALID_ARGUMENT, "TMA loader requested for unaligned pitches");
 
   CUtensorMap lmap, rmap;
-  memset(&lmap, 0, sizeof(lmap));
-  memset(&rmap, 0, sizeof(rmap));
+  std::memset(&lmap, 0, sizeof(lmap));
+  std::memset(&rmap, 0, sizeof(rmap));
   if (use_tma) {
     const CUtensorMapDataType dt = sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
-    {
-      uint64_t dims[3] = {(uint64_t)g.Wl, (uint64_t)g.Hl, (uint64_t)pm.n_left};
-      uint64_t strides[2] = {(uint64_t)g.Wl * es, (uint64_t)g.Wl * g.Hl * es};
-      uint32_t box[3] = {(uint32_t)C::LW, (uint32_t)C::BSY, 1};
-      if (!encode_tiled(&lmap, dt, 3, left, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
-        return XC_ERR_INVALID_ARGUMENT;
-    }
-    {
-      const uint64_t mat = (uint64_t)g.Wr * g.Hr * es;
-      uint64_t d2 = pm.r_l != 0 ? (uint64_t)pm.n_left : 1;
-      uint64_t dims[4] = {(uint64_t)g.Wr, (uint64_t)g.Hr, d2, (uint64_t)pm.K};
-      uint64_t strides[3] = {(uint64_t)g.Wr * es, mat * (uint64_t)(pm.r_l != 0 ? pm.r_l : 1),
-                             mat * (uint64_t)pm.r_k};
-      uint32_t box[4] = {(uint32_t)C::XC, 1, 1, (uint32_t)C::G};
-      if (!encode_tiled(&rmap, dt, 4, right, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_NONE))
-        return XC_ERR_INVALID_ARGUMENT;
-    }
+    uint64_t ldims[3] = {(uint64_t)g.Wl, (uint64_t)g.Hl, (uint64_t)pm.n_left};
+    uint64_t lstr[2] = {(uint64_t)g.Wl * es, (uint64_t)g.Wl * g.Hl * es};
+    uint32_t lbox[3] = {(uint32_t)C::LW, (uint32_t)C::BSY, 1};
+    if (!encode_tiled(&lmap, dt, 3, left, ldims, lstr, lbox, CU_TENSOR_MAP_SWIZZLE_NONE)) return XC_ERR_INVALID_ARGUMENT;
+    const uint64_t mat = (uint64_t)g.Wr * g.Hr * es;
+    uint64_t rdims[4] = {(uint64_t)g.Wr, (uint64_t)g.Hr, pm.r_l != 0 ? (uint64_t)pm.n_left : 1, (uint64_t)pm.K};
+    uint64_t rstr[3] = {(uint64_t)g.Wr * es, mat * (uint64_t)(pm.r_l != 0 ? pm.r_l : 1), mat * (uint64_t)pm.r_k};
+    uint32_t rbox[4] = {(uint32_t)C::XC, 1, 1, (uint32_t)C::G};
+    if (!encode_tiled(&rmap, dt, 4, right, rdims, rstr, rbox, CU_TENSOR_MAP_SWIZZLE_NONE)) return XC_ERR_INVALID_ARGUMENT;
   }
 
   static_assert(C::SMEM_BYTES <= 227 * 1024, "shared memory budget");
@@ -373,22 +518,73 @@ xc_status launch_cfg(const typename C::type* left, const typename C::type* right
   return XC_OK;
 }
 
+template <typename C>
+xc_status launch_ragged(const RaggedLaunch& rl, cudaStream_t stream) {
+  using T = typename C::type;
+  DirectArgs<T> p;
+  std::memset(&p, 0, sizeof(p));
+  p.left = reinterpret_cast<const T*>(rl.left);
+  p.right = reinterpret_cast<const T*>(rl.right);
+  p.out = reinterpret_cast<T*>(rl.out);
+  p.rg.tiles = rl.tiles;
+  p.rg.pairs = rl.pairs;
+  p.rg.lmaps = rl.lmaps;
+  p.rg.rmaps = rl.rmaps;
+  p.rg.queue = rl.queue;
+  p.rg.n_tiles = rl.n_tiles;
+  p.flags = device_flags();
+  CUtensorMap dummy;
+  std::memset(&dummy, 0, sizeof(dummy));
+  // (the caller raised the kernel's shared-memory limit before any capture)
+  direct_kernel<C><<<(unsigned)rl.grid, C::NT, C::SMEM_BYTES, stream>>>(dummy, dummy, p, true);
+  XC_CUDA_TRY(cudaGetLastError());
+  return XC_OK;
+}
+
+template <typename C>
+RaggedShape shape_of() {
+  RaggedShape s;
+  s.bsy = C::BSY;
+  s.bsx = C::BSX;
+  s.lw = C::LW;
+  s.xc = C::XC;
+  s.vec = C::VEC;
+  s.threads = C::NT;
+  s.smem = C::SMEM_BYTES;
+  s.kernel = reinterpret_cast<const void*>(&direct_kernel<C>);
+  return s;
+}
+
 }  // namespace
 
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
                         const PairMap& pm, cudaStream_t stream, int force_loader) {
   if (dtype == XC_F32) {
     if (pm.K >= 4)
-      return launch_cfg<CfgF32Multi>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
-                                     force_loader);
-    return launch_cfg<CfgF32Single>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
-                                    force_loader);
+      return launch_uniform<CfgF32Multi>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
+                                         force_loader);
+    return launch_uniform<CfgF32Single>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
+                                        force_loader);
   }
   if (pm.K >= 3)
-    return launch_cfg<CfgF64Multi>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
-                                   force_loader);
-  return launch_cfg<CfgF64Single>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
-                                  force_loader);
+    return launch_uniform<CfgF64Multi>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
+                                       force_loader);
+  return launch_uniform<CfgF64Single>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
+                                      force_loader);
+}
+
+// Tile shapes a ragged plan may pick from (the autotuner's candidates).
+int ragged_shape_count(xc_dtype dtype) { return dtype == XC_F32 ? 2 : 1; }
+
+RaggedShape ragged_shape(xc_dtype dtype, int index) {
+  if (dtype == XC_F32) return index == 0 ? shape_of<CfgF32Single>() : shape_of<CfgF32Small>();
+  return shape_of<CfgF64Single>();
+}
+
+xc_status ragged_launch(xc_dtype dtype, int index, const RaggedLaunch& rl, cudaStream_t stream) {
+  if (dtype == XC_F32)
+    return index == 0 ? launch_ragged<CfgF32Single>(rl, stream) : launch_ragged<CfgF32Small>(rl, stream);
+  return launch_ragged<CfgF64Single>(rl, stream);
 }
 
 }  // namespace xc

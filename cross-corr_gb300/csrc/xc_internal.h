@@ -2,6 +2,7 @@
 // units (not part of the public C ABI).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -44,6 +45,46 @@ xc_status debug_expire_wait(uint32_t polls, cudaStream_t stream);
 // Plain definition-based correlation (direct_simt.cu).
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
                         const PairMap& pm, cudaStream_t stream, int force_loader /* -1 auto, 0 cp.async, 1 TMA */);
+
+// Ragged batches (ragged.cu drives direct_simt.cu's persistent mode).
+struct RaggedTile {     // one tile of shifts of one pair
+  int pair;
+  int sy0, sx0;
+};
+struct RaggedPairDev {  // a pair, with offsets into the padded copies
+  int left, right;
+  int Hl, Wl, Hr, Wr;
+  long long out_off;    // element offset of the output in the caller's buffer
+};
+struct RaggedLaunch {
+  const void* left;     // unused by the TMA path; kept for symmetry
+  const void* right;
+  void* out;
+  const RaggedTile* tiles;
+  const RaggedPairDev* pairs;
+  const CUtensorMap* lmaps;
+  const CUtensorMap* rmaps;
+  unsigned int* queue;
+  int n_tiles;
+  int grid;
+};
+struct RaggedShape {    // a tile shape the ragged kernel can run with
+  int bsy, bsx, lw, xc, vec, threads, smem;
+  const void* kernel;
+};
+int ragged_shape_count(xc_dtype dtype);
+RaggedShape ragged_shape(xc_dtype dtype, int index);
+xc_status ragged_launch(xc_dtype dtype, int index, const RaggedLaunch& rl, cudaStream_t stream);
+struct RaggedPlanImpl;
+xc_status ragged_plan_create(RaggedPlanImpl** plan, xc_dtype dtype, const void* d_left, const xc_matrix_desc* lefts,
+                             uint32_t n_left, const void* d_right, const xc_matrix_desc* rights, uint32_t n_right,
+                             const xc_pair_desc* pairs, uint32_t n_pairs, void* d_out);
+xc_status ragged_execute(RaggedPlanImpl* plan, cudaStream_t stream);
+xc_status ragged_autotune(RaggedPlanImpl* plan, cudaStream_t stream, int* chosen, double* best_ms);
+void ragged_plan_destroy(RaggedPlanImpl* plan);
+xc_status correlate_pairs(xc_dtype dtype, const void* d_left, const xc_matrix_desc* lefts, uint32_t n_left,
+                          const void* d_right, const xc_matrix_desc* rights, uint32_t n_right,
+                          const xc_pair_desc* pairs, uint32_t n_pairs, void* d_out, cudaStream_t stream);
 
 // FFT pipeline (fft_pipeline.cu).
 struct FftPlanImpl;

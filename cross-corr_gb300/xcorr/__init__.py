@@ -46,6 +46,8 @@ EXPORTED = [
     "xc_run_hadamard_n_to_m_over_output_c64", "xc_run_hadamard_n_to_m_over_output_c128",
     "xc_run_scatter_f32", "xc_run_scatter_f64",
     "xc_normalize_fft_results_f32", "xc_normalize_fft_results_f64",
+    "xc_ragged_plan_create", "xc_ragged_autotune", "xc_ragged_execute", "xc_ragged_plan_destroy",
+    "xc_correlate_pairs",
 ]
 
 
@@ -61,6 +63,14 @@ class XcError(RuntimeError):
 
 class Size2(ctypes.Structure):
     _fields_ = [("x", ctypes.c_uint32), ("y", ctypes.c_uint32)]
+
+
+class MatrixDesc(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_uint64), ("rows", ctypes.c_uint32), ("cols", ctypes.c_uint32)]
+
+
+class PairDesc(ctypes.Structure):
+    _fields_ = [("left", ctypes.c_uint32), ("right", ctypes.c_uint32), ("out_offset", ctypes.c_uint64)]
 
 
 def size2(rows: int, cols: int) -> Size2:
@@ -101,6 +111,14 @@ def lib():
         L.xc_fft_multiply.argtypes = [vp, vp, sz, vp]
         L.xc_fft_inverse.argtypes = [vp, vp, i, vp, sz, vp]
         L.xc_fft_plan_destroy.argtypes = [vp]
+        P = c.POINTER
+        L.xc_ragged_plan_create.argtypes = [P(vp), i, vp, P(MatrixDesc), u32, vp, P(MatrixDesc), u32, P(PairDesc),
+                                            u32, vp]
+        L.xc_ragged_autotune.argtypes = [vp, vp, P(c.c_int), P(c.c_double)]
+        L.xc_ragged_execute.argtypes = [vp, vp]
+        L.xc_ragged_plan_destroy.argtypes = [vp]
+        L.xc_correlate_pairs.argtypes = [i, vp, P(MatrixDesc), u32, vp, P(MatrixDesc), u32, P(PairDesc), u32, vp,
+                                         vp]
         for t in ("f32", "f64"):
             getattr(L, f"xc_run_ccn_shuffle_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, vp]
             getattr(L, f"xc_run_ccn_shuffle_multimat_right_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, u32, u32,
@@ -219,6 +237,87 @@ class FftPlan:
     def close(self):
         if self.handle:
             lib().xc_fft_plan_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# Ragged batches
+# ---------------------------------------------------------------------------
+def pack(mats, dtype=np.float32):
+    """Stack matrices of any sizes into one flat array + MatrixDesc array."""
+    descs = (MatrixDesc * len(mats))()
+    off = 0
+    for i, m in enumerate(mats):
+        descs[i] = MatrixDesc(off, m.shape[0], m.shape[1])
+        off += m.size
+    flat = np.concatenate([np.ascontiguousarray(m, dtype=dtype).ravel() for m in mats]) if mats else \
+        np.zeros(0, dtype)
+    return flat, descs
+
+
+def pair_layout(lefts, rights, pairs):
+    """PairDesc array and total output elements for (left, right) index pairs."""
+    pd = (PairDesc * len(pairs))()
+    off = 0
+    shapes = []
+    for i, (a, b) in enumerate(pairs):
+        sy = lefts[a].shape[0] + rights[b].shape[0] - 1
+        sx = lefts[a].shape[1] + rights[b].shape[1] - 1
+        pd[i] = PairDesc(a, b, off)
+        shapes.append((off, sy, sx))
+        off += sy * sx
+    return pd, off, shapes
+
+
+class RaggedPlan:
+    """A ragged batch bound to device buffers (xc_ragged_plan_create)."""
+
+    def __init__(self, lefts, rights, pairs, dtype="f32"):
+        import torch
+
+        npdt = np.float32 if dtype == "f32" else np.float64
+        tdt = torch.float32 if dtype == "f32" else torch.float64
+        lflat, self.ldesc = pack(lefts, npdt)
+        rflat, self.rdesc = pack(rights, npdt)
+        self.pdesc, n_out, self.shapes = pair_layout(lefts, rights, pairs)
+        self.left = torch.from_numpy(lflat).cuda()
+        self.right = torch.from_numpy(rflat).cuda()
+        self.out = torch.zeros(n_out, dtype=tdt, device="cuda")
+        self.dtype = dtype
+        self.handle = ctypes.c_void_p()
+        check(lib().xc_ragged_plan_create(ctypes.byref(self.handle), DTYPES[dtype], self.left.data_ptr(), self.ldesc,
+                                          len(lefts), self.right.data_ptr(), self.rdesc, len(rights), self.pdesc,
+                                          len(pairs), self.out.data_ptr()))
+
+    def autotune(self, stream=None):
+        shape = ctypes.c_int()
+        ms = ctypes.c_double()
+        check(lib().xc_ragged_autotune(self.handle, _stream_ptr(stream), ctypes.byref(shape), ctypes.byref(ms)))
+        return shape.value, ms.value
+
+    def execute(self, stream=None):
+        check(lib().xc_ragged_execute(self.handle, _stream_ptr(stream)))
+
+    def per_pair(self, out, stream=None):
+        """The baseline: one plain-kernel launch per pair into `out`."""
+        check(lib().xc_correlate_pairs(DTYPES[self.dtype], self.left.data_ptr(), self.ldesc, len(self.ldesc),
+                                       self.right.data_ptr(), self.rdesc, len(self.rdesc), self.pdesc,
+                                       len(self.pdesc), out.data_ptr(), _stream_ptr(stream)))
+
+    def outputs(self, flat=None):
+        flat = self.out if flat is None else flat
+        host = flat.cpu().numpy()
+        return [host[o:o + sy * sx].reshape(sy, sx) for o, sy, sx in self.shapes]
+
+    def close(self):
+        if self.handle:
+            lib().xc_ragged_plan_destroy(self.handle)
             self.handle = ctypes.c_void_p()
 
     def __del__(self):

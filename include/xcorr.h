@@ -181,6 +181,40 @@ xc_status xc_fft_inverse(xc_fft_plan plan, void* d_out, int normalize, void* d_w
 xc_status xc_fft_plan_destroy(xc_fft_plan plan);
 
 /* ------------------------------------------------------------------------ */
+/* Ragged batches: pairs of matrices of arbitrary, different sizes (new; the */
+/* reference correlates equal sizes only, src/cross_corr.hpp:121-130).      */
+/* ------------------------------------------------------------------------ */
+typedef struct xc_matrix_desc {
+  uint64_t offset; /* elements from the base pointer to the matrix */
+  uint32_t rows;
+  uint32_t cols;
+} xc_matrix_desc;
+typedef struct xc_pair_desc {
+  uint32_t left;       /* index into the left descriptors */
+  uint32_t right;      /* index into the right descriptors */
+  uint64_t out_offset; /* elements from the output base to this pair's (Hl+Hr-1)x(Wl+Wr-1) result */
+} xc_pair_desc;
+typedef struct xc_ragged_plan_s* xc_ragged_plan;
+/* Binds the buffers and prepares padded copies, per-matrix tensor maps and a
+ * work-sorted tile queue, and captures the step (repack, queue reset, one
+ * persistent launch of the plain kernel) into a CUDA graph.  Allocates. */
+xc_status xc_ragged_plan_create(xc_ragged_plan* plan, xc_dtype dtype, const void* d_left,
+                                const xc_matrix_desc* lefts, uint32_t n_left, const void* d_right,
+                                const xc_matrix_desc* rights, uint32_t n_right, const xc_pair_desc* pairs,
+                                uint32_t n_pairs, void* d_out);
+/* Times every candidate tile shape on the plan's batch and keeps the fastest;
+ * decisions are cached by batch signature in $XC_AUTOTUNE_CACHE (default
+ * ~/.cache/xcorr_gb300_autotune.jsonl).  best_ms < 0 when taken from the cache. */
+xc_status xc_ragged_autotune(xc_ragged_plan plan, void* stream, int* chosen_shape, double* best_ms);
+/* Replays the plan's graph on `stream`. */
+xc_status xc_ragged_execute(xc_ragged_plan plan, void* stream);
+xc_status xc_ragged_plan_destroy(xc_ragged_plan plan);
+/* The same batch as one launch of the plain kernel per pair (baseline). */
+xc_status xc_correlate_pairs(xc_dtype dtype, const void* d_left, const xc_matrix_desc* lefts, uint32_t n_left,
+                             const void* d_right, const xc_matrix_desc* rights, uint32_t n_right,
+                             const xc_pair_desc* pairs, uint32_t n_pairs, void* d_out, void* stream);
+
+/* ------------------------------------------------------------------------ */
 /* Kernel-launch layer: drop-ins for the reference's run_* launchers        */
 /* (src/kernels.cuh), typed per element type like its explicit              */
 /* instantiations (src/naive_shuffle.cu:527-651).  Tile arguments are       */

@@ -1,0 +1,99 @@
+"""Ragged batches: pairs of arbitrary sizes through the persistent,
+graph-captured plan and through per-pair launches, against the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_to_max
+from oracle import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import xcorr  # noqa: E402
+
+
+def ragged_batch(n_pairs, lo, hi, seed, dtype=np.float32):
+    rng = np.random.default_rng(seed)
+    lefts, rights = [], []
+    for _ in range(n_pairs):
+        hl, wl, hr, wr = rng.integers(lo, hi + 1, size=4)
+        lefts.append(rng.uniform(-1, 1, (hl, wl)).astype(dtype))
+        rights.append(rng.uniform(-1, 1, (hr, wr)).astype(dtype))
+    # edge shapes: strips and single elements
+    lefts += [np.ones((1, 37), dtype), rng.uniform(-1, 1, (45, 1)).astype(dtype), np.full((1, 1), 2, dtype)]
+    rights += [rng.uniform(-1, 1, (3, 5)).astype(dtype), rng.uniform(-1, 1, (1, 1)).astype(dtype),
+               rng.uniform(-1, 1, (17, 9)).astype(dtype)]
+    return lefts, rights, [(i, i) for i in range(len(lefts))]
+
+
+@pytest.fixture(autouse=True)
+def isolated_cache(tmp_path, monkeypatch):
+    monkeypatch.setenv("XC_AUTOTUNE_CACHE", str(tmp_path / "autotune.jsonl"))
+
+
+def check_outputs(outs, lefts, rights, pairs, dtype="f32acc64", tol=1e-5):
+    refs = oracle.run_pairs([lefts[a] for a, _ in pairs], [rights[b] for _, b in pairs], dtype=dtype, threads=8)
+    assert len(outs) == len(refs)
+    for k, (o, r) in enumerate(zip(outs, refs)):
+        assert o.shape == r.shape, k
+        assert rel_to_max(o, r) <= tol, k
+
+
+def test_ragged_plan_matches_oracle_and_per_pair_launches():
+    lefts, rights, pairs = ragged_batch(24, 5, 90, 7)
+    plan = xcorr.RaggedPlan(lefts, rights, pairs)
+    plan.execute()
+    torch.cuda.synchronize()
+    outs = plan.outputs()
+    check_outputs(outs, lefts, rights, pairs)
+    base = torch.zeros_like(plan.out)
+    plan.per_pair(base)
+    torch.cuda.synchronize()
+    check_outputs(plan.outputs(base), lefts, rights, pairs)
+    plan.close()
+
+
+def test_ragged_autotune_and_graph_replay_with_new_data():
+    lefts, rights, pairs = ragged_batch(16, 10, 140, 8)
+    plan = xcorr.RaggedPlan(lefts, rights, pairs)
+    shape, ms = plan.autotune()
+    assert shape in (0, 1) and ms > 0
+    # the graph re-reads the bound input buffers on every execution
+    rng = np.random.default_rng(9)
+    lefts2 = [rng.uniform(-1, 1, a.shape).astype(np.float32) for a in lefts]
+    plan.left.copy_(torch.from_numpy(xcorr.pack(lefts2)[0]))
+    for _ in range(2):
+        plan.execute()
+    torch.cuda.synchronize()
+    check_outputs(plan.outputs(), lefts2, rights, pairs)
+    # a second plan of the same batch takes the cached decision
+    plan2 = xcorr.RaggedPlan(lefts, rights, pairs)
+    shape2, ms2 = plan2.autotune()
+    assert shape2 == shape and ms2 < 0
+    assert os.path.exists(os.environ["XC_AUTOTUNE_CACHE"])
+    plan.close()
+    plan2.close()
+
+
+def test_ragged_fp64():
+    lefts, rights, pairs = ragged_batch(8, 4, 40, 10, np.float64)
+    plan = xcorr.RaggedPlan(lefts, rights, pairs, dtype="f64")
+    plan.execute()
+    torch.cuda.synchronize()
+    check_outputs(plan.outputs(), lefts, rights, pairs, dtype="f64", tol=1e-12)
+    plan.close()
+
+
+def test_ragged_shared_matrices_n_to_m_style():
+    """Pairs may reuse matrices (a ragged n_to_m: every left with every right)."""
+    rng = np.random.default_rng(11)
+    lefts = [rng.uniform(-1, 1, (h, w)).astype(np.float32) for h, w in [(20, 33), (7, 64), (50, 12)]]
+    rights = [rng.uniform(-1, 1, (h, w)).astype(np.float32) for h, w in [(9, 9), (31, 17)]]
+    pairs = [(a, b) for a in range(3) for b in range(2)]
+    plan = xcorr.RaggedPlan(lefts, rights, pairs)
+    plan.execute()
+    torch.cuda.synchronize()
+    check_outputs(plan.outputs(), lefts, rights, pairs)
+    plan.close()
