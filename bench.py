@@ -315,6 +315,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if plain is not None:
         line["plain_fp32"] = plain
+    if rank == 0 and not args.no_ragged:
+        line["ragged_n_to_m"] = ragged_study(torch, xcorr)
     if rank == 0 and not args.no_cpu_baseline:
         rate, dt = cpu_reference_rate(left, right, 16, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": rate, "unit": "correlations/s", "cores": os.cpu_count() or 1,
@@ -322,6 +324,53 @@ def run_ours(args, rank, world, local_rank):
                                                           "restated in C, T=float"}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def ragged_study(torch, xcorr, reps=5):
+    """Ragged n_to_m batch (512 pairs, every side drawn from U{16..512}, values
+    U[-1,1), seed 4): the persistent, graph-captured plan with its autotuned
+    tile shape against one plain-kernel launch per pair."""
+    import tempfile
+
+    from oracle import oracle
+
+    os.environ.setdefault("XC_AUTOTUNE_CACHE", os.path.join(tempfile.gettempdir(), "xcorr_bench_autotune.jsonl"))
+    rng = np.random.default_rng(4)
+    lefts, rights = [], []
+    for _ in range(512):
+        hl, wl, hr, wr = rng.integers(16, 513, size=4)
+        lefts.append(rng.uniform(-1, 1, (hl, wl)).astype(np.float32))
+        rights.append(rng.uniform(-1, 1, (hr, wr)).astype(np.float32))
+    pairs = [(i, i) for i in range(512)]
+    plan = xcorr.RaggedPlan(lefts, rights, pairs)
+    shape, tune_ms = plan.autotune()
+    base = torch.zeros_like(plan.out)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_graph = timed(plan.execute)
+    ms_pairs = timed(lambda: plan.per_pair(base))
+    outs, outs_b = plan.outputs(), plan.outputs(base)
+    diff = max(oracle.max_rel_to_max(a, b) for a, b in zip(outs, outs_b))
+    small = sorted(range(512), key=lambda i: lefts[i].size * rights[i].size)[:24]
+    refs = oracle.run_pairs([lefts[i] for i in small], [rights[i] for i in small], threads=os.cpu_count() or 1)
+    err = max(oracle.max_rel_to_max(outs[i], r) for i, r in zip(small, refs))
+    flops = sum(2.0 * l.size * r.size for l, r in zip(lefts, rights))
+    plan.close()
+    return {"pairs": 512, "sides": "U{16..512} each of Hl, Wl, Hr, Wr", "values": "U[-1,1)", "seed": 4,
+            "persistent_graph_ms": ms_graph, "per_pair_launches_ms": ms_pairs, "speedup": ms_pairs / ms_graph,
+            "autotuned_tile_shape": shape, "autotune_ms": tune_ms,
+            "correlations_per_s": 512 / (ms_graph / 1000.0), "tflops": flops / (ms_graph / 1000.0) / 1e12,
+            "max_rel_err_vs_oracle_24_smallest_pairs": err, "max_rel_diff_graph_vs_per_pair": diff}
 
 
 def gpu_launches(method, steps):
@@ -339,6 +388,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="tc_bf16x3", choices=["direct", "fft", "tc_bf16x3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ragged", action="store_true", help="skip the ragged n_to_m side study")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I" + INCLUDE, "-I" + CSRC]
 CUDA_SOURCES = ["xc_runtime.cu", "direct_simt.cu", "ragged.cu", "fft_glue.cu", "fft_pipeline.cu", "tc_bf16x3.cu",
-                "api.cu"]
+                "mlp.cu", "api.cu"]
 CLI_SOURCES = ["main.cpp", "data_array.cpp", "json_args.cpp", "algorithms.cpp"]
 
 

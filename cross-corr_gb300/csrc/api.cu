@@ -3,10 +3,14 @@
 // launchers for the reference's run_* kernel-launch layer (src/kernels.cuh).
 #include <cufft.h>
 
+#include <algorithm>
+#include <cmath>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <tuple>
+#include <vector>
 
 #include "xc_common.cuh"
 #include "xc_internal.h"
@@ -117,9 +121,82 @@ size_t fft_workspace_bytes(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t
   return (size_t)(n_left + n_right) * bins * ce + (size_t)n_out * bins * ce + 256;
 }
 
+// ---------------------------------------------------------------------------
+// Method selection for XC_METHOD_AUTO: the MLP's prediction when weights are
+// installed, else the last exhaustive-autotune result for the problem, else
+// the plain kernel.
+// ---------------------------------------------------------------------------
+std::mutex g_sel_mutex;
+std::vector<float> g_sel_params;  // empty: no network installed
+using SelKey = std::tuple<int, int, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t>;
+std::map<SelKey, xc_method> g_tuned;
+
+bool method_supported(xc_method m, xc_dtype dtype, xc_size2 left, xc_size2 right) {
+  if (m == XC_METHOD_TC_BF16X3) return dtype == XC_F32 && left.x + right.x - 1 <= 512 && right.x <= 256;
+  return m == XC_METHOD_DIRECT || m == XC_METHOD_FFT;
+}
+
+void selector_features(xc_mode mode, xc_size2 left, uint32_t n_left, xc_size2 right, uint32_t n_right,
+                       uint64_t n_out, float* f) {
+  const double la = std::log2((double)left.x * left.y), ra = std::log2((double)right.x * right.y);
+  f[0] = (float)(la / 22.0);
+  f[1] = (float)(ra / 22.0);
+  f[2] = (float)(std::log2((double)n_out) / 8.0);
+  for (int i = 0; i < 4; ++i) f[3 + i] = (int)mode == i ? 1.0f : 0.0f;
+  f[7] = (float)((la + ra + std::log2((double)n_out)) / 64.0);
+  (void)n_left;
+  (void)n_right;
+}
+
+// Host copy of the network's forward pass (same arithmetic as mlp.cu).
+void host_forward(const std::vector<float>& P, const float* x, float* y) {
+  const int IN = XC_MLP_IN, H = XC_MLP_HIDDEN, OUT = XC_MLP_OUT;
+  const float* W1 = P.data();
+  const float* b1 = W1 + H * IN;
+  const float* W2 = b1 + H;
+  const float* b2 = W2 + H * H;
+  const float* W3 = b2 + H;
+  const float* b3 = W3 + OUT * H;
+  float h1[XC_MLP_HIDDEN], h2[XC_MLP_HIDDEN];
+  for (int j = 0; j < H; ++j) {
+    float a = b1[j];
+    for (int i = 0; i < IN; ++i) a = std::fma(W1[j * IN + i], x[i], a);
+    h1[j] = std::max(a, 0.0f);
+  }
+  for (int j = 0; j < H; ++j) {
+    float a = b2[j];
+    for (int k = 0; k < H; ++k) a = std::fma(W2[j * H + k], h1[k], a);
+    h2[j] = std::max(a, 0.0f);
+  }
+  for (int o = 0; o < OUT; ++o) {
+    float a = b3[o];
+    for (int k = 0; k < H; ++k) a = std::fma(W3[o * H + k], h2[k], a);
+    y[o] = a;
+  }
+}
+
+xc_method select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                        uint32_t n_right) {
+  static const xc_method order[XC_MLP_OUT] = {XC_METHOD_DIRECT, XC_METHOD_FFT, XC_METHOD_TC_BF16X3};
+  std::lock_guard<std::mutex> lock(g_sel_mutex);
+  PairMap pm;
+  uint64_t n_out = 1;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out)) return XC_METHOD_DIRECT;
+  if (!g_sel_params.empty()) {
+    float f[XC_MLP_IN], y[XC_MLP_OUT];
+    selector_features(mode, left, n_left, right, n_right, n_out, f);
+    host_forward(g_sel_params, f, y);
+    int best = -1;
+    for (int o = 0; o < XC_MLP_OUT; ++o)
+      if (method_supported(order[o], dtype, left, right) && (best < 0 || y[o] < y[best])) best = o;
+    return best >= 0 ? order[best] : XC_METHOD_DIRECT;
+  }
+  auto it = g_tuned.find(SelKey{(int)mode, (int)dtype, left.x, left.y, n_left, right.x, right.y, n_right});
+  return it != g_tuned.end() ? it->second : XC_METHOD_DIRECT;
+}
+
 xc_method resolve(xc_method m, xc_dtype dtype) {
   (void)dtype;
-  if (m == XC_METHOD_AUTO) return XC_METHOD_DIRECT;
   return m;
 }
 
@@ -184,7 +261,7 @@ xc_status xc_workspace_size(xc_mode mode, xc_dtype dtype, xc_method method, xc_s
   PairMap pm;
   uint64_t n_out;
   if (!make_pair_map(mode, n_left, n_right, &pm, &n_out)) return fail(XC_ERR_INVALID_ARGUMENT, "invalid counts");
-  method = resolve(method, dtype);
+  if (method == XC_METHOD_AUTO) method = select_method(mode, dtype, left, n_left, right, n_right);
   switch (method) {
     case XC_METHOD_DIRECT: *bytes = 0; return XC_OK;
     case XC_METHOD_FFT: *bytes = fft_workspace_bytes(mode, dtype, left, n_left, right, n_right); return XC_OK;
@@ -208,7 +285,7 @@ xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const voi
   if (!make_pair_map(mode, n_left, n_right, &pm, &n_out))
     return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts for the mode");
   const Geometry g = make_geometry(left, right);
-  method = resolve(method, dtype);
+  if (method == XC_METHOD_AUTO) method = select_method(mode, dtype, left, n_left, right, n_right);
   switch (method) {
     case XC_METHOD_DIRECT: return direct_launch(dtype, d_left, d_right, d_out, g, pm, as_stream(stream), -1);
     case XC_METHOD_FFT: {
@@ -323,6 +400,106 @@ xc_status xc_fft_plan_destroy(xc_fft_plan plan) {
   if (plan == nullptr) return XC_OK;
   fft_plan_destroy(plan->impl);
   delete plan;
+  return XC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Method selector
+// ---------------------------------------------------------------------------
+xc_status xc_selector_features(xc_mode mode, xc_size2 left, uint32_t n_left, xc_size2 right, uint32_t n_right,
+                               float* features) {
+  if (features == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "features is NULL");
+  XC_TRY(check_sizes(left, right));
+  uint64_t n_out = 0;
+  XC_TRY(xc_output_count(mode, n_left, n_right, &n_out));
+  selector_features(mode, left, n_left, right, n_right, n_out, features);
+  return XC_OK;
+}
+
+xc_status xc_mlp_forward(const float* d_params, const float* d_x, uint32_t n, float* d_y, void* stream) {
+  if (d_params == nullptr || d_x == nullptr || d_y == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");
+  return mlp_forward(d_params, d_x, n, d_y, as_stream(stream));
+}
+
+xc_status xc_mlp_gradient(const float* d_params, const float* d_x, const float* d_target, const float* d_mask,
+                          uint32_t n, float mask_count, float* d_grad, float* d_loss, void* stream) {
+  if (d_params == nullptr || d_x == nullptr || d_target == nullptr || d_mask == nullptr || d_grad == nullptr ||
+      d_loss == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");
+  return mlp_gradient(d_params, d_x, d_target, d_mask, n, mask_count, d_grad, d_loss, as_stream(stream));
+}
+
+xc_status xc_mlp_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v, uint32_t step, float lr,
+                           void* stream) {
+  if (d_params == nullptr || d_grad == nullptr || d_m == nullptr || d_v == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");
+  if (step == 0) return fail(XC_ERR_INVALID_ARGUMENT, "Adam steps count from 1");
+  return mlp_adam(d_params, d_grad, d_m, d_v, step, lr, as_stream(stream));
+}
+
+xc_status xc_selector_load(const float* h_params) {
+  std::lock_guard<std::mutex> lock(g_sel_mutex);
+  if (h_params == nullptr) g_sel_params.clear();
+  else g_sel_params.assign(h_params, h_params + XC_MLP_PARAMS);
+  return XC_OK;
+}
+
+xc_status xc_select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                           uint32_t n_right, xc_method* method) {
+  if (method == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "method is NULL");
+  XC_TRY(check_sizes(left, right));
+  uint64_t n_out = 0;
+  XC_TRY(xc_output_count(mode, n_left, n_right, &n_out));
+  *method = select_method(mode, dtype, left, n_left, right, n_right);
+  return XC_OK;
+}
+
+xc_status xc_autotune_method(xc_mode mode, xc_dtype dtype, const void* d_left, xc_size2 left, uint32_t n_left,
+                             const void* d_right, xc_size2 right, uint32_t n_right, void* d_out, void* stream,
+                             xc_method* best, double* best_ms) {
+  if (best == nullptr || best_ms == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL result pointer");
+  cudaStream_t s = as_stream(stream);
+  const xc_method cands[3] = {XC_METHOD_DIRECT, XC_METHOD_FFT, XC_METHOD_TC_BF16X3};
+  cudaEvent_t e0, e1;
+  XC_CUDA_TRY(cudaEventCreate(&e0));
+  XC_CUDA_TRY(cudaEventCreate(&e1));
+  double bms = 1e300;
+  xc_method bm = XC_METHOD_DIRECT;
+  xc_status st = XC_OK;
+  for (xc_method m : cands) {
+    if (!method_supported(m, dtype, left, right)) continue;
+    size_t wb = 0;
+    if ((st = xc_workspace_size(mode, dtype, m, left, n_left, right, n_right, &wb)) != XC_OK) break;
+    void* ws = nullptr;
+    if (wb > 0 && cudaMalloc(&ws, wb) != cudaSuccess) {
+      st = fail(XC_ERR_CUDA, "workspace allocation failed");
+      break;
+    }
+    float ms = 0.f;
+    st = xc_correlate(mode, dtype, m, d_left, left, n_left, d_right, right, n_right, d_out, ws, wb, stream);
+    if (st == XC_OK && cudaEventRecord(e0, s) == cudaSuccess) {
+      for (int r = 0; r < 3 && st == XC_OK; ++r)
+        st = xc_correlate(mode, dtype, m, d_left, left, n_left, d_right, right, n_right, d_out, ws, wb, stream);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      cudaEventElapsedTime(&ms, e0, e1);
+    }
+    cudaFree(ws);
+    if (st != XC_OK) break;
+    if (ms / 3.0 < bms) {
+      bms = ms / 3.0;
+      bm = m;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  XC_TRY(st);
+  {
+    std::lock_guard<std::mutex> lock(g_sel_mutex);
+    g_tuned[SelKey{(int)mode, (int)dtype, left.x, left.y, n_left, right.x, right.y, n_right}] = bm;
+  }
+  *best = bm;
+  *best_ms = bms;
   return XC_OK;
 }
 

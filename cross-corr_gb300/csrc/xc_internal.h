@@ -86,6 +86,13 @@ xc_status correlate_pairs(xc_dtype dtype, const void* d_left, const xc_matrix_de
                           const void* d_right, const xc_matrix_desc* rights, uint32_t n_right,
                           const xc_pair_desc* pairs, uint32_t n_pairs, void* d_out, cudaStream_t stream);
 
+// Selector network (mlp.cu).
+xc_status mlp_forward(const float* params, const float* x, uint32_t n, float* y, cudaStream_t stream);
+xc_status mlp_gradient(const float* params, const float* x, const float* target, const float* mask, uint32_t n,
+                       float mask_count, float* grad, float* loss, cudaStream_t stream);
+xc_status mlp_adam(float* params, const float* grad, float* m, float* v, uint32_t step, float lr,
+                   cudaStream_t stream);
+
 // FFT pipeline (fft_pipeline.cu).
 struct FftPlanImpl;
 xc_status fft_plan_create(FftPlanImpl** plan, xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left,

@@ -47,7 +47,8 @@ EXPORTED = [
     "xc_run_scatter_f32", "xc_run_scatter_f64",
     "xc_normalize_fft_results_f32", "xc_normalize_fft_results_f64",
     "xc_ragged_plan_create", "xc_ragged_autotune", "xc_ragged_execute", "xc_ragged_plan_destroy",
-    "xc_correlate_pairs",
+    "xc_correlate_pairs", "xc_selector_features", "xc_mlp_forward", "xc_mlp_gradient", "xc_mlp_adam_step",
+    "xc_selector_load", "xc_select_method", "xc_autotune_method",
 ]
 
 
@@ -119,6 +120,14 @@ def lib():
         L.xc_ragged_plan_destroy.argtypes = [vp]
         L.xc_correlate_pairs.argtypes = [i, vp, P(MatrixDesc), u32, vp, P(MatrixDesc), u32, P(PairDesc), u32, vp,
                                          vp]
+        f32p = P(c.c_float)
+        L.xc_selector_features.argtypes = [i, Size2, u32, Size2, u32, f32p]
+        L.xc_mlp_forward.argtypes = [vp, vp, u32, vp, vp]
+        L.xc_mlp_gradient.argtypes = [vp, vp, vp, vp, u32, c.c_float, vp, vp, vp]
+        L.xc_mlp_adam_step.argtypes = [vp, vp, vp, vp, u32, c.c_float, vp]
+        L.xc_selector_load.argtypes = [vp]
+        L.xc_select_method.argtypes = [i, i, Size2, u32, Size2, u32, P(i)]
+        L.xc_autotune_method.argtypes = [i, i, vp, Size2, u32, vp, Size2, u32, vp, vp, P(i), P(c.c_double)]
         for t in ("f32", "f64"):
             getattr(L, f"xc_run_ccn_shuffle_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, vp]
             getattr(L, f"xc_run_ccn_shuffle_multimat_right_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, u32, u32,

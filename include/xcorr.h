@@ -215,6 +215,49 @@ xc_status xc_correlate_pairs(xc_dtype dtype, const void* d_left, const xc_matrix
                              const xc_pair_desc* pairs, uint32_t n_pairs, void* d_out, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Method selector (new; the reference picks algorithms and tiles by hand,  */
+/* benchmarking/args_test/*.yml): a 3-layer 64-wide FP32 MLP predicting the */
+/* log run time of each method, trained on timings measured on this GPU.    */
+/* ------------------------------------------------------------------------ */
+#define XC_MLP_IN 8
+#define XC_MLP_HIDDEN 64
+#define XC_MLP_OUT 3 /* direct, fft, tc_bf16x3 */
+#define XC_MLP_PARAMS                                                                                       \
+  (XC_MLP_HIDDEN * XC_MLP_IN + XC_MLP_HIDDEN + XC_MLP_HIDDEN * XC_MLP_HIDDEN + XC_MLP_HIDDEN +            \
+   XC_MLP_OUT * XC_MLP_HIDDEN + XC_MLP_OUT)
+/* The 8 selector features of a problem: log2 of the left area, right area,
+ * output count and multiply-accumulate count (scaled to ~[0,1]) and the mode
+ * one-hot. */
+xc_status xc_selector_features(xc_mode mode, xc_size2 left, uint32_t n_left, xc_size2 right, uint32_t n_right,
+                               float* features);
+/* Batched inference: y[n][3] = MLP(x[n][8]) on the device. */
+xc_status xc_mlp_forward(const float* d_params, const float* d_x, uint32_t n, float* d_y, void* stream);
+/* Gradient of the masked mean-squared error
+ *   loss = sum_{s,o} mask[s][o] (y[s][o] - target[s][o])^2 / mask_count
+ * with respect to the parameters, into d_grad (XC_MLP_PARAMS floats), and the
+ * loss into d_loss (1 float). */
+xc_status xc_mlp_gradient(const float* d_params, const float* d_x, const float* d_target, const float* d_mask,
+                          uint32_t n, float mask_count, float* d_grad, float* d_loss, void* stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8, bias-corrected; step >= 1). */
+xc_status xc_mlp_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v, uint32_t step, float lr,
+                           void* stream);
+/* Installs trained weights (host copy of XC_MLP_PARAMS floats) for
+ * XC_METHOD_AUTO; NULL uninstalls them. */
+xc_status xc_selector_load(const float* h_params);
+/* The method XC_METHOD_AUTO runs for a problem: the network's fastest
+ * prediction among the methods that support it; without weights, the
+ * method xc_autotune_method last measured fastest for this problem, else
+ * XC_METHOD_DIRECT. */
+xc_status xc_select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                           uint32_t n_right, xc_method* method);
+/* Exhaustive autotune (the selector's fallback and judge): times every
+ * method on the given device buffers (CUDA events, synchronising `stream`),
+ * remembers the fastest for this problem and returns it with its time. */
+xc_status xc_autotune_method(xc_mode mode, xc_dtype dtype, const void* d_left, xc_size2 left, uint32_t n_left,
+                             const void* d_right, xc_size2 right, uint32_t n_right, void* d_out, void* stream,
+                             xc_method* best, double* best_ms);
+
+/* ------------------------------------------------------------------------ */
 /* Kernel-launch layer: drop-ins for the reference's run_* launchers        */
 /* (src/kernels.cuh), typed per element type like its explicit              */
 /* instantiations (src/naive_shuffle.cu:527-651).  Tile arguments are       */
