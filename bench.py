@@ -229,7 +229,7 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local_rank) as clk:
+    with ClockSampler(local_rank) as clk, xcorr.kernel_timing() as kt:
         times = timed(step, args.steps)
         torch.cuda.synchronize()
     if world > 1:
@@ -286,7 +286,8 @@ def run_ours(args, rank, world, local_rank):
 
     peaks, peak_src = measured_peaks()
     flops = algorithmic_flops(left.shape, right.shape, pairs)
-    achieved = flops / (ms / 1000.0) / 1e12
+    kernel_ms = kt.total_ms / kt.launches if kt.launches else None
+    achieved = flops / ((kernel_ms if kernel_ms else ms) / 1000.0) / 1e12
     if method == "tc_bf16x3":
         bound, peak, unit = "tensor", float(peaks.get("bf16_tflops", 1900.0)), "TFLOP/s"
         peak_note = f"{peak_src} cuBLAS bf16 burst; algorithmic FP32 flops (3 bf16 products each)"
@@ -295,6 +296,7 @@ def run_ours(args, rank, world, local_rank):
         bound, peak, unit = "fp32", 152 * 128 * 2 * mhz * 1e6 / 1e12, "TFLOP/s"
         peak_note = "nominal FP32 FMA peak (152 SMs x 128 lanes x 2 x max SM clock); no measured SIMT peak exists"
     clocks = clk.summary()
+    kernel_name = "direct_kernel" if method != "tc_bf16x3" else "tc_kernel"
     line = {
         "metric": METRIC, "value": value, "unit": "correlations/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -307,9 +309,14 @@ def run_ours(args, rank, world, local_rank):
                 "h2d_bytes_per_step": int(left.nbytes + right.nbytes), "d2h_bytes_per_step": int(ho.numel() * 4),
                 "api": "xc_correlate_host (pinned host buffers)", "max_abs_diff_vs_device_run": e2e_err},
         "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
-                     "traffic": None, "kernel": "direct_kernel" if method != "tc_bf16x3" else "tc_kernel",
+                     "traffic": profiled_traffic(kernel_name), "kernel": kernel_name,
                      "algorithmic_flops_per_launch": flops, "peak_source": peak_note,
-                     "duration": "CUDA events around the whole xc_correlate call (all its kernels)"},
+                     "kernel_ms": kernel_ms, "kernel_launches_timed": kt.launches,
+                     "kernel_share_of_step": (kernel_ms / ms) if kernel_ms else None,
+                     "duration": "CUDA events around each launch of the kernel on its stream, inside the timed "
+                                 "region (xc_kernel_timing)",
+                     "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum per launch, ncu capture "
+                                       f"summarised in profiles/{kernel_name}_one_to_many_256x64.md"},
         "clocks": clocks,
         "gpu_launches": gpu_launches(method, args.steps),
     }
@@ -317,6 +324,8 @@ def run_ours(args, rank, world, local_rank):
         line["plain_fp32"] = plain
     if rank == 0 and not args.no_ragged:
         line["ragged_n_to_m"] = ragged_study(torch, xcorr)
+    if rank == 0 and not args.no_configs:
+        line["configs"] = config_studies(torch, xcorr)
     if rank == 0 and not args.no_cpu_baseline:
         rate, dt = cpu_reference_rate(left, right, 16, os.cpu_count() or 1)
         line["cpu_baseline"] = {"value": rate, "unit": "correlations/s", "cores": os.cpu_count() or 1,
@@ -373,6 +382,68 @@ def ragged_study(torch, xcorr, reps=5):
             "max_rel_err_vs_oracle_24_smallest_pairs": err, "max_rel_diff_graph_vs_per_pair": diff}
 
 
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` at this workload, read from its
+    committed ncu summary (a line `traffic_bytes_per_launch: N`), or None."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_one_to_many_256x64.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def config_studies(torch, xcorr, reps=20):
+    """The other fixed configurations, each method's rate and error vs FP64:
+    one_to_one 128x128 (U[0,1), seed 1); 8 left + 32 right 64x64 N(0,1)
+    (seed 3) as n_to_mn (32 outputs) and as n_to_m (256 outputs), in FP32 and
+    FP64.  Inputs are small (L2-resident); each rate is the mean of `reps`
+    back-to-back calls after a warm-up call."""
+    from oracle import oracle
+
+    cases = []
+    rng = np.random.default_rng(1)
+    a, b = rng.random((1, 128, 128)), rng.random((1, 128, 128))
+    cases.append(("one_to_one 128x128 U[0,1) seed 1", "one_to_one", a, b))
+    rng = np.random.default_rng(3)
+    a, b = rng.standard_normal((8, 64, 64)), rng.standard_normal((32, 64, 64))
+    cases.append(("n_to_mn 8+32 x 64x64 N(0,1) seed 3", "n_to_mn", a, b))
+    cases.append(("n_to_m 8+32 x 64x64 N(0,1) seed 3", "n_to_m", a, b))
+    out = []
+    threads = os.cpu_count() or 1
+    for name, mode, a, b in cases:
+        for dtype in ("f32", "f64"):
+            np_t = np.float32 if dtype == "f32" else np.float64
+            la, rb = a.astype(np_t), b.astype(np_t)
+            ref = oracle.run_mode(mode, la, rb, dtype="f64" if dtype == "f64" else "f32acc64", threads=threads)
+            dl, dr = torch.from_numpy(la).cuda(), torch.from_numpy(rb).cuda()
+            row = {"config": name, "dtype": dtype, "outputs": int(ref.shape[0])}
+            for method in ("direct", "fft", "tc_bf16x3"):
+                if method == "tc_bf16x3" and dtype == "f64":
+                    continue
+                ws_bytes = xcorr.workspace_size(mode, dtype, method, la.shape[1:], la.shape[0], rb.shape[1:],
+                                                rb.shape[0])
+                ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device="cuda")
+                o = xcorr.correlate(mode, dl, dr, method=method, workspace=ws if ws_bytes else None)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    xcorr.correlate(mode, dl, dr, method=method, out=o, workspace=ws if ws_bytes else None)
+                e1.record()
+                e1.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                host = o.cpu().numpy()
+                err = max(oracle.max_rel_to_max(host[k], ref[k]) for k in range(ref.shape[0]))
+                row[method] = {"correlations_per_s": ref.shape[0] / (ms / 1000.0), "ms": ms,
+                               "max_rel_err_vs_fp64": err}
+            out.append(row)
+    return out
+
+
 def gpu_launches(method, steps):
     # kernels per xc_correlate call: direct 1; fft 2 pads + multiply + normalise
     # (+ cuFFT's own); tc: mean, 2 prefix, split, correction, tcgen05 kernel
@@ -389,6 +460,7 @@ def main():
     ap.add_argument("--method", default="tc_bf16x3", choices=["direct", "fft", "tc_bf16x3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged n_to_m side study")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other fixed configurations")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -127,7 +127,15 @@ size_t fft_workspace_bytes(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t
 // the plain kernel.
 // ---------------------------------------------------------------------------
 std::mutex g_sel_mutex;
+#if __has_include("selector_weights.inc")
+#include "selector_weights.inc"
+#endif
+#ifdef XC_SELECTOR_BUILTIN
+static_assert(sizeof(kSelectorBuiltin) / sizeof(float) == XC_MLP_PARAMS, "built-in selector size");
+std::vector<float> g_sel_params(kSelectorBuiltin, kSelectorBuiltin + XC_MLP_PARAMS);
+#else
 std::vector<float> g_sel_params;  // empty: no network installed
+#endif
 using SelKey = std::tuple<int, int, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t>;
 std::map<SelKey, xc_method> g_tuned;
 
@@ -235,6 +243,13 @@ xc_status xc_check_device(void* stream) { return check_device_flags(as_stream(st
 xc_status xc_debug_expire_wait(uint32_t polls, void* stream) {
   if (polls == 0 || polls > (1u << 24)) return fail(XC_ERR_INVALID_ARGUMENT, "polls must be in [1, 2^24]");
   return debug_expire_wait(polls, as_stream(stream));
+}
+
+xc_status xc_kernel_timing(int enable) { return kernel_timing(enable); }
+
+xc_status xc_kernel_timing_read(double* total_ms, uint32_t* launches) {
+  if (total_ms == nullptr || launches == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL result pointer");
+  return kernel_timing_read(total_ms, launches);
 }
 
 xc_status xc_output_count(xc_mode mode, uint32_t n_left, uint32_t n_right, uint64_t* n_out) {
@@ -442,6 +457,14 @@ xc_status xc_selector_load(const float* h_params) {
   if (h_params == nullptr) g_sel_params.clear();
   else g_sel_params.assign(h_params, h_params + XC_MLP_PARAMS);
   return XC_OK;
+}
+
+xc_status xc_selector_load_builtin(void) {
+#ifdef XC_SELECTOR_BUILTIN
+  return xc_selector_load(kSelectorBuiltin);
+#else
+  return fail(XC_ERR_UNSUPPORTED, "library built without a selector network");
+#endif
 }
 
 xc_status xc_select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,

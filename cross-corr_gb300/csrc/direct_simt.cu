@@ -513,7 +513,9 @@ xc_status launch_uniform(const typename C::type* left, const typename C::type* r
   static_assert(C::SMEM_BYTES <= 227 * 1024, "shared memory budget");
   auto kern = direct_kernel<C>;
   XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES));
+  const int slot = kernel_timer_begin(stream);
   kern<<<(unsigned)blocks, C::NT, C::SMEM_BYTES, stream>>>(lmap, rmap, p, use_tma);
+  kernel_timer_end(slot, stream);
   XC_CUDA_TRY(cudaGetLastError());
   return XC_OK;
 }

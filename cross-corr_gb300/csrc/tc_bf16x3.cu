@@ -775,7 +775,9 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
   auto launch = [&](auto kern) -> xc_status {
     XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
+    const int slot = kernel_timer_begin(stream);
     kern<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
+    kernel_timer_end(slot, stream);
     XC_CUDA_TRY(cudaGetLastError());
     return XC_OK;
   };

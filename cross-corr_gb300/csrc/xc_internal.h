@@ -42,6 +42,14 @@ inline Geometry make_geometry(xc_size2 left, xc_size2 right) {
 
 xc_status debug_expire_wait(uint32_t polls, cudaStream_t stream);
 
+// Optional CUDA-event timing of the dense kernels (xc_kernel_timing).
+// kernel_timer_begin returns a slot (or -1 when timing is off) that
+// kernel_timer_end closes after the launch on the same stream.
+int kernel_timer_begin(cudaStream_t stream);
+void kernel_timer_end(int slot, cudaStream_t stream);
+xc_status kernel_timing(int enable);
+xc_status kernel_timing_read(double* total_ms, uint32_t* launches);
+
 // Plain definition-based correlation (direct_simt.cu).
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
                         const PairMap& pm, cudaStream_t stream, int force_loader /* -1 auto, 0 cp.async, 1 TMA */);

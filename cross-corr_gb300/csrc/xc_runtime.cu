@@ -4,6 +4,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "xc_common.cuh"
 #include "xc_internal.h"
@@ -130,6 +131,69 @@ xc_status debug_expire_wait(uint32_t polls, cudaStream_t stream) {
   if (f == nullptr) return fail(XC_ERR_CUDA, "device flag word unavailable");
   expire_wait_kernel<<<1, 32, 0, stream>>>(f, polls);
   XC_CUDA_TRY(cudaGetLastError());
+  return XC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel timing: event pairs around each dense kernel launch while enabled.
+// Events come from a pool that grows on demand and is reused after a read.
+// ---------------------------------------------------------------------------
+namespace {
+struct KernelTimer {
+  std::mutex mu;
+  bool on = false;
+  std::vector<cudaEvent_t> pool;  // 2 per slot
+  size_t used = 0;                // slots recorded since the last enable
+};
+KernelTimer& ktimer() {
+  static KernelTimer t;
+  return t;
+}
+}  // namespace
+
+int kernel_timer_begin(cudaStream_t stream) {
+  KernelTimer& t = ktimer();
+  std::lock_guard<std::mutex> lock(t.mu);
+  if (!t.on) return -1;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return -1;
+  while (t.pool.size() < 2 * (t.used + 1)) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return -1;
+    t.pool.push_back(e);
+  }
+  const int slot = (int)t.used++;
+  if (cudaEventRecord(t.pool[2 * slot], stream) != cudaSuccess) return -1;
+  return slot;
+}
+
+void kernel_timer_end(int slot, cudaStream_t stream) {
+  if (slot < 0) return;
+  KernelTimer& t = ktimer();
+  std::lock_guard<std::mutex> lock(t.mu);
+  cudaEventRecord(t.pool[2 * slot + 1], stream);
+}
+
+xc_status kernel_timing(int enable) {
+  KernelTimer& t = ktimer();
+  std::lock_guard<std::mutex> lock(t.mu);
+  t.on = enable != 0;
+  t.used = 0;
+  return XC_OK;
+}
+
+xc_status kernel_timing_read(double* total_ms, uint32_t* launches) {
+  KernelTimer& t = ktimer();
+  std::lock_guard<std::mutex> lock(t.mu);
+  double sum = 0.0;
+  for (size_t k = 0; k < t.used; ++k) {
+    XC_CUDA_TRY(cudaEventSynchronize(t.pool[2 * k + 1]));
+    float ms = 0.f;
+    XC_CUDA_TRY(cudaEventElapsedTime(&ms, t.pool[2 * k], t.pool[2 * k + 1]));
+    sum += ms;
+  }
+  *total_ms = sum;
+  *launches = (uint32_t)t.used;
   return XC_OK;
 }
 

@@ -32,7 +32,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "cuFFT error", 4: 
 # Every symbol declared in include/xcorr.h (checked by the CPU test suite).
 EXPORTED = [
     "xc_version", "xc_status_string", "xc_last_error", "xc_device_check", "xc_check_device",
-    "xc_debug_expire_wait", "xc_output_count", "xc_output_size",
+    "xc_debug_expire_wait", "xc_kernel_timing", "xc_kernel_timing_read", "xc_output_count", "xc_output_size",
     "xc_workspace_size", "xc_correlate", "xc_correlate_host", "xc_release_thread_cache", "xc_correlate_tc_noalloc",
     "xc_fft_plan_create", "xc_fft_plan_workspace_size", "xc_fft_plan_pad_size", "xc_fft_execute",
     "xc_fft_forward", "xc_fft_multiply", "xc_fft_inverse", "xc_fft_plan_destroy",
@@ -48,7 +48,7 @@ EXPORTED = [
     "xc_normalize_fft_results_f32", "xc_normalize_fft_results_f64",
     "xc_ragged_plan_create", "xc_ragged_autotune", "xc_ragged_execute", "xc_ragged_plan_destroy",
     "xc_correlate_pairs", "xc_selector_features", "xc_mlp_forward", "xc_mlp_gradient", "xc_mlp_adam_step",
-    "xc_selector_load", "xc_select_method", "xc_autotune_method",
+    "xc_selector_load", "xc_selector_load_builtin", "xc_select_method", "xc_autotune_method",
 ]
 
 
@@ -97,6 +97,8 @@ def lib():
         L.xc_device_check.argtypes = [i]
         L.xc_check_device.argtypes = [vp]
         L.xc_debug_expire_wait.argtypes = [u32, vp]
+        L.xc_kernel_timing.argtypes = [i]
+        L.xc_kernel_timing_read.argtypes = [c.POINTER(c.c_double), c.POINTER(u32)]
         L.xc_output_count.argtypes = [i, u32, u32, c.POINTER(c.c_uint64)]
         L.xc_output_size.argtypes = [Size2, Size2, c.POINTER(Size2)]
         L.xc_workspace_size.argtypes = [i, i, i, Size2, u32, Size2, u32, c.POINTER(sz)]
@@ -222,6 +224,26 @@ def correlate_host(mode: str, left: np.ndarray, right: np.ndarray, method: str =
                                   right.ctypes.data, size2(hr, wr), m, out.ctypes.data,
                                   None if stream is None else int(stream)))
     return out
+
+
+class kernel_timing:
+    """Context manager: CUDA-event time of the dense correlation kernels
+    (plain and split-BF16) launched inside the block.  After exit,
+    `total_ms` and `launches` hold the summed kernel time and the count."""
+
+    def __enter__(self):
+        check(lib().xc_kernel_timing(1))
+        self.total_ms, self.launches = 0.0, 0
+        return self
+
+    def __exit__(self, *exc):
+        ms, n = ctypes.c_double(), ctypes.c_uint32()
+        try:
+            check(lib().xc_kernel_timing_read(ctypes.byref(ms), ctypes.byref(n)))
+        finally:
+            lib().xc_kernel_timing(0)
+        self.total_ms, self.launches = ms.value, n.value
+        return False
 
 
 class FftPlan:

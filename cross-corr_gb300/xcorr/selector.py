@@ -146,8 +146,11 @@ def standardise(T, M):
 
 
 def install(params):
-    """Make XC_METHOD_AUTO use these weights (None uninstalls)."""
-    if params is None:
+    """Make XC_METHOD_AUTO use these weights (None uninstalls any network,
+    "builtin" reinstalls the network compiled into the library)."""
+    if isinstance(params, str) and params == "builtin":
+        check(lib().xc_selector_load_builtin())
+    elif params is None:
         check(lib().xc_selector_load(None))
     else:
         p = np.ascontiguousarray(params, dtype=np.float32)
@@ -159,3 +162,39 @@ def select(mode, dtype, left_shape, n_left, right_shape, n_right):
     check(lib().xc_select_method(MODES[mode], DTYPES[dtype], size2(*left_shape), n_left, size2(*right_shape),
                                  n_right, ctypes.byref(m)))
     return {v: k for k, v in METHODS.items()}[m.value]
+
+
+def autotune(mode, left, right, out, stream=None):
+    """Exhaustive autotune (xc_autotune_method) on device tensors: returns the
+    fastest method's name and its time in ms."""
+    import torch
+    n_l, hl, wl = left.shape
+    n_r, hr, wr = right.shape
+    dtype = "f32" if left.dtype == torch.float32 else "f64"
+    m = ctypes.c_int()
+    ms = ctypes.c_double()
+    st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
+    check(lib().xc_autotune_method(MODES[mode], DTYPES[dtype], left.data_ptr(), size2(hl, wl), n_l, right.data_ptr(),
+                                   size2(hr, wr), n_r, out.data_ptr(), st, ctypes.byref(m), ctypes.byref(ms)))
+    return {v: k for k, v in METHODS.items()}[m.value], ms.value
+
+
+def time_method(mode, left, right, out, method, reps=5):
+    """Mean CUDA-event time (ms) of one correlation with `method`, workspace
+    allocated outside the timed calls."""
+    import torch
+    from . import correlate, workspace_size
+    n_l, hl, wl = left.shape
+    n_r, hr, wr = right.shape
+    dtype = "f32" if left.dtype == torch.float32 else "f64"
+    wb = workspace_size(mode, dtype, method, (hl, wl), n_l, (hr, wr), n_r)
+    ws = torch.empty(max(wb, 1), dtype=torch.uint8, device=left.device)
+    correlate(mode, left, right, method=method, out=out, workspace=ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        correlate(mode, left, right, method=method, out=out, workspace=ws)
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps

@@ -83,6 +83,16 @@ xc_status xc_check_device(void* stream);
  * one block that waits on a shared-memory mbarrier nothing completes, gives up
  * after `polls` polls, records the expiry and returns.  No fault, no hang. */
 xc_status xc_debug_expire_wait(uint32_t polls, void* stream);
+/* Kernel timing (new, no reference counterpart; the reference times whole
+ * steps with its stopwatch, src/stopwatch.hpp:57-71).  While enabled, every
+ * launch of a dense correlation kernel (the plain kernel and the split-BF16
+ * tensor kernel; not the ragged plan, which runs as a captured graph) is
+ * bracketed by CUDA events on its own stream.  xc_kernel_timing_read waits
+ * for the recorded events and returns the summed kernel time and the launch
+ * count since the last enable.  Enabling clears the record; the record is
+ * process-wide. */
+xc_status xc_kernel_timing(int enable);
+xc_status xc_kernel_timing_read(double* total_ms, uint32_t* launches);
 
 /* ------------------------------------------------------------------------ */
 /* Geometry (src/validate.hpp:190-214 result_matrix_size / counts)          */
@@ -242,8 +252,12 @@ xc_status xc_mlp_gradient(const float* d_params, const float* d_x, const float* 
 xc_status xc_mlp_adam_step(float* d_params, const float* d_grad, float* d_m, float* d_v, uint32_t step, float lr,
                            void* stream);
 /* Installs trained weights (host copy of XC_MLP_PARAMS floats) for
- * XC_METHOD_AUTO; NULL uninstalls them. */
+ * XC_METHOD_AUTO; NULL uninstalls them.  The library starts with the
+ * network trained on its own GB300 timings installed. */
 xc_status xc_selector_load(const float* h_params);
+/* Reinstalls that built-in network (XC_ERR_UNSUPPORTED if the library was
+ * built without one). */
+xc_status xc_selector_load_builtin(void);
 /* The method XC_METHOD_AUTO runs for a problem: the network's fastest
  * prediction among the methods that support it; without weights, the
  * method xc_autotune_method last measured fastest for this problem, else
