@@ -31,7 +31,7 @@ def baselines(times, M, X):
 
 
 def write_inc(path, params, source, steps, seed):
-    vals = ",\n".join(", ".join(f"{float(v):.9g}f" for v in params[i:i + 6]) for i in range(0, len(params), 6))
+    vals = ",\n".join(", ".join(f"{float(v):.9e}f" for v in params[i:i + 6]) for i in range(0, len(params), 6))
     with open(path, "w") as f:
         f.write(f"// Default weights of the method selector (XC_MLP_PARAMS floats in the layout of\n"
                 f"// mlp.cu), trained by selector/train.py on {source}\n"
