@@ -36,6 +36,11 @@ TC_SHAPES = [
     ("one_to_many", 1, 9, (64, 64), (64, 64), "uniform"),
     ("n_to_m", 2, 16, (30, 70), (30, 66), "signed"),
     ("one_to_many", 1, 64, (40, 48), (40, 48), "uniform"),
+    # narrow left rows under wide shift ranges: windowed MMAs over part of the
+    # B rows; right widths that leave empty K-steps in the last 64-column chunk
+    ("one_to_many", 1, 3, (12, 40), (10, 200), "uniform"),
+    ("one_to_one", 1, 1, (9, 100), (7, 250), "normal"),
+    ("n_to_m", 2, 3, (16, 256), (12, 256), "signed"),
 ]
 
 
