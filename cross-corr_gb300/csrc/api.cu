@@ -203,11 +203,6 @@ xc_method select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_
   return it != g_tuned.end() ? it->second : XC_METHOD_DIRECT;
 }
 
-xc_method resolve(xc_method m, xc_dtype dtype) {
-  (void)dtype;
-  return m;
-}
-
 }  // namespace
 
 extern "C" {

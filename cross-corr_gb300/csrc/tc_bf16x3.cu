@@ -65,9 +65,8 @@ constexpr int kStageBytes = 2 * kTileBytes;
 constexpr int kEpiWarps = 8;        // epilogue warps (2 per TMEM lane quadrant)
 constexpr int kThreads = 32 * (4 + kEpiWarps);
 constexpr int kMaxLeftCols = 512;   // staged centred left row (Sx <= 512 on this path)
-// 15 mbarriers (120 B), the abort flag and the TMEM address slot
+// 17 mbarriers (136 B), the abort flag and the TMEM address slot
 constexpr int kBarBytes = 256;
-constexpr uint32_t kARingCol = 256;  // first TMEM column of the right-row ring
 
 struct TcParams {
   const float* left;
@@ -80,7 +79,6 @@ struct TcParams {
   int n_pgroups;    // ceil(K / P)
   int n_dytiles;    // ceil(Sy / DY)
   int N;            // B rows per phase (multiple of 16, 8N >= Sx)
-  int Nw;           // B rows of one windowed MMA (multiple of 16, <= N): covers every non-zero row of a K-step
   int nkc;          // 64-column chunks of a right row
   int buf_len;      // elements of one phase copy (multiple of 8)
   int flush_rows;   // drain TMEM every this many left rows
@@ -149,23 +147,6 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Copies a 128-row x 256-bit (16 BF16) K-slice of a shared-memory tile,
-// described like an MMA operand, into 128 lanes x 8 columns of tensor memory.
-__device__ __forceinline__ void tmem_cp_128x256b(uint32_t taddr, uint64_t sdesc) {
-  asm volatile("tcgen05.cp.cta_group::1.128x256b [%0], %1;" ::"r"(taddr), "l"(sdesc) : "memory");
-}
-
-// D[tmem] (+)= A[tmem] * B[smem]^T.
-__device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
-                                            uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void red_add(float* addr, float v) {
@@ -213,11 +194,9 @@ template <int N>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
               const TcParams p) {
-  constexpr int kPhases = 4;             // column phases handled by this CTA
-  constexpr int kHalfN = N / 2;          // B rows per phase drained by one epilogue warp
-  constexpr int kAcc = kPhases * kHalfN;  // accumulators per epilogue thread
-  constexpr uint32_t kCols = 512;        // TMEM: [0, 4N) accumulators, [256, 512) right-row ring
-  static_assert(kPhases * N <= (int)kARingCol, "accumulators overlap the right-row ring");
+  constexpr int kPhases = 4;            // column phases handled by this CTA
+  constexpr int kDCols = kPhases * N;   // TMEM columns of one accumulator buffer
+  constexpr int kAcc = 2 * N;           // accumulators per epilogue thread (4 phases x N/2)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -230,9 +209,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* a_empty = bars + kStages;
   uint64_t* b_full = bars + 2 * kStages;
   uint64_t* b_empty = b_full + 2;
-  uint64_t* t_full = b_empty + 2;
-  uint64_t* t_empty = t_full + 1;
-  uint64_t* mma_done = t_empty + 1;
+  uint64_t* t_full = b_empty + 2;   // [2]
+  uint64_t* t_empty = t_full + 2;   // [2]
+  uint64_t* mma_done = t_empty + 2;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 1);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 2);
 
@@ -256,6 +235,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (n_rows <= 0) return;  // uniform over the CTA
   const int n_drains = (n_rows + p.flush_rows - 1) / p.flush_rows;
   const int rdim2 = p.pm.r_l != 0 ? l : 0;
+  constexpr uint32_t ncols = 2 * kDCols <= 32 ? 32u : (2 * kDCols <= 64 ? 64u : (2 * kDCols <= 128 ? 128u : (2 * kDCols <= 256 ? 256u : 512u)));
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -267,9 +247,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int s = 0; s < 2; ++s) {
       mbar_init(&b_full[s], 64);
       mbar_init(&b_empty[s], 1);
+      mbar_init(&t_full[s], 1);
+      mbar_init(&t_empty[s], 32 * kEpiWarps);
     }
-    mbar_init(t_full, 1);
-    mbar_init(t_empty, 32 * kEpiWarps);
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     fence_mbar_init();
@@ -278,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(kCols)
+                 "r"(ncols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -326,12 +306,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const uint32_t idesc_full = idesc_bf16_f32(128, N);
-      const uint32_t idesc_win = idesc_bf16_f32(128, p.Nw);
+      const uint32_t idesc = idesc_bf16_f32(128, N);
       const uint32_t a_base = smem_u32(a_tiles);
       const uint32_t b_base = smem_u32(b_bufs);
       const uint32_t copy_bytes = (uint32_t)p.buf_len * 2;
-      int it = 0, rows_in = 0, windows = 0;
+      int it = 0, buf = 0, rows_in = 0;
+      uint32_t uses[2] = {0u, 0u};
       bool ok = true;
       for (int ai = 0; ai < n_rows && ok; ++ai) {
         const int bs = ai & 1;
@@ -340,14 +320,15 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         if (rows_in == 0) {
-          // the epilogue must have drained the previous window
-          if (!wait_or_abort(t_empty, (windows & 1) ^ 1, abort_flag, p.flags, 14)) {
+          // the epilogue must have drained this buffer's previous use
+          if (!wait_or_abort(&t_empty[buf], (uses[buf] & 1) ^ 1, abort_flag, p.flags, 14)) {
             ok = false;
             break;
           }
         }
         tc_fence_after();
         const uint32_t bslot = b_base + (uint32_t)bs * (uint32_t)b_slot_elems * 2;
+        const uint32_t dbase = tmem_base + (uint32_t)(buf * kDCols);
         for (int kc = 0; kc < p.nkc; ++kc, ++it) {
           const int s = it % kStages;
           if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13)) {
@@ -355,44 +336,23 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           tc_fence_after();
-          // right-row tiles of this stage -> TMEM ring slot s (4 K-steps x (hi, lo) x 8 columns)
           const uint32_t a_hi_addr = a_base + (uint32_t)s * kStageBytes;
-          const uint32_t ring = tmem_base + kARingCol + (uint32_t)s * 64;
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            tmem_cp_128x256b(ring + ks * 16, smem_desc(a_hi_addr + ks * 32, 16, 1024, 2));
-            tmem_cp_128x256b(ring + ks * 16 + 8, smem_desc(a_hi_addr + kTileBytes + ks * 32, 16, 1024, 2));
-          }
+          const uint32_t a_lo_addr = a_hi_addr + kTileBytes;
 #pragma unroll 1
           for (int ks = 0; ks < 4; ++ks) {
-            const int k0 = kc * 64 + ks * 16;
-            const bool first = rows_in == 0 && k0 == 0;
-            if (k0 >= p.Wr && !first) continue;  // right columns past the row: all zero
-            const uint32_t ahi = ring + ks * 16, alo = ahi + 8;
-            const uint32_t koff = (uint32_t)k0 * 2;
+            const uint64_t ahi = smem_desc(a_hi_addr + ks * 32, 16, 1024, 2);
+            const uint64_t alo = smem_desc(a_lo_addr + ks * 32, 16, 1024, 2);
+            const uint32_t koff = (uint32_t)(kc * 64 + ks * 16) * 2;
+            const uint32_t acc0 = (rows_in == 0 && kc == 0 && ks == 0) ? 0u : 1u;
 #pragma unroll
             for (int c = 0; c < kPhases; ++c) {
-              // B rows n with a non-zero Toeplitz entry in this K-step:
-              // 0 <= cg + 8n + k0 + k - (Wr - 1) < Wl for some k in [0, 16)
-              const int cg = half * kPhases + c;
-              int n0 = 0;
-              uint32_t id = idesc_full;
-              if (!first) {
-                const int lo_num = p.Wr - 16 - cg - k0, hi_num = p.Wr + p.Wl - 2 - cg - k0;
-                const int n_lo = max(0, -((-lo_num) >> 3));
-                const int n_hi = min(N - 1, hi_num >> 3);
-                if (n_lo > n_hi) continue;
-                n0 = min(n_lo & ~7, N - p.Nw);
-                if (n_hi < n0 + p.Nw) id = idesc_win;
-                else n0 = 0;
-              }
-              const uint32_t bhi_addr = bslot + (uint32_t)c * 2 * copy_bytes + koff + (uint32_t)n0 * 16;
+              const uint32_t bhi_addr = bslot + (uint32_t)c * 2 * copy_bytes + koff;
               const uint64_t bhi = smem_desc(bhi_addr, 16, 128, 0);
               const uint64_t blo = smem_desc(bhi_addr + copy_bytes, 16, 128, 0);
-              const uint32_t d = tmem_base + (uint32_t)(c * N + n0);
-              mma_bf16_ts(d, ahi, bhi, id, first ? 0u : 1u);
-              mma_bf16_ts(d, ahi, blo, id, 1u);
-              mma_bf16_ts(d, alo, bhi, id, 1u);
+              const uint32_t d = dbase + (uint32_t)(c * N);
+              mma_bf16(d, ahi, bhi, idesc, acc0);
+              mma_bf16(d, ahi, blo, idesc, 1u);
+              mma_bf16(d, alo, bhi, idesc, 1u);
             }
           }
           mma_commit(&a_empty[s]);
@@ -401,8 +361,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         mma_commit(&b_empty[bs]);
         ++rows_in;
         if (rows_in == p.flush_rows || ai == n_rows - 1) {
-          mma_commit(t_full);
-          ++windows;
+          mma_commit(&t_full[buf]);
+          ++uses[buf];
+          buf ^= 1;
           rows_in = 0;
         }
       }
@@ -453,6 +414,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // warps 4..11: lane quadrant q, B-row half e: phases 0..3, rows n in
     // [e*N/2, (e+1)*N/2) of each.  acc[c * N/2 + n'] is shift
     // sx = half*4 + c + 8 * (e*N/2 + n').
+    constexpr int kHalfN = N / 2;
     const int q = warp & 3;
     const int e = (warp - 4) >> 2;
     float acc[kAcc];
@@ -460,12 +422,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int i = 0; i < kAcc; ++i) acc[i] = 0.0f;
     bool ok = true;
     for (int d = 0; d < n_drains; ++d) {
-      if (!wait_or_abort(t_full, d & 1, abort_flag, p.flags, 16)) {
+      const int b = d & 1;
+      if (!wait_or_abort(&t_full[b], (d >> 1) & 1, abort_flag, p.flags, 16)) {
         ok = false;
         break;
       }
       tc_fence_after();
-      const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(e * kHalfN);
+      const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kDCols + e * kHalfN);
 #pragma unroll
       for (int c = 0; c < kPhases; ++c) {
 #pragma unroll
@@ -486,12 +449,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       tc_fence_before();
-      mbar_arrive(t_empty);
+      mbar_arrive(&t_empty[b]);
     }
     if (ok) {
       // Coalesced reduction into the output: each warp stages 32 rows x 32
       // consecutive owned shifts at a time in shared memory (the right-row
-      // stages are idle once the last window is drained), then adds row by
+      // stages are idle once the last buffer is drained), then adds row by
       // row, so one warp instruction covers 32 owned shifts of one row.
       fence_proxy_async_shared();
       float* stage = reinterpret_cast<float*>(a_tiles) + (warp - 4) * (32 * 33);
@@ -532,7 +495,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(kCols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(ncols) : "memory");
   }
 }
 
@@ -669,7 +632,7 @@ __global__ void correction_kernel(float* __restrict__ out, const double* __restr
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, N, Nw, nkc, buf_len, pitch;
+  int P, DY, mats_mode, N, nkc, buf_len, pitch;
   int smem_bytes;
 };
 
@@ -684,10 +647,6 @@ bool tc_plan(const Geometry& g, const PairMap& pm, TcPlan* t) {
   N = (N + 15) / 16 * 16;
   if (N < 16) N = 16;
   t->N = N;
-  // A K-step of 16 right columns meets at most floor((Wl + 14) / 8) + 2 B rows
-  // with non-zero entries; the window starts on a multiple of 8.
-  int Nw = ((g.Wl + 14) / 8 + 2 + 7 + 15) / 16 * 16;
-  t->Nw = std::min(N, Nw);
   t->nkc = (g.Wr + 63) / 64;
   t->buf_len = t->nkc * 64 + 8 * N;
   t->pitch = (g.Wr + 7) / 8 * 8;
@@ -842,7 +801,6 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.n_pgroups = div_up(pm.K, t.P);
   prm.n_dytiles = div_up(g.Sy, t.DY);
   prm.N = t.N;
-  prm.Nw = t.Nw;
   prm.nkc = t.nkc;
   prm.buf_len = t.buf_len;
   prm.flush_rows = flush_rows(t.nkc);
