@@ -7,24 +7,27 @@
 // Formulation (implicit GEMM).  For a left row a and a right row b the
 // contribution to output row sy = a - b + Hr - 1 is a 1D correlation, a
 // Toeplitz matrix-vector product.  One tcgen05.mma computes
-//     D[m][n] += sum_k A[m][k] * B[n][k]        (M=128, N<=64, K=16, BF16)
+//     D[m][n] += sum_k A[m][k] * B[n][k]        (M=128, N=128, K=16, BF16)
 // with
-//   m -> (partner matrix p, row shift dy): A[m][k] = R_p[a - dy][k0 + k]
-//        (right rows, staged by TMA with 128-byte swizzle, K-major);
-//   n -> column shift sx = c + 8n for a phase c in 0..7:
-//        B[n][k] = Lpad_a[c + 8n + k0 + k]
-//        where Lpad_a[j] = L[a][j - (Wr-1)] (zero outside the row).
-// B is a Toeplitz matrix.  It is read straight out of one shared-memory copy
-// of the (split) left row per phase c: a no-swizzle K-major descriptor whose
-// 8x16-byte core matrices overlap (leading byte offset 16 = 8 elements along
-// K, stride byte offset 128 = 64 elements along N) addresses element
-// 8n + k of the copy.  Nothing is materialised per shift; eight phase copies
-// of each left row cover every column shift.
+//   m -> column shift sx = s0 + m of a 128-shift tile:
+//        A[m][k] = Lp_a[s0 + m + k0 + k], Lp_a[j] = L[a][j - (Wr-1)] (zero
+//        outside the row).  A is a Toeplitz matrix; builder warps write it
+//        straight into tensor memory (tcgen05.st), one lane per shift, from
+//        a staged copy of the left row.
+//   n -> (partner matrix p, row shift dy): B[n][k] = R_p[a - dy][k0 + k]
+//        (right rows, staged by TMA with 128-byte swizzle, K-major).
+// N = 128 keeps each MMA at the tensor pipe's full rate (narrower MMAs are
+// bound by a per-instruction cost of ~44 cycles on GB300, measured), and the
+// shift axis lies along M, so K-steps whose 128 shifts see only zeros are
+// skipped (a quarter of them at Wl = Wr).
 //
-// The accumulator tile is 128 lanes x (8 phases x N) FP32 columns of tensor
-// memory.  Every `flush_rows` left rows the epilogue warps drain it into the
-// output with FP32 reductions (red.global.add), so long row ranges can also
-// be split over several CTAs; the MMA warp waits during a drain.
+// Each CTA owns two shift tiles (256 shifts) of one (partner group, row-shift
+// group, chunk of left rows); a second CTA owns the other two when
+// Sx > 256.  Tensor memory holds the two FP32 accumulator tiles (256
+// columns) and a two-slot ring of split Toeplitz operands (256 columns).
+// Every `flush_rows` left rows the epilogue warps drain the accumulators into
+// FP32 registers; at the end they add them to the output with coalesced
+// red.global.add (consecutive lanes are consecutive shifts).
 //
 // Accuracy.  Tensor-core FP32 accumulation drops low bits on every MMA with a
 // consistent sign, so the error of a long chain grows linearly with its
@@ -36,13 +39,14 @@
 //   out = corr(L', R') + mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area
 // (S = sum of the centred matrix over the overlap of a shift, from FP64 2D
 // prefix sums) is written first by a correction kernel, which the tensor-core
-// drains then accumulate into.
+// results are then added to.  The drains bound every accumulator's chain at
+// 192 MMAs.
 //
-// Warp roles (256 threads, one CTA per SM):
-//   warp 0    TMA producer of the right-row tiles (hi and lo planes)
-//   warp 1    TMEM allocation and the single-thread MMA issuer
-//   warps 2-3 build the eight phase copies of each split left row
-//   warps 4-7 epilogue (tcgen05.ld -> shared staging -> coalesced global)
+// Warp roles (704 threads, one CTA per SM):
+//   warp 0      TMA producer of the right-row tiles (hi and lo planes)
+//   warp 1      TMEM allocation and the single-thread MMA issuer
+//   warps 2-5   Toeplitz builders (one per TMEM lane quadrant)
+//   warps 6-21  epilogue: 4 per lane quadrant, 64 accumulator columns each
 // All waits are bounded: an expired wait records a flag, the CTA winds down,
 // waits (bounded) for its own copies and MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
@@ -59,14 +63,15 @@ namespace xc {
 
 namespace {
 
-constexpr int kStages = 4;          // right-row tile pipeline depth
+constexpr int kStages = 4;             // right-row tile pipeline depth
 constexpr int kTileBytes = 128 * 128;  // 128 rows x 64 bf16 (one plane)
 constexpr int kStageBytes = 2 * kTileBytes;
-constexpr int kEpiWarps = 8;        // epilogue warps (2 per TMEM lane quadrant)
-constexpr int kThreads = 32 * (4 + kEpiWarps);
-constexpr int kMaxLeftCols = 512;   // staged centred left row (Sx <= 512 on this path)
-// 17 mbarriers (136 B), the abort flag and the TMEM address slot
-constexpr int kBarBytes = 256;
+constexpr int kBuilderWarps = 4;       // one per TMEM lane quadrant
+constexpr int kEpiWarps = 16;          // four per TMEM lane quadrant
+constexpr int kThreads = 32 * (2 + kBuilderWarps + kEpiWarps);
+constexpr int kMaxLp = 512 + 256;      // staged left row: 128 * tiles + 64 * chunks
+constexpr uint32_t kRingCol = 256;     // first TMEM column of the Toeplitz ring
+constexpr int kBarBytes = 256;         // 15 mbarriers, the abort flag, the TMEM address slot
 
 struct TcParams {
   const float* left;
@@ -74,13 +79,13 @@ struct TcParams {
   float* out;
   int Hl, Wl, Hr, Wr, Sy, Sx;
   PairMap pm;
-  int P, DY;        // partners x row shifts per tile, P*DY = 128
+  int P, DY;        // partners x row shifts per B tile, P*DY = 128
   int mats_mode;    // 1: one TMA box per row shift spans P partners; 0: one box per partner spans DY rows
   int n_pgroups;    // ceil(K / P)
   int n_dytiles;    // ceil(Sy / DY)
-  int N;            // B rows per phase (multiple of 16, 8N >= Sx)
+  int n_halves;     // CTAs per work item (two 128-shift tiles each)
   int nkc;          // 64-column chunks of a right row
-  int buf_len;      // elements of one phase copy (multiple of 8)
+  int lp_len;       // staged left row length
   int flush_rows;   // drain TMEM every this many left rows
   int chunk_rows;   // left rows per CTA (a longer row range is split over CTAs)
   int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
@@ -90,32 +95,28 @@ struct TcParams {
 // ---------------------------------------------------------------------------
 // tcgen05 / descriptor helpers
 // ---------------------------------------------------------------------------
-// Shared-memory matrix descriptor (sm_100 family): start>>4 [0,14), LBO>>4
-// [16,30), SBO>>4 [32,46), version 1 at bit 46, layout type [61,64)
-// (0 = no swizzle, 2 = 128-byte swizzle).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo, uint32_t layout) {
-  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  d |= (uint64_t)(layout & 7u) << 61;
-  return d;
-}
-
+// Shared-memory matrix descriptors are assembled from two 32-bit words:
+// low word = start>>4 [0,14) | LBO>>4 [16,30); high word = SBO>>4 [0,14) |
+// version 1 at bit 14 | layout type at bits [29,32) (2 = 128-byte swizzle).
 // Instruction descriptor, kind::f16: D=F32 (bits 4-5 = 1), A=B=BF16 (bits 7-9,
 // 10-12 = 1), both K-major, N>>3 at bit 17, M>>4 at bit 24.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
+// D[tmem] (+)= A[tmem] * B[smem]^T.
+__device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
+}
+
+__device__ __forceinline__ uint64_t make_desc(uint32_t lo, uint32_t hi) {
+  return ((uint64_t)hi << 32) | (uint64_t)lo;
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
@@ -190,35 +191,58 @@ __device__ __forceinline__ int centre_out(int r, int n, int tc) {
   return above > below ? tc + m + extra : tc - m - extra;
 }
 
-template <int N>
+// Active K-steps of a 128-shift tile starting at s0: bit j is set when
+// A's K-step j (columns 16j..16j+15 of the right row) meets a left column.
+__device__ __forceinline__ uint32_t tile_mask(int s0, const TcParams& p) {
+  uint32_t m = 0;
+  if (s0 >= p.Sx) return 0;
+  for (int j = 0; j < 4 * p.nkc; ++j) {
+    const int k0 = 16 * j;
+    if (k0 < p.Wr && s0 + k0 + 142 >= p.Wr - 1 && s0 + k0 <= p.Wr + p.Wl - 2) m |= 1u << j;
+  }
+  return m;
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
+
+// 22 warps: at most 6 on one SM sub-partition, whose 16K registers cap a
+// thread at 80.
 __global__ void __launch_bounds__(kThreads, 1)
     tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
               const TcParams p) {
-  constexpr int kPhases = 4;            // column phases handled by this CTA
-  constexpr int kDCols = kPhases * N;   // TMEM columns of one accumulator buffer
-  constexpr int kAcc = 2 * N;           // accumulators per epilogue thread (4 phases x N/2)
+  constexpr int kCols = 64;  // accumulator columns per epilogue warp
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* a_tiles = smem;  // kStages x (hi, lo) x 16 KB
-  __nv_bfloat16* b_bufs = reinterpret_cast<__nv_bfloat16*>(smem + kStages * kStageBytes);
-  const int b_slot_elems = kPhases * 2 * p.buf_len;  // 4 phases x (hi, lo) per slot
-  float* lrows = reinterpret_cast<float*>(b_bufs + 2 * b_slot_elems);  // 2 x kMaxLeftCols
-  uint64_t* bars = reinterpret_cast<uint64_t*>(lrows + 2 * kMaxLeftCols);
-  uint64_t* a_full = bars;
-  uint64_t* a_empty = bars + kStages;
-  uint64_t* b_full = bars + 2 * kStages;
-  uint64_t* b_empty = b_full + 2;
-  uint64_t* t_full = b_empty + 2;   // [2]
-  uint64_t* t_empty = t_full + 2;   // [2]
-  uint64_t* mma_done = t_empty + 2;
+  unsigned char* b_tiles = smem;                                                  // kStages x (hi, lo) x 16 KB
+  float* lp_buf = reinterpret_cast<float*>(smem + kStages * kStageBytes);         // 2 x kMaxLp
+  long long* row_base = reinterpret_cast<long long*>(lp_buf + 2 * kMaxLp);        // 128 output row offsets
+  uint64_t* bars = reinterpret_cast<uint64_t*>(row_base + 128);
+  uint64_t* a_full = bars;              // [kStages] right-row tiles landed
+  uint64_t* a_empty = bars + kStages;   // [kStages] tiles consumed
+  uint64_t* s_full = bars + 2 * kStages;  // [2] Toeplitz ring slot written
+  uint64_t* s_empty = s_full + 2;         // [2] ring slot consumed
+  uint64_t* t_full = s_empty + 2;         // accumulators ready to drain
+  uint64_t* t_empty = t_full + 1;         // accumulators drained
+  uint64_t* mma_done = t_empty + 1;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 1);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 2);
 
   // ---- work item of this CTA ---------------------------------------------
-  // blockIdx = ((chunk * n_dytiles + rank) * per_rank + lp) * 2 + half
-  const int half = blockIdx.x & 1;
-  const int bid = blockIdx.x >> 1;
+  // blockIdx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_halves + half
+  const int half = blockIdx.x % p.n_halves;
+  const int bid = blockIdx.x / p.n_halves;
   const int per_rank = p.pm.n_left * p.n_pgroups;
   const int lp = bid % per_rank;
   const int rank = (bid / per_rank) % p.n_dytiles;
@@ -235,7 +259,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (n_rows <= 0) return;  // uniform over the CTA
   const int n_drains = (n_rows + p.flush_rows - 1) / p.flush_rows;
   const int rdim2 = p.pm.r_l != 0 ? l : 0;
-  constexpr uint32_t ncols = 2 * kDCols <= 32 ? 32u : (2 * kDCols <= 64 ? 64u : (2 * kDCols <= 128 ? 128u : (2 * kDCols <= 256 ? 256u : 512u)));
+  const int s0_0 = 256 * half, s0_1 = s0_0 + 128;
+  const uint32_t mask0 = tile_mask(s0_0, p), mask1 = tile_mask(s0_1, p);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -245,11 +270,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&a_empty[s], 1);
     }
     for (int s = 0; s < 2; ++s) {
-      mbar_init(&b_full[s], 64);
-      mbar_init(&b_empty[s], 1);
-      mbar_init(&t_full[s], 1);
-      mbar_init(&t_empty[s], 32 * kEpiWarps);
+      mbar_init(&s_full[s], 32 * kBuilderWarps);
+      mbar_init(&s_empty[s], 1);
     }
+    mbar_init(t_full, 1);
+    mbar_init(t_empty, 32 * kEpiWarps);
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     fence_mbar_init();
@@ -258,7 +283,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(ncols)
+                 "r"(512)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -281,7 +306,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           mbar_arrive_expect_tx(&a_full[s], kStageBytes);
-          unsigned char* hi = a_tiles + s * kStageBytes;
+          unsigned char* hi = b_tiles + s * kStageBytes;
           unsigned char* lo = hi + kTileBytes;
           if (p.mats_mode) {
             for (int d = 0; d < p.DY; ++d) {
@@ -306,64 +331,55 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(128, N);
-      const uint32_t a_base = smem_u32(a_tiles);
-      const uint32_t b_base = smem_u32(b_bufs);
-      const uint32_t copy_bytes = (uint32_t)p.buf_len * 2;
-      int it = 0, buf = 0, rows_in = 0;
-      uint32_t uses[2] = {0u, 0u};
+      constexpr uint32_t kDescHi = (1024u >> 4) | (1u << 14) | (2u << 29);  // SBO 1024 B, 128-byte swizzle
+      const uint32_t idesc = idesc_bf16_f32(128, 128);
+      const uint32_t b_lo_word = ((smem_u32(b_tiles) >> 4) & 0x3FFFu) | (1u << 16);
+      const int first0 = mask0 ? __ffs(mask0) - 1 : -1;
+      const int first1 = mask1 ? __ffs(mask1) - 1 : -1;
+      int it = 0, rows_in = 0, windows = 0;
       bool ok = true;
       for (int ai = 0; ai < n_rows && ok; ++ai) {
-        const int bs = ai & 1;
-        if (!wait_or_abort(&b_full[bs], (ai >> 1) & 1, abort_flag, p.flags, 12)) {
-          ok = false;
-          break;
-        }
         if (rows_in == 0) {
-          // the epilogue must have drained this buffer's previous use
-          if (!wait_or_abort(&t_empty[buf], (uses[buf] & 1) ^ 1, abort_flag, p.flags, 14)) {
+          // the epilogue must have drained the previous window
+          if (!wait_or_abort(t_empty, (windows & 1) ^ 1, abort_flag, p.flags, 14)) {
             ok = false;
             break;
           }
         }
-        tc_fence_after();
-        const uint32_t bslot = b_base + (uint32_t)bs * (uint32_t)b_slot_elems * 2;
-        const uint32_t dbase = tmem_base + (uint32_t)(buf * kDCols);
         for (int kc = 0; kc < p.nkc; ++kc, ++it) {
-          const int s = it % kStages;
-          if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13)) {
+          const int s = it & (kStages - 1), slot = it & 1;
+          if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13) ||
+              !wait_or_abort(&s_full[slot], (it >> 1) & 1, abort_flag, p.flags, 12)) {
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t a_hi_addr = a_base + (uint32_t)s * kStageBytes;
-          const uint32_t a_lo_addr = a_hi_addr + kTileBytes;
-#pragma unroll 1
-          for (int ks = 0; ks < 4; ++ks) {
-            const uint64_t ahi = smem_desc(a_hi_addr + ks * 32, 16, 1024, 2);
-            const uint64_t alo = smem_desc(a_lo_addr + ks * 32, 16, 1024, 2);
-            const uint32_t koff = (uint32_t)(kc * 64 + ks * 16) * 2;
-            const uint32_t acc0 = (rows_in == 0 && kc == 0 && ks == 0) ? 0u : 1u;
+          const uint32_t bw = b_lo_word + (uint32_t)s * (kStageBytes >> 4);
+          const uint32_t ring = tmem_base + kRingCol + (uint32_t)slot * 128;
 #pragma unroll
-            for (int c = 0; c < kPhases; ++c) {
-              const uint32_t bhi_addr = bslot + (uint32_t)c * 2 * copy_bytes + koff;
-              const uint64_t bhi = smem_desc(bhi_addr, 16, 128, 0);
-              const uint64_t blo = smem_desc(bhi_addr + copy_bytes, 16, 128, 0);
-              const uint32_t d = dbase + (uint32_t)(c * N);
-              mma_bf16(d, ahi, bhi, idesc, acc0);
-              mma_bf16(d, ahi, blo, idesc, 1u);
-              mma_bf16(d, alo, bhi, idesc, 1u);
+          for (int ks = 0; ks < 4; ++ks) {
+            const int j = kc * 4 + ks;
+            const uint64_t bhi = make_desc(bw + ks * 2, kDescHi);
+            const uint64_t blo = make_desc(bw + (kTileBytes >> 4) + ks * 2, kDescHi);
+#pragma unroll
+            for (int tt = 0; tt < 2; ++tt) {
+              if (!(((tt == 0 ? mask0 : mask1) >> j) & 1u)) continue;
+              const bool reset = rows_in == 0 && j == (tt == 0 ? first0 : first1);
+              const uint32_t ahi = ring + (uint32_t)(tt * 4 + ks) * 16, alo = ahi + 8;
+              const uint32_t d = tmem_base + (uint32_t)tt * 128;
+              mma_bf16_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
+              mma_bf16_ts(d, ahi, blo, idesc, 1u);
+              mma_bf16_ts(d, alo, bhi, idesc, 1u);
             }
           }
           mma_commit(&a_empty[s]);
+          mma_commit(&s_empty[slot]);
         }
         if (!ok) break;
-        mma_commit(&b_empty[bs]);
         ++rows_in;
         if (rows_in == p.flush_rows || ai == n_rows - 1) {
-          mma_commit(&t_full[buf]);
-          ++uses[buf];
-          buf ^= 1;
+          mma_commit(t_full);
+          ++windows;
           rows_in = 0;
         }
       }
@@ -371,122 +387,120 @@ __global__ void __launch_bounds__(kThreads, 1)
       mma_commit(mma_done);
       mbar_wait_bounded(mma_done, 0, 1u << 22);
     }
-  } else if (warp < 4) {
-    // ------------------------------------------------------------ B builders
-    const int bt = threadIdx.x - 64;  // 0..63
+  } else if (warp < 2 + kBuilderWarps) {
+    // ------------------------------------------------------------ Toeplitz builders
+    // Lane m of TMEM quadrant q (m = 32 q + lane) is shift s0 + m; per K-step
+    // it writes 8 columns of packed hi pairs and 8 of lo pairs.
+    const int bt = threadIdx.x - 64;  // 0..127
+    const int qd = warp & 3;
+    const int m = 32 * qd + lane;
+    const uint32_t lane_addr = tmem_base + ((uint32_t)(32 * qd) << 16) + kRingCol;
     const float* lrow_base = p.left + (long long)l * p.Hl * p.Wl;
     const float mu = p.mu_left[l];
-    const int nvec = p.buf_len / 8;
+    int it = 0;
+    bool ok = true;
     for (int ai = 0; ai < n_rows; ++ai) {
-      const int bs = ai & 1;
-      const bool ok = wait_or_abort(&b_empty[bs], ((ai >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
-      // the 64 builder threads leave together (they share a named barrier)
-      if (bar_red_or(!ok, 1, 64)) break;
-      // stage the centred left row (coalesced), then build the phase copies
-      float* lr = lrows + bs * kMaxLeftCols;
+      // stage the centred, zero-padded left row: lp[j] = L[a][j - (Wr-1)] - mu
+      float* lpr = lp_buf + (ai & 1) * kMaxLp;
       const float* src = lrow_base + (long long)(a_lo + ai) * p.Wl;
-      for (int x = bt; x < p.Wl; x += 64) lr[x] = __ldg(src + x) - mu;
-      asm volatile("bar.sync 1, 64;" ::: "memory");
-      __nv_bfloat16* slot = b_bufs + bs * b_slot_elems;
-      for (int item = bt; item < kPhases * nvec; item += 64) {
-        const int cl = item / nvec, jv = item % nvec;
-        const int c = half * kPhases + cl;
-        const int j0 = jv * 8 + c - (p.Wr - 1);  // left column of element 0
-        __align__(16) __nv_bfloat16 hi[8];
-        __align__(16) __nv_bfloat16 lo[8];
-#pragma unroll
-        for (int e = 0; e < 8; ++e) {
-          const int x = j0 + e;
-          const float v = (x >= 0 && x < p.Wl) ? lr[x] : 0.0f;
-          const __nv_bfloat16 h = __float2bfloat16_rn(v);
-          hi[e] = h;
-          lo[e] = __float2bfloat16_rn(v - __bfloat162float(h));
-        }
-        __nv_bfloat16* dst = slot + (cl * 2) * p.buf_len + jv * 8;
-        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(hi);
-        *reinterpret_cast<uint4*>(dst + p.buf_len) = *reinterpret_cast<const uint4*>(lo);
+      for (int j = bt; j < p.lp_len; j += 32 * kBuilderWarps) {
+        const int x = j - (p.Wr - 1);
+        lpr[j] = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
       }
-      fence_proxy_async_shared();
-      mbar_arrive(&b_full[bs]);
+      // the builder threads leave together (they share a named barrier)
+      if (bar_red_or(!ok, 1, 32 * kBuilderWarps)) break;
+      for (int kc = 0; kc < p.nkc; ++kc, ++it) {
+        const int slot = it & 1;
+        bool w = wait_or_abort(&s_empty[slot], ((it >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
+        w = __all_sync(0xffffffffu, w);  // tcgen05.st below must stay warp-uniform
+        if (!w) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+#pragma unroll
+        for (int tt = 0; tt < 2; ++tt) {
+#pragma unroll
+          for (int ks = 0; ks < 4; ++ks) {
+            const int j = kc * 4 + ks;
+            if (!(((tt == 0 ? mask0 : mask1) >> j) & 1u)) continue;
+            const float* v = lpr + (tt == 0 ? s0_0 : s0_1) + m + 16 * j;
+            uint32_t r[16];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              const float x0 = v[2 * e], x1 = v[2 * e + 1];
+              const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+              const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h));
+              r[e] = bf16x2_bits(h);
+              r[8 + e] = bf16x2_bits(lo);
+            }
+            tmem_st16(lane_addr + (uint32_t)slot * 128 + (uint32_t)(tt * 4 + ks) * 16, r);
+          }
+        }
+        tmem_wait_st();
+        tc_fence_before();
+        mbar_arrive(&s_full[slot]);
+      }
     }
   } else {
     // ------------------------------------------------------------ epilogue
-    // warps 4..11: lane quadrant q, B-row half e: phases 0..3, rows n in
-    // [e*N/2, (e+1)*N/2) of each.  acc[c * N/2 + n'] is shift
-    // sx = half*4 + c + 8 * (e*N/2 + n').
-    constexpr int kHalfN = N / 2;
+    // Warp w (index ew = w - 6): lane quadrant q = w % 4, accumulator
+    // columns [64 * (ew / 4), +64): tile tt = ew / 8, B rows nb.. of it.
+    const int ew = warp - (2 + kBuilderWarps);
     const int q = warp & 3;
-    const int e = (warp - 4) >> 2;
-    float acc[kAcc];
+    const int tt = ew >> 3;
+    const int nb = ((ew >> 2) & 1) * kCols;
+    const int et = threadIdx.x - 32 * (2 + kBuilderWarps);  // 0..511
+    if (et < 128) {
+      // output row offset of B row n (-1: outside the output)
+      const int n = et;
+      int pp, dy;
+      if (p.mats_mode) {
+        pp = n % p.P;
+        dy = dy0 + n / p.P;
+      } else {
+        pp = n / p.DY;
+        dy = dy0 + (p.DY - 1) - (n % p.DY);
+      }
+      const int k = p0 + pp, sy = dy + p.Hr - 1;
+      row_base[n] = (k < p.pm.K && sy >= 0 && sy < p.Sy)
+                        ? (((long long)l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx
+                        : -1LL;
+    }
+    asm volatile("bar.sync 2, %0;" ::"r"(32 * kEpiWarps) : "memory");
+    float acc[kCols];
 #pragma unroll
-    for (int i = 0; i < kAcc; ++i) acc[i] = 0.0f;
+    for (int i = 0; i < kCols; ++i) acc[i] = 0.0f;
+    const bool live = (tt == 0 ? mask0 : mask1) != 0u;
     bool ok = true;
     for (int d = 0; d < n_drains; ++d) {
-      const int b = d & 1;
-      if (!wait_or_abort(&t_full[b], (d >> 1) & 1, abort_flag, p.flags, 16)) {
+      bool w = wait_or_abort(t_full, d & 1, abort_flag, p.flags, 16);
+      w = __all_sync(0xffffffffu, w);  // tcgen05.ld below must stay warp-uniform
+      if (!w) {
         ok = false;
         break;
       }
       tc_fence_after();
-      const uint32_t lane_base = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * kDCols + e * kHalfN);
+      if (live) {
+        const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(tt * 128 + nb);
 #pragma unroll
-      for (int c = 0; c < kPhases; ++c) {
-#pragma unroll
-        for (int j = 0; j + 16 <= kHalfN; j += 16) {
-          float v[16];
-          tmem_ld16(lane_base + (uint32_t)(c * N + j), v);
-          tmem_wait_ld();
-#pragma unroll
-          for (int i = 0; i < 16; ++i) acc[c * kHalfN + j + i] += v[i];
-        }
-        if constexpr (kHalfN % 16 != 0) {
-          constexpr int j = kHalfN - 8;
+        for (int j = 0; j < kCols; j += 8) {
           float v[8];
-          tmem_ld8(lane_base + (uint32_t)(c * N + j), v);
+          tmem_ld8(col0 + (uint32_t)j, v);
           tmem_wait_ld();
 #pragma unroll
-          for (int i = 0; i < 8; ++i) acc[c * kHalfN + j + i] += v[i];
+          for (int i = 0; i < 8; ++i) acc[j + i] += v[i];
         }
       }
       tc_fence_before();
-      mbar_arrive(&t_empty[b]);
+      mbar_arrive(t_empty);
     }
-    if (ok) {
-      // Coalesced reduction into the output: each warp stages 32 rows x 32
-      // consecutive owned shifts at a time in shared memory (the right-row
-      // stages are idle once the last buffer is drained), then adds row by
-      // row, so one warp instruction covers 32 owned shifts of one row.
-      fence_proxy_async_shared();
-      float* stage = reinterpret_cast<float*>(a_tiles) + (warp - 4) * (32 * 33);
-      // output row of this lane's accumulator row m (-1: outside the output)
-      long long row_base = -1;
-      {
-        const int m = q * 32 + lane;
-        int pp, dy;
-        if (p.mats_mode) {
-          pp = m % p.P;
-          dy = dy0 + m / p.P;
-        } else {
-          pp = m / p.DY;
-          dy = dy0 + (p.DY - 1) - (m % p.DY);
-        }
-        const int k = p0 + pp, sy = dy + p.Hr - 1;
-        if (k < p.pm.K && sy >= 0 && sy < p.Sy)
-          row_base = (((long long)l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx;
-      }
+    const int sx = (tt == 0 ? s0_0 : s0_1) + 32 * q + lane;
+    if (ok && live && sx < p.Sx) {
 #pragma unroll
-      for (int h = 0; h < kAcc / 32; ++h) {
-        // owned shift index s' = 4 n' + c in [32h, 32h + 32)
-#pragma unroll
-        for (int i = 0; i < 32; ++i) stage[lane * 33 + i] = acc[(i & 3) * kHalfN + 8 * h + (i >> 2)];
-        __syncwarp();
-        const int sp = 32 * h + lane;
-        const int sx = half * kPhases + (sp & 3) + 8 * (e * kHalfN + (sp >> 2));
-        for (int r = 0; r < 32; ++r) {
-          const long long rb = __shfl_sync(0xffffffffu, row_base, r);
-          if (rb >= 0 && sx < p.Sx) red_add(p.out + rb + sx, stage[r * 33 + lane]);
-        }
-        __syncwarp();
+      for (int i = 0; i < kCols; ++i) {
+        const long long rb = row_base[nb + i];
+        if (rb >= 0) red_add(p.out + rb + sx, acc[i]);
       }
     }
   }
@@ -495,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   tc_fence_after();
   if (warp == 1) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(ncols) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512) : "memory");
   }
 }
 
@@ -632,26 +646,24 @@ __global__ void correction_kernel(float* __restrict__ out, const double* __restr
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, N, nkc, buf_len, pitch;
+  int P, DY, mats_mode, n_tiles, n_halves, nkc, lp_len, pitch;
   int smem_bytes;
 };
 
 bool tc_plan(const Geometry& g, const PairMap& pm, TcPlan* t) {
-  if (g.Sx > 512 || g.Wr > 256) return false;  // 8 phases x N <= 512 TMEM columns
+  if (g.Sx > 512 || g.Wr > 256) return false;  // four 128-shift tiles, 16 K-steps
   int P = 1;
   while (P < 128 && P < pm.K) P *= 2;
   t->P = P;
   t->DY = 128 / P;
   t->mats_mode = P >= 8 ? 1 : 0;
-  int N = (g.Sx + 7) / 8;
-  N = (N + 15) / 16 * 16;
-  if (N < 16) N = 16;
-  t->N = N;
+  t->n_tiles = (g.Sx + 127) / 128;
+  t->n_halves = (t->n_tiles + 1) / 2;
   t->nkc = (g.Wr + 63) / 64;
-  t->buf_len = t->nkc * 64 + 8 * N;
+  t->lp_len = 128 * t->n_tiles + 64 * t->nkc;
   t->pitch = (g.Wr + 7) / 8 * 8;
-  t->smem_bytes = 1024 + kStages * kStageBytes + 2 * 4 * 2 * t->buf_len * 2 + 2 * kMaxLeftCols * 4 + kBarBytes;
-  return t->smem_bytes <= 227 * 1024;
+  t->smem_bytes = 1024 + kStages * kStageBytes + 2 * kMaxLp * 4 + 128 * 8 + kBarBytes;
+  return t->lp_len <= kMaxLp && t->smem_bytes <= 227 * 1024;
 }
 
 long long n_right_of(const PairMap& pm) {
@@ -800,30 +812,23 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.mats_mode = t.mats_mode;
   prm.n_pgroups = div_up(pm.K, t.P);
   prm.n_dytiles = div_up(g.Sy, t.DY);
-  prm.N = t.N;
+  prm.n_halves = t.n_halves;
   prm.nkc = t.nkc;
-  prm.buf_len = t.buf_len;
+  prm.lp_len = t.lp_len;
   prm.flush_rows = flush_rows(t.nkc);
   prm.chunk_rows = chunk_rows();
   prm.n_chunks = div_up(t.DY - 1 + std::min(g.Hl, g.Hr), prm.chunk_rows);
   prm.flags = device_flags();
 
-  const long long blocks = 2LL * prm.n_chunks * prm.n_dytiles * pm.n_left * prm.n_pgroups;
+  const long long blocks =
+      (long long)t.n_halves * prm.n_chunks * prm.n_dytiles * pm.n_left * prm.n_pgroups;
   if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
-  auto launch = [&](auto kern) -> xc_status {
-    XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
-    const int slot = kernel_timer_begin(stream);
-    kern<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
-    kernel_timer_end(slot, stream);
-    XC_CUDA_TRY(cudaGetLastError());
-    return XC_OK;
-  };
-  switch (t.N) {
-    case 16: return launch(tc_kernel<16>);
-    case 32: return launch(tc_kernel<32>);
-    case 48: return launch(tc_kernel<48>);
-    default: return launch(tc_kernel<64>);
-  }
+  XC_CUDA_TRY(cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
+  const int slot = kernel_timer_begin(stream);
+  tc_kernel<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
+  kernel_timer_end(slot, stream);
+  XC_CUDA_TRY(cudaGetLastError());
+  return XC_OK;
 }
 
 // ---------------------------------------------------------------------------
