@@ -63,13 +63,13 @@ namespace xc {
 
 namespace {
 
-constexpr int kStages = 4;             // right-row tile pipeline depth
+constexpr int kStages = 6;             // right-row tile pipeline depth
 constexpr int kTileBytes = 128 * 128;  // 128 rows x 64 bf16 (one plane)
 constexpr int kStageBytes = 2 * kTileBytes;
 constexpr int kBuilderWarps = 4;       // one per TMEM lane quadrant
 constexpr int kEpiWarps = 16;          // four per TMEM lane quadrant
 constexpr int kThreads = 32 * (2 + kBuilderWarps + kEpiWarps);
-constexpr int kMaxLp = 512 + 256;      // staged left row: 128 * tiles + 64 * chunks
+constexpr int kMaxLp = 512 + 256;      // staged left row pairs: 128 * tiles + 64 * chunks
 constexpr uint32_t kRingCol = 256;     // first TMEM column of the Toeplitz ring
 constexpr int kBarBytes = 256;         // 15 mbarriers, the abort flag, the TMEM address slot
 
@@ -166,6 +166,20 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, vo
   return false;
 }
 
+// The same for roles that wait long and should not take issue slots from
+// the MMA issuer: each poll sleeps up to 20 us (woken early when the phase
+// completes); at most 2^17 polls.
+__device__ __forceinline__ bool wait_or_abort_sleep(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                                    DeviceFlags* flags, unsigned where) {
+  for (uint32_t i = 0; i < (1u << 17); ++i) {
+    if (mbar_try_wait_sleep(bar, parity, 20000u)) return true;
+    if (*abort_flag) return false;
+  }
+  *abort_flag = 1;
+  record_timeout(flags, where);
+  return false;
+}
+
 // OR-reduction over the threads of named barrier `id` (also a barrier).
 __device__ __forceinline__ bool bar_red_or(bool v, int id, int nthreads) {
   uint32_t r;
@@ -226,8 +240,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* b_tiles = smem;                                                  // kStages x (hi, lo) x 16 KB
-  float* lp_buf = reinterpret_cast<float*>(smem + kStages * kStageBytes);         // 2 x kMaxLp
-  long long* row_base = reinterpret_cast<long long*>(lp_buf + 2 * kMaxLp);        // 128 output row offsets
+  // split left row as overlapping BF16 pairs, two rows: pairs[row][hi/lo][j] = (x_j, x_j+1)
+  uint32_t* pairs = reinterpret_cast<uint32_t*>(smem + kStages * kStageBytes);    // 2 x 2 x kMaxLp
+  long long* row_base = reinterpret_cast<long long*>(pairs + 4 * kMaxLp);         // 128 output row offsets
   uint64_t* bars = reinterpret_cast<uint64_t*>(row_base + 128);
   uint64_t* a_full = bars;              // [kStages] right-row tiles landed
   uint64_t* a_empty = bars + kStages;   // [kStages] tiles consumed
@@ -301,7 +316,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int a = a_lo + ai;
         for (int kc = 0; kc < p.nkc && ok; ++kc, ++it) {
           const int s = it % kStages;
-          if (!wait_or_abort(&a_empty[s], ((it / kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
+          if (!wait_or_abort_sleep(&a_empty[s], ((it / kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
             ok = false;
             break;
           }
@@ -347,7 +362,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
         for (int kc = 0; kc < p.nkc; ++kc, ++it) {
-          const int s = it & (kStages - 1), slot = it & 1;
+          const int s = it % kStages, slot = it & 1;
           if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13) ||
               !wait_or_abort(&s_full[slot], (it >> 1) & 1, abort_flag, p.flags, 12)) {
             ok = false;
@@ -390,7 +405,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp < 2 + kBuilderWarps) {
     // ------------------------------------------------------------ Toeplitz builders
     // Lane m of TMEM quadrant q (m = 32 q + lane) is shift s0 + m; per K-step
-    // it writes 8 columns of packed hi pairs and 8 of lo pairs.
+    // it writes 8 columns of packed hi pairs and 8 of lo pairs, read from
+    // the row's overlapping pair arrays (one 32-bit load per column).
     const int bt = threadIdx.x - 64;  // 0..127
     const int qd = warp & 3;
     const int m = 32 * qd + lane;
@@ -400,18 +416,24 @@ __global__ void __launch_bounds__(kThreads, 1)
     int it = 0;
     bool ok = true;
     for (int ai = 0; ai < n_rows; ++ai) {
-      // stage the centred, zero-padded left row: lp[j] = L[a][j - (Wr-1)] - mu
-      float* lpr = lp_buf + (ai & 1) * kMaxLp;
+      // split the centred, zero-padded left row x_j = L[a][j - (Wr-1)] - mu
+      // into pairs (x_j, x_j+1) of BF16 hi parts and of BF16 lo parts
+      uint32_t* ph = pairs + (ai & 1) * (2 * kMaxLp);
+      uint32_t* pl = ph + kMaxLp;
       const float* src = lrow_base + (long long)(a_lo + ai) * p.Wl;
       for (int j = bt; j < p.lp_len; j += 32 * kBuilderWarps) {
         const int x = j - (p.Wr - 1);
-        lpr[j] = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
+        const float x0 = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
+        const float x1 = (x + 1 >= 0 && x + 1 < p.Wl) ? __ldg(src + x + 1) - mu : 0.0f;
+        const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+        ph[j] = bf16x2_bits(h);
+        pl[j] = bf16x2_bits(__floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h)));
       }
       // the builder threads leave together (they share a named barrier)
       if (bar_red_or(!ok, 1, 32 * kBuilderWarps)) break;
       for (int kc = 0; kc < p.nkc; ++kc, ++it) {
         const int slot = it & 1;
-        bool w = wait_or_abort(&s_empty[slot], ((it >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
+        bool w = wait_or_abort_sleep(&s_empty[slot], ((it >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
         w = __all_sync(0xffffffffu, w);  // tcgen05.st below must stay warp-uniform
         if (!w) {
           ok = false;
@@ -424,15 +446,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int ks = 0; ks < 4; ++ks) {
             const int j = kc * 4 + ks;
             if (!(((tt == 0 ? mask0 : mask1) >> j) & 1u)) continue;
-            const float* v = lpr + (tt == 0 ? s0_0 : s0_1) + m + 16 * j;
+            const int base = (tt == 0 ? s0_0 : s0_1) + m + 16 * j;
             uint32_t r[16];
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-              const float x0 = v[2 * e], x1 = v[2 * e + 1];
-              const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-              const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h));
-              r[e] = bf16x2_bits(h);
-              r[8 + e] = bf16x2_bits(lo);
+              r[e] = ph[base + 2 * e];
+              r[8 + e] = pl[base + 2 * e];
             }
             tmem_st16(lane_addr + (uint32_t)slot * 128 + (uint32_t)(tt * 4 + ks) * 16, r);
           }
@@ -474,7 +493,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool live = (tt == 0 ? mask0 : mask1) != 0u;
     bool ok = true;
     for (int d = 0; d < n_drains; ++d) {
-      bool w = wait_or_abort(t_full, d & 1, abort_flag, p.flags, 16);
+      bool w = wait_or_abort_sleep(t_full, d & 1, abort_flag, p.flags, 16);
       w = __all_sync(0xffffffffu, w);  // tcgen05.ld below must stay warp-uniform
       if (!w) {
         ok = false;
@@ -662,7 +681,7 @@ bool tc_plan(const Geometry& g, const PairMap& pm, TcPlan* t) {
   t->nkc = (g.Wr + 63) / 64;
   t->lp_len = 128 * t->n_tiles + 64 * t->nkc;
   t->pitch = (g.Wr + 7) / 8 * 8;
-  t->smem_bytes = 1024 + kStages * kStageBytes + 2 * kMaxLp * 4 + 128 * 8 + kBarBytes;
+  t->smem_bytes = 1024 + kStages * kStageBytes + 4 * kMaxLp * 4 + 128 * 8 + kBarBytes;
   return t->lp_len <= kMaxLp && t->smem_bytes <= 227 * 1024;
 }
 
