@@ -285,11 +285,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&a_empty[s], 1);
     }
     for (int s = 0; s < 2; ++s) {
-      mbar_init(&s_full[s], 32 * kBuilderWarps);
+      mbar_init(&s_full[s], kBuilderWarps);
       mbar_init(&s_empty[s], 1);
     }
     mbar_init(t_full, 1);
-    mbar_init(t_empty, 32 * kEpiWarps);
+    mbar_init(t_empty, kEpiWarps);
     mbar_init(mma_done, 1);
     *abort_flag = 0;
     fence_mbar_init();
@@ -458,7 +458,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tmem_wait_st();
         tc_fence_before();
-        mbar_arrive(&s_full[slot]);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&s_full[slot]);  // one arrival per warp
       }
     }
   } else {
@@ -512,7 +513,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       tc_fence_before();
-      mbar_arrive(t_empty);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(t_empty);  // one arrival per warp
     }
     const int sx = (tt == 0 ? s0_0 : s0_1) + 32 * q + lane;
     if (ok && live && sx < p.Sx) {
