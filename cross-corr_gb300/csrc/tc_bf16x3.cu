@@ -37,9 +37,10 @@
 // (L' = L - mu_L, R' = R - mu_R): the tensor cores correlate the centred data,
 // whose partial sums are small random walks, and the exact remainder
 //   out = corr(L', R') + mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area
-// (S = sum of the centred matrix over the overlap of a shift, from FP64 2D
-// prefix sums) is written first by a correction kernel, which the tensor-core
-// results are then added to.  The drains bound every accumulator's chain at
+// (S = sum of the centred matrix over the overlap of a shift, from column
+// prefix sums of the centred matrices, scanned along the row per output row)
+// is written first by a correction kernel, which the tensor-core results are
+// then added to.  The drains bound every accumulator's chain at
 // 192 MMAs.
 //
 // Warp roles (704 threads, one CTA per SM):
@@ -126,18 +127,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
-      "[%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
   uint32_t r[8];
@@ -534,69 +523,108 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Mean of every matrix (FP64 sum, FP32 result): one block per matrix.
-__global__ void mean_kernel(const float* __restrict__ left, long long left_area, int n_left,
-                            const float* __restrict__ right, long long right_area, float* __restrict__ mu) {
-  const int m = blockIdx.x;
-  const float* src = m < n_left ? left + (long long)m * left_area : right + (long long)(m - n_left) * right_area;
-  const long long area = m < n_left ? left_area : right_area;
-  double acc = 0.0;
-  for (long long i = threadIdx.x; i < area; i += blockDim.x) acc += (double)src[i];
-  __shared__ double red[32];
+// Matrix sums for the means: grid (matrix, slice); FP64 partial sums of a
+// slice, block-reduced, added into sums[m] (zeroed before the launch).
+__global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src, long long area, int slices,
+                                                  double* __restrict__ sums) {
+  __shared__ double red[8];
+  const int m = blockIdx.x / slices, sl = blockIdx.x % slices;
+  const long long per = (area + slices - 1) / slices;
+  const long long lo = sl * per, hi = min(area, lo + per);
+  const float* a = src + (long long)m * area;
+  // FP32 within a thread (at most a few dozen terms; FP64 arithmetic is slow
+  // on this GPU), FP64 across threads and blocks
+  float part = 0.0f;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) part += __ldg(a + i);
+  double acc = (double)part;
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
-  if (threadIdx.x < 32) {
-    acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (threadIdx.x == 0) mu[m] = (float)(acc / (double)area);
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int j = 0; j < 8; ++j) t += red[j];
+    atomicAdd(&sums[m], t);
   }
 }
 
-// 2D prefix sums (FP64) of the centred matrices fl32(x - mu):
-// P[y][x] = sum_{i<y, j<x}, (H+1) x (W+1) per matrix.  Pass 1: one warp per
-// row scans it (warp shuffles); pass 2: one thread per column accumulates
-// down the rows.
-__global__ void prefix_rows_kernel(const float* __restrict__ src, int n_mats, int H, int W,
-                                   const float* __restrict__ mu, double* __restrict__ P) {
-  const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;  // (matrix, y) with y in [0, H]
+__global__ void mean_kernel(const double* __restrict__ sums, int n_left, double left_area, int n_total,
+                            double right_area, float* __restrict__ mu) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < n_total) mu[m] = (float)(sums[m] / (m < n_left ? left_area : right_area));
+}
+
+// Column prefix sums of the centred matrices fl32(M - mu) (the values the
+// split sees): C[m][y][x] = sum_{i<y} fl32(M[m][i][x] - mu_m), (H+1) x W per
+// matrix, FP32.  Centred, these sums are random walks of modest size, so FP32
+// holds them to ~1e-7; the summation is blocked (8-row segments, a carry per
+// 64-row chunk), which keeps every FP32 chain short.  One block per (matrix,
+// 32-column strip); each of its 8 warps loads 8 consecutive rows of a chunk
+// (coalesced, independent loads).
+__global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ src, int H, int W,
+                                                     const float* __restrict__ mu, float* __restrict__ C) {
+  __shared__ float seg[8][32];
+  __shared__ float carry[32];
+  const int strips = (W + 31) / 32;
+  const int m = blockIdx.x / strips;
   const int lane = threadIdx.x & 31;
-  if (gw >= (long long)n_mats * (H + 1)) return;
-  const int m = (int)(gw / (H + 1));
-  const int y = (int)(gw % (H + 1));
-  double* row = P + ((long long)m * (H + 1) + y) * (W + 1);
-  if (y == 0) {
-    for (int x = lane; x <= W; x += 32) row[x] = 0.0;
-    return;
-  }
-  const float* a = src + ((long long)m * H + (y - 1)) * W;
+  const int x = (blockIdx.x % strips) * 32 + lane;
+  const int w = threadIdx.x >> 5;
+  const float* a = src + (long long)m * H * W;
+  float* c = C + (long long)m * (H + 1) * W;
   const float mv = mu[m];
-  if (lane == 0) row[0] = 0.0;
-  double carry = 0.0;
-  for (int x0 = 0; x0 < W; x0 += 32) {
-    const int x = x0 + lane;
-    double v = x < W ? (double)(a[x] - mv) : 0.0;
+  if (w == 0) {
+    carry[lane] = 0.0f;
+    if (x < W) c[x] = 0.0f;
+  }
+  for (int y0 = 0; y0 < H; y0 += 64) {
+    const int yb = y0 + 8 * w;
+    float run[8];
+    float acc = 0.0f;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const double t = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += t;
+    for (int i = 0; i < 8; ++i) {
+      const float v = (x < W && yb + i < H) ? __ldg(a + (long long)(yb + i) * W + x) - mv : 0.0f;
+      acc += v;
+      run[i] = acc;
     }
-    if (x < W) row[x + 1] = carry + v;
-    carry += __shfl_sync(0xffffffffu, v, 31);
+    seg[w][lane] = acc;
+    __syncthreads();
+    float off = carry[lane];
+    for (int j = 0; j < w; ++j) off += seg[j][lane];
+    if (x < W) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (yb + i < H) c[(long long)(yb + i + 1) * W + x] = off + run[i];
+    }
+    __syncthreads();
+    if (w == 0) {
+      float t = 0.0f;
+      for (int j = 0; j < 8; ++j) t += seg[j][lane];
+      carry[lane] += t;
+    }
+    __syncthreads();
   }
 }
 
-__global__ void prefix_cols_kernel(int n_mats, int H, int W, double* __restrict__ P) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= (long long)n_mats * (W + 1)) return;
-  const int m = (int)(t / (W + 1));
-  const int x = (int)(t % (W + 1));
-  double* q = P + (long long)m * (H + 1) * (W + 1) + x;
-  double acc = 0.0;
-  for (int y = 1; y <= H; ++y) {
-    acc += q[(long long)y * (W + 1)];
-    q[(long long)y * (W + 1)] = acc;
+// Exclusive prefix of q[1..n] in place by one warp (q[0] = 0 on entry):
+// afterwards q[x] = sum of the first x band values.  Each lane scans a
+// contiguous segment, then a shuffle scan combines the segment totals.
+__device__ __forceinline__ void warp_scan_inplace(float* q, int n, int lane) {
+  const int per = (n + 31) / 32;
+  const int lo = 1 + lane * per, hi = min(n + 1, lo + per);
+  float acc = 0.0f;
+  for (int i = lo; i < hi; ++i) {
+    acc += q[i];
+    q[i] = acc;
   }
+  float v = acc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += u;
+  }
+  const float off = v - acc;
+  for (int i = lo; i < hi; ++i) q[i] += off;
+  __syncwarp();
 }
 
 // Splits the centred right matrices fl32(R - mu_R) into BF16 hi/lo planes
@@ -617,16 +645,21 @@ __global__ void split_kernel(const float* __restrict__ src, const float* __restr
 }
 
 // out[o][sy][sx] = mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area over the
-// overlap of shift (sy, sx); one block per output row.  The row band sums
-// Q[x] = P[y1][x] - P[y0][x] of both matrices are formed once per row in
-// shared memory (FP64); per element only the two band differences are FP64
-// and the products are FP32 (their rounding is ~6e-8 of max|out|).
-__global__ void correction_kernel(float* __restrict__ out, const double* __restrict__ PL,
-                                  const double* __restrict__ PR, const float* __restrict__ mu_l,
-                                  const float* __restrict__ mu_r, int Hl, int Wl, int Hr, int Wr, int Sy, int Sx,
-                                  PairMap pm) {
-  extern __shared__ double qs[];  // (Wl + 1) + (Wr + 1)
-  const long long row = blockIdx.x;  // o * Sy + sy
+// overlap of shift (sy, sx), where S' are sums of the centred matrices; one
+// warp per output row (8 rows per block, no block-wide barrier).  The band
+// sums of the overlapping rows, b[x] = C[y1][x] - C[y0][x] (centred column
+// prefix sums), are scanned along x in the warp's shared-memory slice;
+// everything is FP32 (the centred sums are small, and the result's rounding
+// stays near 1e-7 of max|out|).
+__global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out, const float* __restrict__ CL,
+                                                         const float* __restrict__ CR,
+                                                         const float* __restrict__ mu_l,
+                                                         const float* __restrict__ mu_r, int Hl, int Wl, int Hr,
+                                                         int Wr, int Sy, int Sx, long long n_rows, PairMap pm) {
+  extern __shared__ float qs[];  // 8 x ((Wl + 1) + (Wr + 1))
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const long long row = blockIdx.x * 8LL + wid;  // o * Sy + sy
+  if (row >= n_rows) return;  // warp-uniform
   const long long o = row / Sy;
   const int sy = (int)(row % Sy);
   // invert o = l*o_l + k*o_k for the three pair-map forms
@@ -644,24 +677,30 @@ __global__ void correction_kernel(float* __restrict__ out, const double* __restr
   const long long r = l * pm.r_l + k * pm.r_k;
   const int dy = sy - (Hr - 1);
   const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
-  const double* pl0 = PL + (l * (Hl + 1) + y0) * (long long)(Wl + 1);
-  const double* pl1 = PL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
-  const double* pr0 = PR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
-  const double* pr1 = PR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
-  double* ql = qs;
-  double* qr = qs + (Wl + 1);
-  for (int x = threadIdx.x; x <= Wl; x += blockDim.x) ql[x] = pl1[x] - pl0[x];
-  for (int x = threadIdx.x; x <= Wr; x += blockDim.x) qr[x] = pr1[x] - pr0[x];
-  __syncthreads();
+  const float* cl0 = CL + (l * (Hl + 1) + y0) * (long long)Wl;
+  const float* cl1 = CL + (l * (Hl + 1) + y1) * (long long)Wl;
+  const float* cr0 = CR + (r * (Hr + 1) + (y0 - dy)) * (long long)Wr;
+  const float* cr1 = CR + (r * (Hr + 1) + (y1 - dy)) * (long long)Wr;
+  float* ql = qs + wid * (Wl + Wr + 2);
+  float* qr = ql + (Wl + 1);
+  for (int x = lane; x < Wl; x += 32) ql[x + 1] = cl1[x] - cl0[x];
+  for (int x = lane; x < Wr; x += 32) qr[x + 1] = cr1[x] - cr0[x];
+  if (lane == 0) {
+    ql[0] = 0.0f;
+    qr[0] = 0.0f;
+  }
+  __syncwarp();
+  warp_scan_inplace(ql, Wl, lane);
+  warp_scan_inplace(qr, Wr, lane);
   const float ml = mu_l[l], mr = mu_r[r];
   const float mlr = ml * mr;
   const float rows = (float)(y1 - y0);
   float* orow = out + row * Sx;
-  for (int sx = threadIdx.x; sx < Sx; sx += blockDim.x) {
+  for (int sx = lane; sx < Sx; sx += 32) {
     const int dx = sx - (Wr - 1);
     const int x0 = max(0, dx), x1 = min(Wl, Wr + dx);
-    const float sl = (float)(ql[x1] - ql[x0]);
-    const float sr = (float)(qr[x1 - dx] - qr[x0 - dx]);
+    const float sl = ql[x1] - ql[x0];
+    const float sr = qr[x1 - dx] - qr[x0 - dx];
     orow[sx] = fmaf(mr, sl, fmaf(ml, sr, mlr * (rows * (float)(x1 - x0))));
   }
 }
@@ -718,8 +757,9 @@ int chunk_rows() {
 // Workspace layout (each part 256-byte aligned).
 struct TcWs {
   float* mu;        // n_left + n_right means
-  double* PL;       // n_left x (Hl+1)(Wl+1)
-  double* PR;       // n_right x (Hr+1)(Wr+1)
+  double* sums;     // n_left + n_right matrix sums
+  float* CL;        // n_left x (Hl+1) x Wl centred column prefix sums
+  float* CR;        // n_right x (Hr+1) x Wr
   __nv_bfloat16* hi;  // n_right x Hr x pitch
   __nv_bfloat16* lo;
   size_t bytes;
@@ -739,8 +779,9 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
     return ptr;
   };
   w.mu = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
-  w.PL = reinterpret_cast<double*>(take(sizeof(double) * (size_t)pm.n_left * (g.Hl + 1) * (g.Wl + 1)));
-  w.PR = reinterpret_cast<double*>(take(sizeof(double) * (size_t)nr * (g.Hr + 1) * (g.Wr + 1)));
+  w.sums = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
+  w.CL = reinterpret_cast<float*>(take(sizeof(float) * (size_t)pm.n_left * (g.Hl + 1) * g.Wl));
+  w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * g.Wr));
   w.hi = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * plane));
   w.lo = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * plane));
   w.bytes = off + 256;
@@ -769,23 +810,24 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   const int nl = pm.n_left;
   const uint64_t n_out = (uint64_t)((long long)(nl - 1) * pm.o_l + (long long)(pm.K - 1) * pm.o_k + 1);
 
-  // 1. per-matrix means, 2. FP64 prefix sums of the centred matrices
-  mean_kernel<<<(unsigned)(nl + nr), 256, 0, stream>>>(left, (long long)g.Hl * g.Wl, nl, right,
-                                                         (long long)g.Hr * g.Wr, w.mu);
-  XC_CUDA_TRY(cudaGetLastError());
+  // 1. per-matrix means, 2. column prefix sums of the centred matrices
   {
-    auto prefix = [&](const float* src, int n, int H, int W, const float* mu, double* P) -> xc_status {
-      const long long warps = (long long)n * (H + 1);
-      prefix_rows_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, stream>>>(src, n, H, W, mu, P);
-      XC_CUDA_TRY(cudaGetLastError());
-      const long long cols = (long long)n * (W + 1);
-      prefix_cols_kernel<<<(unsigned)((cols + 255) / 256), 256, 0, stream>>>(n, H, W, P);
-      XC_CUDA_TRY(cudaGetLastError());
-      return XC_OK;
-    };
-    XC_TRY(prefix(left, nl, g.Hl, g.Wl, w.mu, w.PL));
-    XC_TRY(prefix(right, (int)nr, g.Hr, g.Wr, w.mu + nl, w.PR));
+    const long long la = (long long)g.Hl * g.Wl, ra = (long long)g.Hr * g.Wr;
+    // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
+    const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
+    XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, sizeof(double) * (nl + nr), stream));
+    sum_kernel<<<(unsigned)(nl * ls), 256, 0, stream>>>(left, la, ls, w.sums);
+    XC_CUDA_TRY(cudaGetLastError());
+    sum_kernel<<<(unsigned)(nr * rs), 256, 0, stream>>>(right, ra, rs, w.sums + nl);
+    XC_CUDA_TRY(cudaGetLastError());
+    mean_kernel<<<(unsigned)((nl + nr + 255) / 256), 256, 0, stream>>>(w.sums, nl, (double)la, (int)(nl + nr),
+                                                                        (double)ra, w.mu);
+    XC_CUDA_TRY(cudaGetLastError());
   }
+  colsum_kernel<<<(unsigned)(nl * ((g.Wl + 31) / 32)), 256, 0, stream>>>(left, g.Hl, g.Wl, w.mu, w.CL);
+  XC_CUDA_TRY(cudaGetLastError());
+  colsum_kernel<<<(unsigned)(nr * ((g.Wr + 31) / 32)), 256, 0, stream>>>(right, g.Hr, g.Wr, w.mu + nl, w.CR);
+  XC_CUDA_TRY(cudaGetLastError());
   // 3. split of the centred right matrices
   {
     const long long rows = nr * g.Hr;
@@ -795,8 +837,13 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
     XC_CUDA_TRY(cudaGetLastError());
   }
   // 4. the mean terms initialise the output
-  correction_kernel<<<(unsigned)(n_out * g.Sy), 256, sizeof(double) * (g.Wl + g.Wr + 2), stream>>>(
-      out, w.PL, w.PR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, pm);
+  {
+    const long long n_rows = (long long)n_out * g.Sy;
+    const size_t smem = sizeof(float) * 8 * (g.Wl + g.Wr + 2);
+    XC_CUDA_TRY(cudaFuncSetAttribute(correction_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    correction_kernel<<<(unsigned)((n_rows + 7) / 8), 256, smem, stream>>>(
+        out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, n_rows, pm);
+  }
   XC_CUDA_TRY(cudaGetLastError());
 
   CUtensorMap mhi, mlo;
