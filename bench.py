@@ -250,6 +250,22 @@ def run_ours(args, rank, world, local_rank):
         plain = {"value": pairs / (ms_p / 1000.0), "ms_per_step": ms_p, "max_rel_err_vs_fp64": gate_p,
                  "method": "direct (plain FP32 FMA kernel)", "speedup_of_headline": ms_p / ms}
         del out_p
+    # ---- the split-TF32 arm on the same inputs (more accurate, half the tensor rate)
+    tf32 = None
+    if method == "tc_bf16x3":
+        out_t = torch.empty_like(out)
+        wb_t = xcorr.workspace_size("one_to_many", "f32", "tc_tf32x3", (256, 256), 1, (256, 256), pairs)
+        ws_t = torch.empty(max(wb_t, 1), dtype=torch.uint8, device="cuda")
+        step_t = make_step("tc_tf32x3", out_t, ws_t, wb_t)
+        for _ in range(args.warmup):
+            step_t()
+        torch.cuda.synchronize()
+        gate_t, _, _ = accuracy_gate(out_t, left, right, torch, xcorr)
+        ts_t = timed(step_t, args.steps)
+        ms_t = sum(ts_t) / len(ts_t)
+        tf32 = {"value": pairs / (ms_t / 1000.0), "ms_per_step": ms_t, "max_rel_err_vs_fp64": gate_t,
+                "method": "tc_tf32x3 (split-TF32 tensor cores)"}
+        del out_t, ws_t
     ms_max = ms
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -291,12 +307,16 @@ def run_ours(args, rank, world, local_rank):
     if method == "tc_bf16x3":
         bound, peak, unit = "tensor", float(peaks.get("bf16_tflops", 1900.0)), "TFLOP/s"
         peak_note = f"{peak_src} cuBLAS bf16 burst; algorithmic FP32 flops (3 bf16 products each)"
+    elif method == "tc_tf32x3":
+        bound, peak, unit = "tensor", float(peaks.get("bf16_tflops", 1900.0)) / 2, "TFLOP/s"
+        peak_note = (f"half the {peak_src} cuBLAS bf16 burst (a TF32 MMA does half the K of a BF16 one in the "
+                     "same time); algorithmic FP32 flops (3 tf32 products each)")
     else:
         mhz = float(peaks.get("sm_max_mhz", 2070.0))
         bound, peak, unit = "fp32", 152 * 128 * 2 * mhz * 1e6 / 1e12, "TFLOP/s"
         peak_note = "nominal FP32 FMA peak (152 SMs x 128 lanes x 2 x max SM clock); no measured SIMT peak exists"
     clocks = clk.summary()
-    kernel_name = "direct_kernel" if method != "tc_bf16x3" else "tc_kernel"
+    kernel_name = "tc_kernel" if method.startswith("tc_") else "direct_kernel"
     line = {
         "metric": METRIC, "value": value, "unit": "correlations/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
@@ -322,6 +342,8 @@ def run_ours(args, rank, world, local_rank):
     }
     if plain is not None:
         line["plain_fp32"] = plain
+    if tf32 is not None:
+        line["tf32x3"] = tf32
     if rank == 0 and not args.no_ragged:
         line["ragged_n_to_m"] = ragged_study(torch, xcorr)
     if rank == 0 and not args.no_configs:
@@ -421,8 +443,8 @@ def config_studies(torch, xcorr, reps=20):
             ref = oracle.run_mode(mode, la, rb, dtype="f64" if dtype == "f64" else "f32acc64", threads=threads)
             dl, dr = torch.from_numpy(la).cuda(), torch.from_numpy(rb).cuda()
             row = {"config": name, "dtype": dtype, "outputs": int(ref.shape[0])}
-            for method in ("direct", "fft", "tc_bf16x3"):
-                if method == "tc_bf16x3" and dtype == "f64":
+            for method in ("direct", "fft", "tc_bf16x3", "tc_tf32x3"):
+                if method.startswith("tc_") and dtype == "f64":
                     continue
                 ws_bytes = xcorr.workspace_size(mode, dtype, method, la.shape[1:], la.shape[0], rb.shape[1:],
                                                 rb.shape[0])
@@ -446,8 +468,9 @@ def config_studies(torch, xcorr, reps=20):
 
 def gpu_launches(method, steps):
     # kernels per xc_correlate call: direct 1; fft 2 pads + multiply + normalise
-    # (+ cuFFT's own); tc: mean, 2 prefix, split, correction, tcgen05 kernel
-    per_step = {"direct": 1, "fft": 4, "tc_bf16x3": 6}.get(method, 1)
+    # (+ cuFFT's own); tc: 2 sums, mean, 2 column sums, split, correction,
+    # tcgen05 kernel
+    per_step = {"direct": 1, "fft": 4, "tc_bf16x3": 8, "tc_tf32x3": 8}.get(method, 1)
     return per_step * steps
 
 
@@ -457,7 +480,7 @@ def main():
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--method", default="tc_bf16x3", choices=["direct", "fft", "tc_bf16x3"])
+    ap.add_argument("--method", default="tc_bf16x3", choices=["direct", "fft", "tc_bf16x3", "tc_tf32x3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged n_to_m side study")
     ap.add_argument("--no-configs", action="store_true", help="skip the other fixed configurations")

@@ -8,6 +8,7 @@
 //   nai_*                -> XC_METHOD_DIRECT (plain FP32/FP64 kernel)
 //   fft_*                -> XC_METHOD_FFT (cuFFT + fused glue)
 //   tc_bf16x3_*          -> XC_METHOD_TC_BF16X3 (new: split-BF16 tensor cores)
+//   tc_tf32x3_*          -> XC_METHOD_TC_TF32X3 (new: split-TF32 tensor cores)
 // The reference's tile arguments are validated with its limits and reported
 // in the measurement CSV, but the GB300 kernels choose their own tiling.
 //
@@ -32,7 +33,7 @@ namespace cross {
 
 namespace {
 
-enum class kind { cpu, direct, fft_orig, fft_reduced, fft_better, tc };
+enum class kind { cpu, direct, fft_orig, fft_reduced, fft_better, tc, tc32 };
 
 struct arg_def {
   std::string key;
@@ -146,6 +147,10 @@ const std::vector<alg_spec>& registry() {
         {"tc_bf16x3_one_to_many", {kind::tc, none}},
         {"tc_bf16x3_n_to_mn", {kind::tc, none}},
         {"tc_bf16x3_n_to_m", {kind::tc, none}},
+        {"tc_tf32x3_one_to_one", {kind::tc32, none}},
+        {"tc_tf32x3_one_to_many", {kind::tc32, none}},
+        {"tc_tf32x3_n_to_mn", {kind::tc32, none}},
+        {"tc_tf32x3_n_to_m", {kind::tc32, none}},
     };
     std::vector<alg_spec> out;
     for (auto& e : list) out.push_back(alg_spec{e.first, mode_of(e.first), e.second.first, e.second.second});
@@ -321,7 +326,8 @@ class instance {
       return;
     }
     const xc_dtype dt = sizeof(T) == 4 ? XC_F32 : XC_F64;
-    if (spec_.k == kind::tc && dt != XC_F32) throw std::runtime_error("tc_bf16x3_* algorithms take -d single data");
+    if ((spec_.k == kind::tc || spec_.k == kind::tc32) && dt != XC_F32)
+      throw std::runtime_error("tc_bf16x3_* and tc_tf32x3_* algorithms take -d single data");
     auto alloc = [&]() {
       cuda_check(cudaMalloc(&d_left_, left_.size() * sizeof(T)), "cudaMalloc");
       cuda_check(cudaMalloc(&d_right_, right_.size() * sizeof(T)), "cudaMalloc");
@@ -447,6 +453,7 @@ class instance {
   xc_method method() const {
     switch (spec_.k) {
       case kind::tc: return XC_METHOD_TC_BF16X3;
+      case kind::tc32: return XC_METHOD_TC_TF32X3;
       case kind::direct: return XC_METHOD_DIRECT;
       default: return XC_METHOD_FFT;
     }

@@ -18,8 +18,8 @@
 namespace xc {
 const char* last_error_cstr();
 xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream);
-size_t tc_workspace_size(const Geometry& g, const PairMap& pm);
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32);
+size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32);
 }  // namespace xc
 
 using namespace xc;
@@ -140,7 +140,8 @@ using SelKey = std::tuple<int, int, uint32_t, uint32_t, uint32_t, uint32_t, uint
 std::map<SelKey, xc_method> g_tuned;
 
 bool method_supported(xc_method m, xc_dtype dtype, xc_size2 left, xc_size2 right) {
-  if (m == XC_METHOD_TC_BF16X3) return dtype == XC_F32 && left.x + right.x - 1 <= 512 && right.x <= 256;
+  if (m == XC_METHOD_TC_BF16X3 || m == XC_METHOD_TC_TF32X3)
+    return dtype == XC_F32 && left.x + right.x - 1 <= 512 && right.x <= 256;
   return m == XC_METHOD_DIRECT || m == XC_METHOD_FFT;
 }
 
@@ -276,8 +277,9 @@ xc_status xc_workspace_size(xc_mode mode, xc_dtype dtype, xc_method method, xc_s
     case XC_METHOD_DIRECT: *bytes = 0; return XC_OK;
     case XC_METHOD_FFT: *bytes = fft_workspace_bytes(mode, dtype, left, n_left, right, n_right); return XC_OK;
     case XC_METHOD_TC_BF16X3:
-      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split-BF16 tensor path is FP32 only");
-      *bytes = tc_workspace_size(make_geometry(left, right), pm);
+    case XC_METHOD_TC_TF32X3:
+      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split tensor-core paths are FP32 only");
+      *bytes = tc_workspace_size(make_geometry(left, right), pm, method == XC_METHOD_TC_TF32X3);
       return XC_OK;
     default: return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
   }
@@ -304,9 +306,10 @@ xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const voi
       return fft_plan_execute(plan, d_left, d_right, d_out, 1, d_workspace, workspace_bytes, as_stream(stream));
     }
     case XC_METHOD_TC_BF16X3:
-      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split-BF16 tensor path is FP32 only");
+    case XC_METHOD_TC_TF32X3:
+      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split tensor-core paths are FP32 only");
       return tc_correlate((const float*)d_left, (const float*)d_right, (float*)d_out, g, pm, d_workspace,
-                          workspace_bytes, as_stream(stream));
+                          workspace_bytes, as_stream(stream), method == XC_METHOD_TC_TF32X3);
     default: return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
   }
 }

@@ -1,4 +1,8 @@
-// tc_bf16x3.cu -- split-BF16 tensor-core correlation on tcgen05 (sm_103a).
+// tc_bf16x3.cu -- split-BF16 (and split-TF32) tensor-core correlation on
+// tcgen05 (sm_103a).  The TF32x3 variant runs the same kernel with FP32
+// operands rounded to TF32 (hi = tf32(x), lo = tf32(x - hi)), K = 8 per MMA
+// (kind::tf32); it keeps ~21 bits per operand instead of ~16 at half the
+// tensor rate.
 //
 // FP32 inputs, FP32 outputs, three BF16 products per FP32 product:
 //   x = x_hi + x_lo, x_hi = bf16(x), x_lo = bf16(x - x_hi)
@@ -85,7 +89,8 @@ struct TcParams {
   int n_pgroups;    // ceil(K / P)
   int n_dytiles;    // ceil(Sy / DY)
   int n_halves;     // CTAs per work item (two 128-shift tiles each)
-  int nkc;          // 64-column chunks of a right row
+  int nkc;          // 128-byte column chunks of a right row (64 BF16 or 32 TF32 columns)
+  int kstep;        // columns per K-step: 16 (BF16) or 8 (TF32)
   int lp_len;       // staged left row length
   int flush_rows;   // drain TMEM every this many left rows
   int chunk_rows;   // left rows per CTA (a longer row range is split over CTAs)
@@ -103,6 +108,30 @@ struct TcParams {
 // 10-12 = 1), both K-major, N>>3 at bit 17, M>>4 at bit 24.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Instruction descriptor, kind::tf32: D=F32, A=B=TF32 (format 2), both
+// K-major, N>>3 at bit 17, M>>4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_tf32_f32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// D[tmem] (+)= A[tmem] * B[smem]^T, TF32 operands (K = 8 per instruction).
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Round to TF32 (10 explicit mantissa bits), nearest with ties away.
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
 }
 
 // D[tmem] (+)= A[tmem] * B[smem]^T.
@@ -195,13 +224,14 @@ __device__ __forceinline__ int centre_out(int r, int n, int tc) {
 }
 
 // Active K-steps of a 128-shift tile starting at s0: bit j is set when
-// A's K-step j (columns 16j..16j+15 of the right row) meets a left column.
+// A's K-step j (right columns kstep*j .. kstep*j + kstep - 1) meets a left
+// column.
 __device__ __forceinline__ uint32_t tile_mask(int s0, const TcParams& p) {
   uint32_t m = 0;
   if (s0 >= p.Sx) return 0;
   for (int j = 0; j < 4 * p.nkc; ++j) {
-    const int k0 = 16 * j;
-    if (k0 < p.Wr && s0 + k0 + 142 >= p.Wr - 1 && s0 + k0 <= p.Wr + p.Wl - 2) m |= 1u << j;
+    const int k0 = p.kstep * j;
+    if (k0 < p.Wr && s0 + k0 + 127 + p.kstep - 1 >= p.Wr - 1 && s0 + k0 <= p.Wr + p.Wl - 2) m |= 1u << j;
   }
   return m;
 }
@@ -220,7 +250,8 @@ __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
 
 // 22 warps: at most 6 on one SM sub-partition, whose 16K registers cap a
-// thread at 80.
+// thread at 80.  TF: TF32 operands (K = 8 per MMA) instead of BF16 (K = 16).
+template <bool TF>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
               const TcParams p) {
@@ -336,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
       constexpr uint32_t kDescHi = (1024u >> 4) | (1u << 14) | (2u << 29);  // SBO 1024 B, 128-byte swizzle
-      const uint32_t idesc = idesc_bf16_f32(128, 128);
+      const uint32_t idesc = TF ? idesc_tf32_f32(128, 128) : idesc_bf16_f32(128, 128);
       const uint32_t b_lo_word = ((smem_u32(b_tiles) >> 4) & 0x3FFFu) | (1u << 16);
       const int first0 = mask0 ? __ffs(mask0) - 1 : -1;
       const int first1 = mask1 ? __ffs(mask1) - 1 : -1;
@@ -371,9 +402,15 @@ __global__ void __launch_bounds__(kThreads, 1)
               const bool reset = rows_in == 0 && j == (tt == 0 ? first0 : first1);
               const uint32_t ahi = ring + (uint32_t)(tt * 4 + ks) * 16, alo = ahi + 8;
               const uint32_t d = tmem_base + (uint32_t)tt * 128;
-              mma_bf16_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
-              mma_bf16_ts(d, ahi, blo, idesc, 1u);
-              mma_bf16_ts(d, alo, bhi, idesc, 1u);
+              if constexpr (TF) {
+                mma_tf32_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
+                mma_tf32_ts(d, ahi, blo, idesc, 1u);
+                mma_tf32_ts(d, alo, bhi, idesc, 1u);
+              } else {
+                mma_bf16_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
+                mma_bf16_ts(d, ahi, blo, idesc, 1u);
+                mma_bf16_ts(d, alo, bhi, idesc, 1u);
+              }
             }
           }
           mma_commit(&a_empty[s]);
@@ -413,10 +450,17 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int j = bt; j < p.lp_len; j += 32 * kBuilderWarps) {
         const int x = j - (p.Wr - 1);
         const float x0 = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
-        const float x1 = (x + 1 >= 0 && x + 1 < p.Wl) ? __ldg(src + x + 1) - mu : 0.0f;
-        const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-        ph[j] = bf16x2_bits(h);
-        pl[j] = bf16x2_bits(__floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h)));
+        if constexpr (TF) {
+          // TF32: one element per column, hi and lo parts
+          const float h = tf32_round(x0);
+          ph[j] = __float_as_uint(h);
+          pl[j] = __float_as_uint(tf32_round(x0 - h));
+        } else {
+          const float x1 = (x + 1 >= 0 && x + 1 < p.Wl) ? __ldg(src + x + 1) - mu : 0.0f;
+          const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+          ph[j] = bf16x2_bits(h);
+          pl[j] = bf16x2_bits(__floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h)));
+        }
       }
       // the builder threads leave together (they share a named barrier)
       if (bar_red_or(!ok, 1, 32 * kBuilderWarps)) break;
@@ -435,12 +479,12 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int ks = 0; ks < 4; ++ks) {
             const int j = kc * 4 + ks;
             if (!(((tt == 0 ? mask0 : mask1) >> j) & 1u)) continue;
-            const int base = (tt == 0 ? s0_0 : s0_1) + m + 16 * j;
+            const int base = (tt == 0 ? s0_0 : s0_1) + m + p.kstep * j;
             uint32_t r[16];
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-              r[e] = ph[base + 2 * e];
-              r[8 + e] = pl[base + 2 * e];
+              r[e] = ph[base + (TF ? 1 : 2) * e];
+              r[8 + e] = pl[base + (TF ? 1 : 2) * e];
             }
             tmem_st16(lane_addr + (uint32_t)slot * 128 + (uint32_t)(tt * 4 + ks) * 16, r);
           }
@@ -627,20 +671,26 @@ __device__ __forceinline__ void warp_scan_inplace(float* q, int n, int lane) {
   __syncwarp();
 }
 
-// Splits the centred right matrices fl32(R - mu_R) into BF16 hi/lo planes
-// with a padded pitch.
-__global__ void split_kernel(const float* __restrict__ src, const float* __restrict__ mu,
-                             __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo, long long rows,
-                             int rows_per_matrix, int cols, int pitch) {
+// Splits the centred right matrices fl32(R - mu_R) into hi/lo planes with a
+// padded pitch: BF16 (T = __nv_bfloat16) or TF32-rounded FP32 (T = float).
+template <typename T>
+__global__ void split_kernel(const float* __restrict__ src, const float* __restrict__ mu, T* __restrict__ hi,
+                             T* __restrict__ lo, long long rows, int rows_per_matrix, int cols, int pitch) {
   const long long total = rows * pitch;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const long long r = i / pitch;
     const int c = (int)(i % pitch);
     const float v = c < cols ? src[r * cols + c] - mu[r / rows_per_matrix] : 0.0f;
-    const __nv_bfloat16 h = __float2bfloat16_rn(v);
-    hi[i] = h;
-    lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    if constexpr (sizeof(T) == 4) {
+      const float h = tf32_round(v);
+      hi[i] = h;
+      lo[i] = tf32_round(v - h);
+    } else {
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      hi[i] = h;
+      lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+    }
   }
 }
 
@@ -706,11 +756,11 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, n_tiles, n_halves, nkc, lp_len, pitch;
+  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, lp_len, pitch;
   int smem_bytes;
 };
 
-bool tc_plan(const Geometry& g, const PairMap& pm, TcPlan* t) {
+bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   if (g.Sx > 512 || g.Wr > 256) return false;  // four 128-shift tiles, 16 K-steps
   int P = 1;
   while (P < 128 && P < pm.K) P *= 2;
@@ -719,9 +769,12 @@ bool tc_plan(const Geometry& g, const PairMap& pm, TcPlan* t) {
   t->mats_mode = P >= 8 ? 1 : 0;
   t->n_tiles = (g.Sx + 127) / 128;
   t->n_halves = (t->n_tiles + 1) / 2;
-  t->nkc = (g.Wr + 63) / 64;
-  t->lp_len = 128 * t->n_tiles + 64 * t->nkc;
-  t->pitch = (g.Wr + 7) / 8 * 8;
+  t->es = tf32 ? 4 : 2;                 // bytes per operand element
+  t->kstep = tf32 ? 8 : 16;             // columns per MMA K-step (32 bytes)
+  const int chunk = 128 / t->es;        // columns per 128-byte TMA box row
+  t->nkc = (g.Wr + chunk - 1) / chunk;
+  t->lp_len = 128 * t->n_tiles + 4 * t->kstep * t->nkc;
+  t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
   t->smem_bytes = 1024 + kStages * kStageBytes + 4 * kMaxLp * 4 + 128 * 8 + kBarBytes;
   return t->lp_len <= kMaxLp && t->smem_bytes <= 227 * 1024;
 }
@@ -760,8 +813,8 @@ struct TcWs {
   double* sums;     // n_left + n_right matrix sums
   float* CL;        // n_left x (Hl+1) x Wl centred column prefix sums
   float* CR;        // n_right x (Hr+1) x Wr
-  __nv_bfloat16* hi;  // n_right x Hr x pitch
-  __nv_bfloat16* lo;
+  void* hi;         // n_right x Hr x pitch, BF16 or TF32-rounded FP32
+  void* lo;
   size_t bytes;
 };
 
@@ -782,29 +835,29 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   w.sums = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
   w.CL = reinterpret_cast<float*>(take(sizeof(float) * (size_t)pm.n_left * (g.Hl + 1) * g.Wl));
   w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * g.Wr));
-  w.hi = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * plane));
-  w.lo = reinterpret_cast<__nv_bfloat16*>(take(sizeof(__nv_bfloat16) * plane));
+  w.hi = take((size_t)t.es * plane);
+  w.lo = take((size_t)t.es * plane);
   w.bytes = off + 256;
   return w;
 }
 
 }  // namespace
 
-size_t tc_workspace_size(const Geometry& g, const PairMap& pm) {
+size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32) {
   TcPlan t;
-  if (!tc_plan(g, pm, &t)) return 0;
+  if (!tc_plan(g, pm, tf32, &t)) return 0;
   return ws_layout(nullptr, g, pm, t).bytes;
 }
 
 xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream) {
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32) {
   TcPlan t;
-  if (!tc_plan(g, pm, &t))
+  if (!tc_plan(g, pm, tf32, &t))
     return fail(XC_ERR_UNSUPPORTED,
-                "split-BF16 tensor path supports outputs up to 512 columns and right widths up to 256");
+                "split tensor-core paths support outputs up to 512 columns and right widths up to 256");
   const size_t need = ws_layout(nullptr, g, pm, t).bytes;
   if (workspace == nullptr || ws_bytes < need)
-    return fail(XC_ERR_WORKSPACE, "split-BF16 path needs " + std::to_string(need) + " bytes of workspace");
+    return fail(XC_ERR_WORKSPACE, "split tensor-core path needs " + std::to_string(need) + " bytes of workspace");
   const TcWs w = ws_layout(reinterpret_cast<void*>(((uintptr_t)workspace + 255) & ~uintptr_t(255)), g, pm, t);
   const long long nr = n_right_of(pm);
   const int nl = pm.n_left;
@@ -833,7 +886,12 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
     const long long rows = nr * g.Hr;
     long long blocks = (rows * t.pitch + 255) / 256;
     if (blocks > 152 * 32) blocks = 152 * 32;
-    split_kernel<<<(unsigned)blocks, 256, 0, stream>>>(right, w.mu + nl, w.hi, w.lo, rows, g.Hr, g.Wr, t.pitch);
+    if (tf32)
+      split_kernel<float><<<(unsigned)blocks, 256, 0, stream>>>(right, w.mu + nl, (float*)w.hi, (float*)w.lo, rows,
+                                                                 g.Hr, g.Wr, t.pitch);
+    else
+      split_kernel<__nv_bfloat16><<<(unsigned)blocks, 256, 0, stream>>>(
+          right, w.mu + nl, (__nv_bfloat16*)w.hi, (__nv_bfloat16*)w.lo, rows, g.Hr, g.Wr, t.pitch);
     XC_CUDA_TRY(cudaGetLastError());
   }
   // 4. the mean terms initialise the output
@@ -848,19 +906,21 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
 
   CUtensorMap mhi, mlo;
   {
-    const uint64_t es = 2, mat = (uint64_t)t.pitch * g.Hr * es;
+    const uint64_t es = (uint64_t)t.es, mat = (uint64_t)t.pitch * g.Hr * es;
+    const uint32_t box_x = 128u / (uint32_t)t.es;  // one 128-byte swizzle row
     const uint64_t d2 = pm.r_l != 0 ? (uint64_t)pm.n_left : 1;
     uint64_t dims[4] = {(uint64_t)t.pitch, (uint64_t)g.Hr, d2, (uint64_t)pm.K};
     uint64_t strides[3] = {(uint64_t)t.pitch * es, mat * (uint64_t)(pm.r_l != 0 ? pm.r_l : 1), mat * (uint64_t)pm.r_k};
     uint32_t box[4];
     if (t.mats_mode) {
-      box[0] = 64; box[1] = 1; box[2] = 1; box[3] = (uint32_t)t.P;
+      box[0] = box_x; box[1] = 1; box[2] = 1; box[3] = (uint32_t)t.P;
     } else {
-      box[0] = 64; box[1] = (uint32_t)t.DY; box[2] = 1; box[3] = 1;
+      box[0] = box_x; box[1] = (uint32_t)t.DY; box[2] = 1; box[3] = 1;
     }
-    if (!encode_tiled(&mhi, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, w.hi, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
+    const CUtensorMapDataType dt = tf32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    if (!encode_tiled(&mhi, dt, 4, w.hi, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
       return XC_ERR_INVALID_ARGUMENT;
-    if (!encode_tiled(&mlo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, w.lo, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
+    if (!encode_tiled(&mlo, dt, 4, w.lo, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B))
       return XC_ERR_INVALID_ARGUMENT;
   }
 
@@ -883,6 +943,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.n_halves = t.n_halves;
   prm.nkc = t.nkc;
   prm.lp_len = t.lp_len;
+  prm.kstep = t.kstep;
   prm.flush_rows = flush_rows(t.nkc);
   prm.chunk_rows = chunk_rows();
   prm.n_chunks = div_up(t.DY - 1 + std::min(g.Hl, g.Hr), prm.chunk_rows);
@@ -891,9 +952,10 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   const long long blocks =
       (long long)t.n_halves * prm.n_chunks * prm.n_dytiles * pm.n_left * prm.n_pgroups;
   if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
-  XC_CUDA_TRY(cudaFuncSetAttribute(tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
+  auto kern = tf32 ? tc_kernel<true> : tc_kernel<false>;
+  XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
   const int slot = kernel_timer_begin(stream);
-  tc_kernel<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
+  kern<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
   kernel_timer_end(slot, stream);
   XC_CUDA_TRY(cudaGetLastError());
   return XC_OK;
@@ -906,7 +968,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
 // device-memory budget or their own pool (and forbid raw allocations), and
 // latency-critical loops where cudaMalloc/cudaFree may stall or synchronise
 // the device.  xc_correlate_tc_noalloc serves them with the scratch of this
-// path (means, FP64 prefix sums, BF16 planes) in the file-scope array below,
+// path (sums, means, column prefix sums, BF16 planes) in the file-scope array below,
 // of fixed size XC_TC_NOALLOC_SCRATCH_BYTES.  Every GPU that loads the library
 // holds that array until the process exits.
 // ---------------------------------------------------------------------------
@@ -949,7 +1011,7 @@ extern "C" xc_status xc_correlate_tc_noalloc(xc_mode mode, const float* d_left, 
     return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts for the mode");
   const Geometry g = make_geometry(left, right);
   TcPlan t;
-  if (!tc_plan(g, pm, &t))
+  if (!tc_plan(g, pm, false, &t))
     return fail(XC_ERR_UNSUPPORTED,
                 "split-BF16 tensor path supports outputs up to 512 columns and right widths up to 256");
   const size_t need = ws_layout(nullptr, g, pm, t).bytes;
@@ -961,5 +1023,5 @@ extern "C" xc_status xc_correlate_tc_noalloc(xc_mode mode, const float* d_left, 
   void* scratch = nullptr;
   XC_TRY(noalloc_scratch(&scratch));
   return tc_correlate(d_left, d_right, d_out, g, pm, scratch, (size_t)XC_TC_NOALLOC_SCRATCH_BYTES,
-                      reinterpret_cast<cudaStream_t>(stream));
+                      reinterpret_cast<cudaStream_t>(stream), false);
 }

@@ -25,7 +25,7 @@ CLI_PATH = os.path.join(PKG, "_build", "cross")
 
 MODES = {"one_to_one": 0, "one_to_many": 1, "n_to_mn": 2, "n_to_m": 3}
 DTYPES = {"f32": 0, "f64": 1}
-METHODS = {"auto": 0, "direct": 1, "fft": 2, "tc_bf16x3": 3}
+METHODS = {"auto": 0, "direct": 1, "fft": 2, "tc_bf16x3": 3, "tc_tf32x3": 4}
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "cuFFT error", 4: "unsupported",
           5: "workspace too small", 6: "device wait timed out"}
 

@@ -57,7 +57,8 @@ typedef enum xc_method {
   XC_METHOD_AUTO = 0,     /* library choice */
   XC_METHOD_DIRECT = 1,   /* plain definition-based kernel (FP32 or FP64 FMA, TMA-staged) */
   XC_METHOD_FFT = 2,      /* cuFFT transforms + fused pad / conj-multiply / normalise kernels */
-  XC_METHOD_TC_BF16X3 = 3 /* split-BF16 (3 products) tcgen05 tensor-core implicit GEMM, FP32 only */
+  XC_METHOD_TC_BF16X3 = 3, /* split-BF16 (3 products) tcgen05 tensor-core implicit GEMM, FP32 only */
+  XC_METHOD_TC_TF32X3 = 4  /* the same with split-TF32 operands (kind::tf32): more accurate, half the rate */
 } xc_method;
 
 typedef struct xc_size2 {

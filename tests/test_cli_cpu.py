@@ -55,6 +55,7 @@ def test_list_has_every_reference_algorithm():
     assert names == sorted(names)
     assert set(REFERENCE_ALGS) <= set(names)
     assert {"tc_bf16x3_one_to_one", "tc_bf16x3_one_to_many", "tc_bf16x3_n_to_mn", "tc_bf16x3_n_to_m"} <= set(names)
+    assert {"tc_tf32x3_one_to_one", "tc_tf32x3_one_to_many", "tc_tf32x3_n_to_mn", "tc_tf32x3_n_to_m"} <= set(names)
 
 
 @pytest.mark.parametrize("name", ["valid_one_to_one_10_10_1_1_1_2.csv.gz", "valid_one_to_many_64_64_1_2_1_1.csv.gz",

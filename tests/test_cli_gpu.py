@@ -31,6 +31,7 @@ CASES = [
     ("tc_bf16x3_one_to_one", "valid_one_to_one_64_64_1_1_1_2.csv.gz"),
     ("tc_bf16x3_n_to_mn", "valid_n_to_mn_128_128_2_4_1_1.csv.gz"),
     ("tc_bf16x3_n_to_m", "valid_n_to_m_64_64_4_4_1_2.csv.gz"),
+    ("tc_tf32x3_n_to_mn", "valid_n_to_mn_128_128_2_4_1_1.csv.gz"),
 ]
 
 

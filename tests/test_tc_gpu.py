@@ -1,4 +1,4 @@
-"""Split-BF16 tensor-core path (tcgen05) against the oracle.
+"""Split-BF16 and split-TF32 tensor-core paths (tcgen05) against the oracle.
 
 Tolerance: max|out - oracle64| / max|oracle64| <= 1e-5 per output matrix,
 the accuracy gate of the headline metric.
@@ -19,8 +19,11 @@ def dev(a):
     return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float32)).cuda()
 
 
-def run_tc(mode, left, right):
-    out = xcorr.correlate(mode, dev(left), dev(right), method="tc_bf16x3")
+TC_METHODS = ["tc_bf16x3", "tc_tf32x3"]
+
+
+def run_tc(mode, left, right, method="tc_bf16x3"):
+    out = xcorr.correlate(mode, dev(left), dev(right), method=method)
     torch.cuda.synchronize()
     xcorr.check(xcorr.lib().xc_device_check(0))
     return out.cpu().numpy()
@@ -44,34 +47,49 @@ TC_SHAPES = [
 ]
 
 
+@pytest.mark.parametrize("method", TC_METHODS)
 @pytest.mark.parametrize("shape", TC_SHAPES, ids=[f"{s[0]}-{s[1]}x{s[2]}-{s[3]}-{s[4]}" for s in TC_SHAPES])
-def test_tc_matches_oracle(shape):
+def test_tc_matches_oracle(shape, method):
     mode, n, m, ls, rs, dist = shape
     left = seeded((n,) + ls, 300 + n, dist)
     right = seeded((m,) + rs, 400 + m, dist)
     ref = oracle.run_mode(mode, left, right, dtype="f32acc64", threads=8)
-    out = run_tc(mode, left, right)
+    out = run_tc(mode, left, right, method)
     assert out.shape == ref.shape
     assert rel_to_max(out, ref) <= 1e-5
 
 
+@pytest.mark.parametrize("method", TC_METHODS)
 @pytest.mark.parametrize("name", [v for v in VALID if "_10_10_" in v or "_64_64_" in v])
-def test_tc_golden(name):
+def test_tc_golden(name, method):
     mode, left, right, valid = golden_case(name)
-    out = run_tc(mode, left.astype(np.float32), right.astype(np.float32))
+    out = run_tc(mode, left.astype(np.float32), right.astype(np.float32), method)
     assert rel_to_max(out, valid) <= 1e-5
 
 
-def test_tc_bench_shape_accuracy():
+@pytest.mark.parametrize("method", TC_METHODS)
+def test_tc_bench_shape_accuracy(method):
     """The benchmark's shape (256x256, 64 right matrices) on 8 of them."""
     left = seeded((1, 256, 256), 2)
     right = seeded((8, 256, 256), 3)
     ref = oracle.run_mode("one_to_many", left, right, dtype="f32acc64", threads=16)
-    out = run_tc("one_to_many", left, right)
+    out = run_tc("one_to_many", left, right, method)
     assert rel_to_max(out, ref) <= 1e-5
 
 
-def test_tc_rejects_unsupported_sizes():
+@pytest.mark.parametrize("method", TC_METHODS)
+def test_tc_rejects_unsupported_sizes(method):
     with pytest.raises(xcorr.XcError) as e:
-        xcorr.correlate("one_to_one", dev(seeded((1, 8, 300), 1)), dev(seeded((1, 8, 300), 2)), method="tc_bf16x3")
+        xcorr.correlate("one_to_one", dev(seeded((1, 8, 300), 1)), dev(seeded((1, 8, 300), 2)), method=method)
     assert e.value.status == 4
+
+
+def test_tf32_more_accurate_than_bf16_on_zero_mean_data():
+    """TF32 operands keep ~21 bits against BF16's ~16: on zero-mean data,
+    where the mean shift does not help, the TF32x3 error is the smaller."""
+    left = seeded((1, 96, 96), 7, "normal")
+    right = seeded((4, 96, 96), 8, "normal")
+    ref = oracle.run_mode("one_to_many", left, right, dtype="f32acc64", threads=16)
+    e_bf = rel_to_max(run_tc("one_to_many", left, right, "tc_bf16x3"), ref)
+    e_tf = rel_to_max(run_tc("one_to_many", left, right, "tc_tf32x3"), ref)
+    assert e_tf <= 1e-5 and e_tf < e_bf
