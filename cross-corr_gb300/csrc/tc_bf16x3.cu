@@ -346,14 +346,14 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (p.mats_mode) {
             for (int d = 0; d < p.DY; ++d) {
               const int b = a - (dy0 + d);
-              tma_load_4d(hi + d * p.P * 128, &map_hi, &a_full[s], kc * 64, b, rdim2, p0);
-              tma_load_4d(lo + d * p.P * 128, &map_lo, &a_full[s], kc * 64, b, rdim2, p0);
+              tma_load_4d(hi + d * p.P * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b, rdim2, p0);
+              tma_load_4d(lo + d * p.P * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b, rdim2, p0);
             }
           } else {
             const int b0 = a - dy0 - (p.DY - 1);
             for (int q = 0; q < p.P; ++q) {
-              tma_load_4d(hi + q * p.DY * 128, &map_hi, &a_full[s], kc * 64, b0, rdim2, p0 + q);
-              tma_load_4d(lo + q * p.DY * 128, &map_lo, &a_full[s], kc * 64, b0, rdim2, p0 + q);
+              tma_load_4d(hi + q * p.DY * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b0, rdim2, p0 + q);
+              tma_load_4d(lo + q * p.DY * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b0, rdim2, p0 + q);
             }
           }
         }
