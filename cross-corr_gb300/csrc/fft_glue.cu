@@ -14,6 +14,8 @@
 //  normalize_kernel      replaces the host loop normalize_fft_results
 //                        (src/fft_helpers.hpp:193-261): quadrant swap, division
 //                        by the transform size and crop in one coalesced pass.
+#include <algorithm>
+
 #include "xc_common.cuh"
 #include "xc_internal.h"
 
@@ -43,28 +45,27 @@ __device__ __forceinline__ C mul_conj(C a, C b) {
 
 // dst[m][y][x] = src[m][y - dst_y][x - dst_x] inside the source, 0 elsewhere;
 // dst rows have pitch `dst_pitch` elements (>= pad_cols; the tail of a row
-// beyond pad_cols is left untouched).  Each thread writes 4 consecutive
-// elements of one dst row.
+// beyond pad_cols is left untouched).  grid.y walks the (matrix, row) pairs,
+// so a row's indices are computed once per block; each thread writes 4
+// consecutive elements of the row.
 template <typename T>
 __global__ void pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int rows, int cols, int count, int pad_rows,
                            int pad_cols, int dst_pitch, int dst_y, int dst_x) {
-  const int quads = (pad_cols + 3) / 4;
-  const long long total = (long long)count * pad_rows * quads;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int q = (int)(i % quads);
-    const long long rowid = i / quads;
+  const long long n_rows = (long long)count * pad_rows;
+  const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  if (x0 >= pad_cols) return;
+  for (long long rowid = blockIdx.y; rowid < n_rows; rowid += gridDim.y) {
     const int y = (int)(rowid % pad_rows);
     const long long m = rowid / pad_rows;
     const int sy = y - dst_y;
+    const bool row_in = sy >= 0 && sy < rows;
     const T* srow = src + (m * rows + sy) * (long long)cols;
-    T* drow = dst + (m * pad_rows + y) * (long long)dst_pitch;
-    const int x0 = q * 4;
+    T* drow = dst + rowid * (long long)dst_pitch;
     T v[4];
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int sx = x0 + e - dst_x;
-      v[e] = (sy >= 0 && sy < rows && sx >= 0 && sx < cols) ? srow[sx] : T(0);
+      v[e] = (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
     }
     bool done = false;
     if constexpr (sizeof(T) == 4) {
@@ -81,49 +82,61 @@ __global__ void pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int r
   }
 }
 
-// grid.y = left index l; each thread owns one spectral bin and walks the K
-// partners of l.
+// out[o] = lspec[l] * conj(rspec[r]) bin by bin; grid.y walks the outputs o
+// of the pair map (o -> (l, k) decoded once per block), threads the bins, so
+// every thread issues independent loads.
 template <typename C>
 __global__ void conj_multiply_kernel(const C* __restrict__ lspec, const C* __restrict__ rspec, C* __restrict__ out,
-                                     long long bins, PairMap pm) {
-  const int l = blockIdx.y;
-  const C* lrow = lspec + (long long)l * bins;
-  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < bins;
-       b += (long long)gridDim.x * blockDim.x) {
-    const C lv = lrow[b];
-    for (int k = 0; k < pm.K; ++k) {
-      const long long r = (long long)l * pm.r_l + (long long)k * pm.r_k;
-      const long long o = (long long)l * pm.o_l + (long long)k * pm.o_k;
-      out[o * bins + b] = mul_conj(lv, __ldg(rspec + r * bins + b));
+                                     long long bins, PairMap pm, long long n_out) {
+  const long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (b >= bins) return;
+  for (long long o = blockIdx.y; o < n_out; o += gridDim.y) {
+    // invert o = l*o_l + k*o_k for the three pair-map forms
+    long long l, k;
+    if (pm.o_l == 0) {
+      l = 0;
+      k = o;
+    } else if (pm.o_k == 1 && pm.o_l == pm.K) {
+      l = o / pm.K;
+      k = o % pm.K;
+    } else {
+      l = o % pm.n_left;
+      k = o / pm.n_left;
     }
+    const long long r = l * pm.r_l + k * pm.r_k;
+    out[o * bins + b] = mul_conj(__ldg(lspec + l * bins + b), __ldg(rspec + r * bins + b));
   }
 }
 
 // out[m][sy][sx] = raw[m][(sy - (Hr-1)) mod py][(sx - (Wr-1)) mod px] * scale;
 // with raw=true it instead copies raw[m][y][x] (dense py x px output).
+// grid.y walks the output rows (indices once per block), threads the columns.
 template <typename T, bool F64SCALE>
 __global__ void normalize_kernel(const T* __restrict__ raw, T* __restrict__ out, int py, int px, int raw_pitch,
                                  int count, int Hr, int Wr, int Sy, int Sx, double scale, bool rawcopy) {
   const int oy = rawcopy ? py : Sy, ox = rawcopy ? px : Sx;
-  const long long total = (long long)count * oy * ox;
+  const int sx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sx >= ox) return;
+  const long long n_rows = (long long)count * oy;
   const T fscale = (T)scale;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const int sx = (int)(i % ox);
-    const long long t = i / ox;
-    const int sy = (int)(t % oy);
-    const long long m = t / oy;
-    int ry = sy, rx = sx;
+  int rx = sx;
+  if (!rawcopy) {
+    rx = sx - (Wr - 1);
+    if (rx < 0) rx += px;
+  }
+  for (long long row = blockIdx.y; row < n_rows; row += gridDim.y) {
+    const int sy = (int)(row % oy);
+    const long long m = row / oy;
+    int ry = sy;
     if (!rawcopy) {
       ry = sy - (Hr - 1);
-      rx = sx - (Wr - 1);
       if (ry < 0) ry += py;
-      if (rx < 0) rx += px;
     }
-    const T v = raw[(m * py + ry) * (long long)raw_pitch + rx];
-    if (rawcopy) out[i] = v;
-    else if (F64SCALE) out[i] = (T)((double)v * scale);
-    else out[i] = v * fscale;
+    const T v = __ldg(raw + (m * py + ry) * (long long)raw_pitch + rx);
+    T* o = out + row * (long long)ox + sx;
+    if (rawcopy) *o = v;
+    else if (F64SCALE) *o = (T)((double)v * scale);
+    else *o = v * fscale;
   }
 }
 
@@ -155,35 +168,32 @@ xc_status glue_pad(xc_dtype dtype, const void* src, void* dst, int rows, int col
 xc_status glue_pad_pitched(xc_dtype dtype, const void* src, void* dst, int rows, int cols, int count, int pad_rows,
                            int pad_cols, int dst_pitch, int dst_y, int dst_x, cudaStream_t stream) {
   if (count <= 0) return XC_OK;
-  const long long work = (long long)count * pad_rows * ((pad_cols + 3) / 4);
-  const int threads = 256;
-  const int blocks = grid_for(work, threads);
+  const int threads = 128;
+  const long long n_rows = (long long)count * pad_rows;
+  dim3 grid((unsigned)((pad_cols + 4 * threads - 1) / (4 * threads)), (unsigned)std::min<long long>(n_rows, 65535));
   if (dtype == XC_F32)
-    pad_kernel<float><<<blocks, threads, 0, stream>>>((const float*)src, (float*)dst, rows, cols, count, pad_rows,
-                                                      pad_cols, dst_pitch, dst_y, dst_x);
+    pad_kernel<float><<<grid, threads, 0, stream>>>((const float*)src, (float*)dst, rows, cols, count, pad_rows,
+                                                    pad_cols, dst_pitch, dst_y, dst_x);
   else
-    pad_kernel<double><<<blocks, threads, 0, stream>>>((const double*)src, (double*)dst, rows, cols, count, pad_rows,
-                                                       pad_cols, dst_pitch, dst_y, dst_x);
+    pad_kernel<double><<<grid, threads, 0, stream>>>((const double*)src, (double*)dst, rows, cols, count, pad_rows,
+                                                     pad_cols, dst_pitch, dst_y, dst_x);
   XC_CUDA_TRY(cudaGetLastError());
   return XC_OK;
 }
 
 xc_status glue_conj_multiply_pairs(xc_dtype dtype, const void* lspec, const void* rspec, void* out, long long bins,
                                    const PairMap& pm, long long n_out, cudaStream_t stream) {
-  (void)n_out;
+  if (n_out <= 0 || bins <= 0) return XC_OK;
   const int threads = 256;
-  long long bx = (bins + threads - 1) / threads;
-  const long long cap = (152LL * 32 + pm.n_left - 1) / pm.n_left;
-  if (bx > cap) bx = cap;
-  if (bx < 1) bx = 1;
-  if (pm.n_left > 65535) return fail(XC_ERR_INVALID_ARGUMENT, "too many left matrices for one launch");
-  dim3 grid((unsigned)bx, (unsigned)pm.n_left);
+  const long long bx = (bins + threads - 1) / threads;
+  if (bx > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "spectrum too large for one launch");
+  dim3 grid((unsigned)bx, (unsigned)std::min<long long>(n_out, 65535));
   if (dtype == XC_F32)
     conj_multiply_kernel<float2><<<grid, threads, 0, stream>>>((const float2*)lspec, (const float2*)rspec,
-                                                               (float2*)out, bins, pm);
+                                                               (float2*)out, bins, pm, n_out);
   else
     conj_multiply_kernel<double2><<<grid, threads, 0, stream>>>((const double2*)lspec, (const double2*)rspec,
-                                                                (double2*)out, bins, pm);
+                                                                (double2*)out, bins, pm, n_out);
   XC_CUDA_TRY(cudaGetLastError());
   return XC_OK;
 }
@@ -191,9 +201,10 @@ xc_status glue_conj_multiply_pairs(xc_dtype dtype, const void* lspec, const void
 xc_status glue_normalize_pitched(xc_dtype dtype, const void* raw, void* out, int py, int px, int raw_pitch, int count,
                                  int Hr, int Wr, int Sy, int Sx, bool rawcopy, cudaStream_t stream) {
   if (count <= 0) return XC_OK;
-  const long long work = (long long)count * (rawcopy ? (long long)py * px : (long long)Sy * Sx);
-  const int threads = 256;
-  const int blocks = grid_for(work, threads);
+  const int threads = 128;
+  const int ox = rawcopy ? px : Sx;
+  const long long n_rows = (long long)count * (rawcopy ? py : Sy);
+  dim3 blocks((unsigned)((ox + threads - 1) / threads), (unsigned)std::min<long long>(n_rows, 65535));
   const double scale = 1.0 / ((double)py * (double)px);
   // FP64 scaling for transform sides of 1024 or more.
   const bool f64scale = py >= 1024 || px >= 1024;
