@@ -43,100 +43,149 @@ __device__ __forceinline__ C mul_conj(C a, C b) {
   return r;
 }
 
+constexpr int kGlueRows = 8;  // rows per block in the row-walking glue kernels
+
 // dst[m][y][x] = src[m][y - dst_y][x - dst_x] inside the source, 0 elsewhere;
 // dst rows have pitch `dst_pitch` elements (>= pad_cols; the tail of a row
-// beyond pad_cols is left untouched).  grid.y walks the (matrix, row) pairs,
-// so a row's indices are computed once per block; each thread writes 4
-// consecutive elements of the row.
+// beyond pad_cols is left untouched).  A block walks `rows_per_block`
+// consecutive (matrix, row) pairs, so the row indices cost one division per
+// block; each thread writes 4 consecutive elements per step along the row.
 template <typename T>
 __global__ void pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int rows, int cols, int count, int pad_rows,
-                           int pad_cols, int dst_pitch, int dst_y, int dst_x) {
+                           int pad_cols, int dst_pitch, int dst_y, int dst_x, int rows_per_block) {
   const long long n_rows = (long long)count * pad_rows;
-  const int x0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-  if (x0 >= pad_cols) return;
-  for (long long rowid = blockIdx.y; rowid < n_rows; rowid += gridDim.y) {
-    const int y = (int)(rowid % pad_rows);
-    const long long m = rowid / pad_rows;
+  const long long r0 = (long long)blockIdx.x * rows_per_block;
+  long long m = r0 / pad_rows;
+  int y = (int)(r0 - m * pad_rows);
+  for (int i = 0; i < rows_per_block && r0 + i < n_rows; ++i) {
     const int sy = y - dst_y;
     const bool row_in = sy >= 0 && sy < rows;
     const T* srow = src + (m * rows + sy) * (long long)cols;
-    T* drow = dst + rowid * (long long)dst_pitch;
-    T v[4];
+    T* drow = dst + (r0 + i) * (long long)dst_pitch;
+    for (int x0 = threadIdx.x * 4; x0 < pad_cols; x0 += blockDim.x * 4) {
+      T v[4];
+      const int sx0 = x0 - dst_x;
+      if constexpr (sizeof(T) == 4) {
+        // one 16-byte load when the 4 source elements are in the row and aligned
+        if (row_in && sx0 >= 0 && sx0 + 4 <= cols && (((uintptr_t)(srow + sx0)) & 15) == 0) {
+          const float4 f = __ldg(reinterpret_cast<const float4*>(srow + sx0));
+          v[0] = f.x;
+          v[1] = f.y;
+          v[2] = f.z;
+          v[3] = f.w;
+        } else {
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int sx = x0 + e - dst_x;
-      v[e] = (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
-    }
-    bool done = false;
-    if constexpr (sizeof(T) == 4) {
-      if (x0 + 4 <= pad_cols && (((uintptr_t)(drow + x0)) & 15) == 0) {
-        *reinterpret_cast<float4*>(drow + x0) = make_float4(v[0], v[1], v[2], v[3]);
-        done = true;
+          for (int e = 0; e < 4; ++e) {
+            const int sx = sx0 + e;
+            v[e] = (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int sx = sx0 + e;
+          v[e] = (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
+        }
+      }
+      bool done = false;
+      if constexpr (sizeof(T) == 4) {
+        if (x0 + 4 <= pad_cols && (((uintptr_t)(drow + x0)) & 15) == 0) {
+          *reinterpret_cast<float4*>(drow + x0) = make_float4(v[0], v[1], v[2], v[3]);
+          done = true;
+        } else if (x0 + 4 <= pad_cols && (((uintptr_t)(drow + x0)) & 7) == 0) {
+          // rows of the in-place R2C layout (even pitch) start 8-byte aligned
+          *reinterpret_cast<float2*>(drow + x0) = make_float2(v[0], v[1]);
+          *reinterpret_cast<float2*>(drow + x0 + 2) = make_float2(v[2], v[3]);
+          done = true;
+        }
+      }
+      if (!done) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (x0 + e < pad_cols) drow[x0 + e] = v[e];
       }
     }
-    if (!done) {
-#pragma unroll
-      for (int e = 0; e < 4; ++e)
-        if (x0 + e < pad_cols) drow[x0 + e] = v[e];
+    if (++y == pad_rows) {
+      y = 0;
+      ++m;
     }
   }
 }
 
-// out[o] = lspec[l] * conj(rspec[r]) bin by bin; grid.y walks the outputs o
-// of the pair map (o -> (l, k) decoded once per block), threads the bins, so
-// every thread issues independent loads.
+// out[l*o_l + k*o_k] = lspec[l] * conj(rspec[l*r_l + k*r_k]) bin by bin:
+// grid.y = left index l, each thread owns one bin and walks the K partners
+// of l eight at a time, with the eight right loads issued together.
 template <typename C>
 __global__ void conj_multiply_kernel(const C* __restrict__ lspec, const C* __restrict__ rspec, C* __restrict__ out,
                                      long long bins, PairMap pm, long long n_out) {
-  const long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (b >= bins) return;
-  for (long long o = blockIdx.y; o < n_out; o += gridDim.y) {
-    // invert o = l*o_l + k*o_k for the three pair-map forms
-    long long l, k;
-    if (pm.o_l == 0) {
-      l = 0;
-      k = o;
-    } else if (pm.o_k == 1 && pm.o_l == pm.K) {
-      l = o / pm.K;
-      k = o % pm.K;
-    } else {
-      l = o % pm.n_left;
-      k = o / pm.n_left;
+  (void)n_out;
+  const int l = blockIdx.y;
+  const C* lrow = lspec + (long long)l * bins;
+  const C* rbase = rspec + (long long)l * pm.r_l * bins;
+  C* obase = out + (long long)l * pm.o_l * bins;
+  const long long rstep = (long long)pm.r_k * bins, ostep = (long long)pm.o_k * bins;
+  for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < bins;
+       b += (long long)gridDim.x * blockDim.x) {
+    const C lv = __ldg(lrow + b);
+    int k = 0;
+    for (; k + 8 <= pm.K; k += 8) {
+      C rv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) rv[u] = __ldg(rbase + (k + u) * rstep + b);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) obase[(k + u) * ostep + b] = mul_conj(lv, rv[u]);
     }
-    const long long r = l * pm.r_l + k * pm.r_k;
-    out[o * bins + b] = mul_conj(__ldg(lspec + l * bins + b), __ldg(rspec + r * bins + b));
+    for (; k < pm.K; ++k) obase[k * ostep + b] = mul_conj(lv, __ldg(rbase + k * rstep + b));
   }
 }
 
 // out[m][sy][sx] = raw[m][(sy - (Hr-1)) mod py][(sx - (Wr-1)) mod px] * scale;
-// with raw=true it instead copies raw[m][y][x] (dense py x px output).
-// grid.y walks the output rows (indices once per block), threads the columns.
+// with raw=true it instead copies raw[m][y][x] (dense py x px output).  A
+// block takes kGlueRows output rows (one division per block) and resolves
+// their row pointers first; each thread then steps along the rows with the
+// kGlueRows loads of a column issued together.
 template <typename T, bool F64SCALE>
 __global__ void normalize_kernel(const T* __restrict__ raw, T* __restrict__ out, int py, int px, int raw_pitch,
                                  int count, int Hr, int Wr, int Sy, int Sx, double scale, bool rawcopy) {
   const int oy = rawcopy ? py : Sy, ox = rawcopy ? px : Sx;
-  const int sx = blockIdx.x * blockDim.x + threadIdx.x;
-  if (sx >= ox) return;
   const long long n_rows = (long long)count * oy;
   const T fscale = (T)scale;
-  int rx = sx;
-  if (!rawcopy) {
-    rx = sx - (Wr - 1);
-    if (rx < 0) rx += px;
-  }
-  for (long long row = blockIdx.y; row < n_rows; row += gridDim.y) {
-    const int sy = (int)(row % oy);
-    const long long m = row / oy;
+  const long long r0 = (long long)blockIdx.x * kGlueRows;
+  long long m = r0 / oy;
+  int sy = (int)(r0 - m * oy);
+  const T* rrow[kGlueRows];
+  const int nr = (int)min((long long)kGlueRows, n_rows - r0);
+#pragma unroll
+  for (int i = 0; i < kGlueRows; ++i) {
     int ry = sy;
     if (!rawcopy) {
       ry = sy - (Hr - 1);
       if (ry < 0) ry += py;
     }
-    const T v = __ldg(raw + (m * py + ry) * (long long)raw_pitch + rx);
-    T* o = out + row * (long long)ox + sx;
-    if (rawcopy) *o = v;
-    else if (F64SCALE) *o = (T)((double)v * scale);
-    else *o = v * fscale;
+    rrow[i] = raw + (m * py + ry) * (long long)raw_pitch;
+    if (++sy == oy) {
+      sy = 0;
+      ++m;
+    }
+  }
+  T* orow = out + r0 * (long long)ox;
+  const int xoff = rawcopy ? 0 : Wr - 1;
+  for (int sx = threadIdx.x; sx < ox; sx += blockDim.x) {
+    int rx = sx - xoff;
+    if (rx < 0) rx += px;
+    T v[kGlueRows];
+#pragma unroll
+    for (int i = 0; i < kGlueRows; ++i) v[i] = i < nr ? __ldg(rrow[i] + rx) : T(0);
+#pragma unroll
+    for (int i = 0; i < kGlueRows; ++i) {
+      if (i < nr) {
+        T w;
+        if (rawcopy) w = v[i];
+        else if (F64SCALE) w = (T)((double)v[i] * scale);
+        else w = v[i] * fscale;
+        orow[(long long)i * ox + sx] = w;
+      }
+    }
   }
 }
 
@@ -168,15 +217,19 @@ xc_status glue_pad(xc_dtype dtype, const void* src, void* dst, int rows, int col
 xc_status glue_pad_pitched(xc_dtype dtype, const void* src, void* dst, int rows, int cols, int count, int pad_rows,
                            int pad_cols, int dst_pitch, int dst_y, int dst_x, cudaStream_t stream) {
   if (count <= 0) return XC_OK;
-  const int threads = 128;
   const long long n_rows = (long long)count * pad_rows;
-  dim3 grid((unsigned)((pad_cols + 4 * threads - 1) / (4 * threads)), (unsigned)std::min<long long>(n_rows, 65535));
+  // a few rows per block when there are many (fewer index divisions), one
+  // when there are few (enough blocks to fill the GPU)
+  const int rpb = (int)std::max(1LL, std::min((long long)kGlueRows, n_rows / (152LL * 16)));
+  const long long blocks = (n_rows + rpb - 1) / rpb;
+  if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "too many rows for one launch");
+  const int threads = pad_cols >= 512 ? 128 : 64;
   if (dtype == XC_F32)
-    pad_kernel<float><<<grid, threads, 0, stream>>>((const float*)src, (float*)dst, rows, cols, count, pad_rows,
-                                                    pad_cols, dst_pitch, dst_y, dst_x);
+    pad_kernel<float><<<(unsigned)blocks, threads, 0, stream>>>((const float*)src, (float*)dst, rows, cols, count,
+                                                                pad_rows, pad_cols, dst_pitch, dst_y, dst_x, rpb);
   else
-    pad_kernel<double><<<grid, threads, 0, stream>>>((const double*)src, (double*)dst, rows, cols, count, pad_rows,
-                                                     pad_cols, dst_pitch, dst_y, dst_x);
+    pad_kernel<double><<<(unsigned)blocks, threads, 0, stream>>>((const double*)src, (double*)dst, rows, cols, count,
+                                                                 pad_rows, pad_cols, dst_pitch, dst_y, dst_x, rpb);
   XC_CUDA_TRY(cudaGetLastError());
   return XC_OK;
 }
@@ -185,9 +238,11 @@ xc_status glue_conj_multiply_pairs(xc_dtype dtype, const void* lspec, const void
                                    const PairMap& pm, long long n_out, cudaStream_t stream) {
   if (n_out <= 0 || bins <= 0) return XC_OK;
   const int threads = 256;
-  const long long bx = (bins + threads - 1) / threads;
-  if (bx > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "spectrum too large for one launch");
-  dim3 grid((unsigned)bx, (unsigned)std::min<long long>(n_out, 65535));
+  long long bx = (bins + threads - 1) / threads;
+  const long long cap = (152LL * 64 + pm.n_left - 1) / pm.n_left;
+  if (bx > cap) bx = cap;
+  if (pm.n_left > 65535) return fail(XC_ERR_INVALID_ARGUMENT, "too many left matrices for one launch");
+  dim3 grid((unsigned)bx, (unsigned)pm.n_left);
   if (dtype == XC_F32)
     conj_multiply_kernel<float2><<<grid, threads, 0, stream>>>((const float2*)lspec, (const float2*)rspec,
                                                                (float2*)out, bins, pm, n_out);
@@ -201,10 +256,12 @@ xc_status glue_conj_multiply_pairs(xc_dtype dtype, const void* lspec, const void
 xc_status glue_normalize_pitched(xc_dtype dtype, const void* raw, void* out, int py, int px, int raw_pitch, int count,
                                  int Hr, int Wr, int Sy, int Sx, bool rawcopy, cudaStream_t stream) {
   if (count <= 0) return XC_OK;
-  const int threads = 128;
   const int ox = rawcopy ? px : Sx;
+  const int threads = ox >= 512 ? 128 : 64;
   const long long n_rows = (long long)count * (rawcopy ? py : Sy);
-  dim3 blocks((unsigned)((ox + threads - 1) / threads), (unsigned)std::min<long long>(n_rows, 65535));
+  const long long nb = (n_rows + kGlueRows - 1) / kGlueRows;
+  if (nb > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "too many rows for one launch");
+  const unsigned blocks = (unsigned)nb;
   const double scale = 1.0 / ((double)py * (double)px);
   // FP64 scaling for transform sides of 1024 or more.
   const bool f64scale = py >= 1024 || px >= 1024;
