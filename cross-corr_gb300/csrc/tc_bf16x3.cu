@@ -60,6 +60,7 @@
 #include <cstdlib>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "xc_common.cuh"
 #include "xc_internal.h"
@@ -77,6 +78,7 @@ constexpr int kThreads = 32 * (2 + kBuilderWarps + kEpiWarps);
 constexpr int kMaxLp = 512 + 256;      // staged left row pairs: 128 * tiles + 64 * chunks
 constexpr uint32_t kRingCol = 256;     // first TMEM column of the Toeplitz ring
 constexpr int kBarBytes = 256;         // 15 mbarriers, the abort flag, the TMEM address slot
+constexpr int kMaxChunkRows = 1024;    // left rows per work item at most
 
 struct TcParams {
   const float* left;
@@ -93,7 +95,9 @@ struct TcParams {
   int kstep;        // columns per K-step: 16 (BF16) or 8 (TF32)
   int lp_len;       // staged left row length
   int flush_rows;   // drain TMEM every this many left rows
-  int chunk_rows;   // left rows per CTA (a longer row range is split over CTAs)
+  int chunk_rows;   // left rows per work item (a longer row range is split over items)
+  const int* items;  // non-empty work items, most left rows first (index encoding of tc_item)
+  const int* n_live; // entries of `items` (written on the device)
   int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
   DeviceFlags* flags;
 };
@@ -214,9 +218,9 @@ __device__ __forceinline__ bool bar_red_or(bool v, int id, int nthreads) {
 
 // dy-tile visiting order: centre (heaviest overlap) first, then alternating
 // outwards, so long tiles start early.
-__device__ __forceinline__ int centre_out(int r, int n, int tc) {
+__host__ __device__ __forceinline__ int centre_out(int r, int n, int tc) {
   const int below = tc, above = n - tc - 1;
-  const int m = min(below, above);
+  const int m = below < above ? below : above;
   if (r == 0) return tc;
   if (r <= 2 * m) return (r & 1) ? tc + (r + 1) / 2 : tc - r / 2;
   const int extra = r - 2 * m;
@@ -234,6 +238,67 @@ __device__ __forceinline__ uint32_t tile_mask(int s0, const TcParams& p) {
     if (k0 < p.Wr && s0 + k0 + 127 + p.kstep - 1 >= p.Wr - 1 && s0 + k0 <= p.Wr + p.Wl - 2) m |= 1u << j;
   }
   return m;
+}
+
+// One work item: two 128-shift tiles (one CTA half) of one (left matrix,
+// partner group, row-shift group, chunk of left rows).
+struct TcItem {
+  int l, p0, dy0, a_lo, n_rows, rdim2, s0_0, s0_1;
+  uint32_t mask0, mask1;
+};
+
+// idx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_halves + half;
+// false when the item has no left rows.
+__device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
+  const int half = (int)(idx % p.n_halves);
+  const long long bid = idx / p.n_halves;
+  const int per_rank = p.pm.n_left * p.n_pgroups;
+  const int lp = (int)(bid % per_rank);
+  const int rank = (int)((bid / per_rank) % p.n_dytiles);
+  const int chunk = (int)(bid / ((long long)per_rank * p.n_dytiles));
+  w->l = lp / p.n_pgroups;
+  w->p0 = (lp % p.n_pgroups) * p.P;
+  const int t = centre_out(rank, p.n_dytiles, (p.Hr - 1) / p.DY);
+  w->dy0 = -(p.Hr - 1) + t * p.DY;
+  const int tile_lo = max(0, w->dy0);
+  const int tile_hi = min(p.Hl, w->dy0 + p.DY - 1 + p.Hr);
+  w->a_lo = tile_lo + chunk * p.chunk_rows;
+  const int a_hi = min(tile_hi, w->a_lo + p.chunk_rows);
+  w->n_rows = a_hi - w->a_lo;
+  w->rdim2 = p.pm.r_l != 0 ? w->l : 0;
+  w->s0_0 = 256 * half;
+  w->s0_1 = w->s0_0 + 128;
+  w->mask0 = tile_mask(w->s0_0, p);
+  w->mask1 = tile_mask(w->s0_1, p);
+  return w->n_rows > 0;
+}
+
+// Lists the non-empty work items, most left rows first (a counting sort by
+// row count): one block.  Every CTA of tc_kernel reads the same list.
+__global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long long n_total, int* __restrict__ items,
+                                                        int* __restrict__ n_live) {
+  __shared__ int cnt[kMaxChunkRows + 1];
+  for (int r = threadIdx.x; r <= kMaxChunkRows; r += blockDim.x) cnt[r] = 0;
+  __syncthreads();
+  for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
+    TcItem w;
+    if (tc_item(p, idx, &w)) atomicAdd(&cnt[w.n_rows], 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int r = p.chunk_rows; r >= 1; --r) {
+      const int c = cnt[r];
+      cnt[r] = run;  // first position of the items with r rows
+      run += c;
+    }
+    *n_live = run;
+  }
+  __syncthreads();
+  for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
+    TcItem w;
+    if (tc_item(p, idx, &w)) items[atomicAdd(&cnt[w.n_rows], 1)] = (int)idx;
+  }
 }
 
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
@@ -262,8 +327,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char* b_tiles = smem;                                                  // kStages x (hi, lo) x 16 KB
   // split left row as overlapping BF16 pairs, two rows: pairs[row][hi/lo][j] = (x_j, x_j+1)
   uint32_t* pairs = reinterpret_cast<uint32_t*>(smem + kStages * kStageBytes);    // 2 x 2 x kMaxLp
-  long long* row_base = reinterpret_cast<long long*>(pairs + 4 * kMaxLp);         // 128 output row offsets
-  uint64_t* bars = reinterpret_cast<uint64_t*>(row_base + 128);
+  long long* row_base = reinterpret_cast<long long*>(pairs + 4 * kMaxLp);         // 2 x 128 output row offsets
+  uint64_t* bars = reinterpret_cast<uint64_t*>(row_base + 256);
   uint64_t* a_full = bars;              // [kStages] right-row tiles landed
   uint64_t* a_empty = bars + kStages;   // [kStages] tiles consumed
   uint64_t* s_full = bars + 2 * kStages;  // [2] Toeplitz ring slot written
@@ -274,30 +339,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 1);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 2);
 
-  // ---- work item of this CTA ---------------------------------------------
-  // blockIdx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_halves + half
-  const int half = blockIdx.x % p.n_halves;
-  const int bid = blockIdx.x / p.n_halves;
-  const int per_rank = p.pm.n_left * p.n_pgroups;
-  const int lp = bid % per_rank;
-  const int rank = (bid / per_rank) % p.n_dytiles;
-  const int chunk = bid / (per_rank * p.n_dytiles);
-  const int l = lp / p.n_pgroups;
-  const int p0 = (lp % p.n_pgroups) * p.P;
-  const int t = centre_out(rank, p.n_dytiles, (p.Hr - 1) / p.DY);
-  const int dy0 = -(p.Hr - 1) + t * p.DY;
-  const int tile_lo = max(0, dy0);
-  const int tile_hi = min(p.Hl, dy0 + p.DY - 1 + p.Hr);
-  const int a_lo = tile_lo + chunk * p.chunk_rows;
-  const int a_hi = min(tile_hi, a_lo + p.chunk_rows);
-  const int n_rows = a_hi - a_lo;
-  if (n_rows <= 0) return;  // uniform over the CTA
-  const int n_drains = (n_rows + p.flush_rows - 1) / p.flush_rows;
-  const int rdim2 = p.pm.r_l != 0 ? l : 0;
-  const int s0_0 = 256 * half, s0_1 = s0_0 + 128;
-  const uint32_t mask0 = tile_mask(s0_0, p), mask1 = tile_mask(s0_1, p);
-
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // Persistent: the work list is sorted by left rows (heaviest first) and
+  // dealt out in a snake order (round r gives position r*G + c, or
+  // r*G + G-1-c on odd rounds); every role walks the same items and keeps its
+  // pipeline counters running across them, so the next item's loads and
+  // MMAs overlap the previous item's final adds.
+  const long long n_items = *p.n_live;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
@@ -332,28 +380,34 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int it = 0;
       bool ok = true;
-      for (int ai = 0; ai < n_rows && ok; ++ai) {
-        const int a = a_lo + ai;
-        for (int kc = 0; kc < p.nkc && ok; ++kc, ++it) {
-          const int s = it % kStages;
-          if (!wait_or_abort_sleep(&a_empty[s], ((it / kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
-            ok = false;
-            break;
-          }
-          mbar_arrive_expect_tx(&a_full[s], kStageBytes);
-          unsigned char* hi = b_tiles + s * kStageBytes;
-          unsigned char* lo = hi + kTileBytes;
-          if (p.mats_mode) {
-            for (int d = 0; d < p.DY; ++d) {
-              const int b = a - (dy0 + d);
-              tma_load_4d(hi + d * p.P * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b, rdim2, p0);
-              tma_load_4d(lo + d * p.P * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b, rdim2, p0);
+      for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
+        const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
+        if (pos >= n_items) continue;
+        TcItem w;
+        if (!tc_item(p, p.items[pos], &w)) continue;
+        for (int ai = 0; ai < w.n_rows && ok; ++ai) {
+          const int a = w.a_lo + ai;
+          for (int kc = 0; kc < p.nkc && ok; ++kc, ++it) {
+            const int s = it % kStages;
+            if (!wait_or_abort_sleep(&a_empty[s], ((it / kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
+              ok = false;
+              break;
             }
-          } else {
-            const int b0 = a - dy0 - (p.DY - 1);
-            for (int q = 0; q < p.P; ++q) {
-              tma_load_4d(hi + q * p.DY * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b0, rdim2, p0 + q);
-              tma_load_4d(lo + q * p.DY * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b0, rdim2, p0 + q);
+            mbar_arrive_expect_tx(&a_full[s], kStageBytes);
+            unsigned char* hi = b_tiles + s * kStageBytes;
+            unsigned char* lo = hi + kTileBytes;
+            if (p.mats_mode) {
+              for (int d = 0; d < p.DY; ++d) {
+                const int b = a - (w.dy0 + d);
+                tma_load_4d(hi + d * p.P * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b, w.rdim2, w.p0);
+                tma_load_4d(lo + d * p.P * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b, w.rdim2, w.p0);
+              }
+            } else {
+              const int b0 = a - w.dy0 - (p.DY - 1);
+              for (int q = 0; q < p.P; ++q) {
+                tma_load_4d(hi + q * p.DY * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b0, w.rdim2, w.p0 + q);
+                tma_load_4d(lo + q * p.DY * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b0, w.rdim2, w.p0 + q);
+              }
             }
           }
         }
@@ -369,59 +423,66 @@ __global__ void __launch_bounds__(kThreads, 1)
       constexpr uint32_t kDescHi = (1024u >> 4) | (1u << 14) | (2u << 29);  // SBO 1024 B, 128-byte swizzle
       const uint32_t idesc = TF ? idesc_tf32_f32(128, 128) : idesc_bf16_f32(128, 128);
       const uint32_t b_lo_word = ((smem_u32(b_tiles) >> 4) & 0x3FFFu) | (1u << 16);
-      const int first0 = mask0 ? __ffs(mask0) - 1 : -1;
-      const int first1 = mask1 ? __ffs(mask1) - 1 : -1;
-      int it = 0, rows_in = 0, windows = 0;
+      int it = 0, windows = 0;
       bool ok = true;
-      for (int ai = 0; ai < n_rows && ok; ++ai) {
-        if (rows_in == 0) {
-          // the epilogue must have drained the previous window
-          if (!wait_or_abort(t_empty, (windows & 1) ^ 1, abort_flag, p.flags, 14)) {
-            ok = false;
-            break;
-          }
-        }
-        for (int kc = 0; kc < p.nkc; ++kc, ++it) {
-          const int s = it % kStages, slot = it & 1;
-          if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13) ||
-              !wait_or_abort(&s_full[slot], (it >> 1) & 1, abort_flag, p.flags, 12)) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          const uint32_t bw = b_lo_word + (uint32_t)s * (kStageBytes >> 4);
-          const uint32_t ring = tmem_base + kRingCol + (uint32_t)slot * 128;
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const int j = kc * 4 + ks;
-            const uint64_t bhi = make_desc(bw + ks * 2, kDescHi);
-            const uint64_t blo = make_desc(bw + (kTileBytes >> 4) + ks * 2, kDescHi);
-#pragma unroll
-            for (int tt = 0; tt < 2; ++tt) {
-              if (!(((tt == 0 ? mask0 : mask1) >> j) & 1u)) continue;
-              const bool reset = rows_in == 0 && j == (tt == 0 ? first0 : first1);
-              const uint32_t ahi = ring + (uint32_t)(tt * 4 + ks) * 16, alo = ahi + 8;
-              const uint32_t d = tmem_base + (uint32_t)tt * 128;
-              if constexpr (TF) {
-                mma_tf32_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
-                mma_tf32_ts(d, ahi, blo, idesc, 1u);
-                mma_tf32_ts(d, alo, bhi, idesc, 1u);
-              } else {
-                mma_bf16_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
-                mma_bf16_ts(d, ahi, blo, idesc, 1u);
-                mma_bf16_ts(d, alo, bhi, idesc, 1u);
-              }
+      for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
+        const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
+        if (pos >= n_items) continue;
+        TcItem w;
+        if (!tc_item(p, p.items[pos], &w)) continue;
+        const int first0 = w.mask0 ? __ffs(w.mask0) - 1 : -1;
+        const int first1 = w.mask1 ? __ffs(w.mask1) - 1 : -1;
+        int rows_in = 0;
+        for (int ai = 0; ai < w.n_rows && ok; ++ai) {
+          if (rows_in == 0) {
+            // the epilogue must have drained the previous window
+            if (!wait_or_abort(t_empty, (windows & 1) ^ 1, abort_flag, p.flags, 14)) {
+              ok = false;
+              break;
             }
           }
-          mma_commit(&a_empty[s]);
-          mma_commit(&s_empty[slot]);
-        }
-        if (!ok) break;
-        ++rows_in;
-        if (rows_in == p.flush_rows || ai == n_rows - 1) {
-          mma_commit(t_full);
-          ++windows;
-          rows_in = 0;
+          for (int kc = 0; kc < p.nkc; ++kc, ++it) {
+            const int s = it % kStages, slot = it & 1;
+            if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13) ||
+                !wait_or_abort(&s_full[slot], (it >> 1) & 1, abort_flag, p.flags, 12)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t bw = b_lo_word + (uint32_t)s * (kStageBytes >> 4);
+            const uint32_t ring = tmem_base + kRingCol + (uint32_t)slot * 128;
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const int j = kc * 4 + ks;
+              const uint64_t bhi = make_desc(bw + ks * 2, kDescHi);
+              const uint64_t blo = make_desc(bw + (kTileBytes >> 4) + ks * 2, kDescHi);
+#pragma unroll
+              for (int tt = 0; tt < 2; ++tt) {
+                if (!(((tt == 0 ? w.mask0 : w.mask1) >> j) & 1u)) continue;
+                const bool reset = rows_in == 0 && j == (tt == 0 ? first0 : first1);
+                const uint32_t ahi = ring + (uint32_t)(tt * 4 + ks) * 16, alo = ahi + 8;
+                const uint32_t d = tmem_base + (uint32_t)tt * 128;
+                if constexpr (TF) {
+                  mma_tf32_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
+                  mma_tf32_ts(d, ahi, blo, idesc, 1u);
+                  mma_tf32_ts(d, alo, bhi, idesc, 1u);
+                } else {
+                  mma_bf16_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
+                  mma_bf16_ts(d, ahi, blo, idesc, 1u);
+                  mma_bf16_ts(d, alo, bhi, idesc, 1u);
+                }
+              }
+            }
+            mma_commit(&a_empty[s]);
+            mma_commit(&s_empty[slot]);
+          }
+          if (!ok) break;
+          ++rows_in;
+          if (rows_in == p.flush_rows || ai == w.n_rows - 1) {
+            mma_commit(t_full);
+            ++windows;
+            rows_in = 0;
+          }
         }
       }
       // All MMAs issued by this thread must finish before TMEM is released.
@@ -437,62 +498,72 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int qd = warp & 3;
     const int m = 32 * qd + lane;
     const uint32_t lane_addr = tmem_base + ((uint32_t)(32 * qd) << 16) + kRingCol;
-    const float* lrow_base = p.left + (long long)l * p.Hl * p.Wl;
-    const float mu = p.mu_left[l];
-    int it = 0;
+    int it = 0, rows_done = 0;
     bool ok = true;
-    for (int ai = 0; ai < n_rows; ++ai) {
-      // split the centred, zero-padded left row x_j = L[a][j - (Wr-1)] - mu
-      // into pairs (x_j, x_j+1) of BF16 hi parts and of BF16 lo parts
-      uint32_t* ph = pairs + (ai & 1) * (2 * kMaxLp);
-      uint32_t* pl = ph + kMaxLp;
-      const float* src = lrow_base + (long long)(a_lo + ai) * p.Wl;
-      for (int j = bt; j < p.lp_len; j += 32 * kBuilderWarps) {
-        const int x = j - (p.Wr - 1);
-        const float x0 = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
-        if constexpr (TF) {
-          // TF32: one element per column, hi and lo parts
-          const float h = tf32_round(x0);
-          ph[j] = __float_as_uint(h);
-          pl[j] = __float_as_uint(tf32_round(x0 - h));
-        } else {
-          const float x1 = (x + 1 >= 0 && x + 1 < p.Wl) ? __ldg(src + x + 1) - mu : 0.0f;
-          const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-          ph[j] = bf16x2_bits(h);
-          pl[j] = bf16x2_bits(__floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h)));
+    for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
+      const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
+      if (pos >= n_items) continue;
+      TcItem w;
+      if (!tc_item(p, p.items[pos], &w)) continue;
+      const float* lrow_base = p.left + (long long)w.l * p.Hl * p.Wl;
+      const float mu = p.mu_left[w.l];
+      for (int ai = 0; ai < w.n_rows; ++ai, ++rows_done) {
+        // split the centred, zero-padded left row x_j = L[a][j - (Wr-1)] - mu
+        // into pairs (x_j, x_j+1) of BF16 hi parts and of BF16 lo parts
+        uint32_t* ph = pairs + (rows_done & 1) * (2 * kMaxLp);
+        uint32_t* pl = ph + kMaxLp;
+        const float* src = lrow_base + (long long)(w.a_lo + ai) * p.Wl;
+        for (int j = bt; j < p.lp_len; j += 32 * kBuilderWarps) {
+          const int x = j - (p.Wr - 1);
+          const float x0 = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
+          if constexpr (TF) {
+            // TF32: one element per column, hi and lo parts
+            const float h = tf32_round(x0);
+            ph[j] = __float_as_uint(h);
+            pl[j] = __float_as_uint(tf32_round(x0 - h));
+          } else {
+            const float x1 = (x + 1 >= 0 && x + 1 < p.Wl) ? __ldg(src + x + 1) - mu : 0.0f;
+            const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+            ph[j] = bf16x2_bits(h);
+            pl[j] = bf16x2_bits(__floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h)));
+          }
         }
-      }
-      // the builder threads leave together (they share a named barrier)
-      if (bar_red_or(!ok, 1, 32 * kBuilderWarps)) break;
-      for (int kc = 0; kc < p.nkc; ++kc, ++it) {
-        const int slot = it & 1;
-        bool w = wait_or_abort_sleep(&s_empty[slot], ((it >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
-        w = __all_sync(0xffffffffu, w);  // tcgen05.st below must stay warp-uniform
-        if (!w) {
+        // the builder threads leave together (they share a named barrier)
+        if (bar_red_or(!ok, 1, 32 * kBuilderWarps)) {
           ok = false;
           break;
         }
-        tc_fence_after();
-#pragma unroll
-        for (int tt = 0; tt < 2; ++tt) {
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const int j = kc * 4 + ks;
-            if (!(((tt == 0 ? mask0 : mask1) >> j) & 1u)) continue;
-            const int base = (tt == 0 ? s0_0 : s0_1) + m + p.kstep * j;
-            uint32_t r[16];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-              r[e] = ph[base + (TF ? 1 : 2) * e];
-              r[8 + e] = pl[base + (TF ? 1 : 2) * e];
-            }
-            tmem_st16(lane_addr + (uint32_t)slot * 128 + (uint32_t)(tt * 4 + ks) * 16, r);
+        for (int kc = 0; kc < p.nkc; ++kc, ++it) {
+          const int slot = it & 1;
+          bool wt = wait_or_abort_sleep(&s_empty[slot], ((it >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
+          wt = __all_sync(0xffffffffu, wt);  // tcgen05.st below must stay warp-uniform
+          if (!wt) {
+            ok = false;
+            break;
           }
+          tc_fence_after();
+#pragma unroll
+          for (int tt = 0; tt < 2; ++tt) {
+#pragma unroll
+            for (int ks = 0; ks < 4; ++ks) {
+              const int j = kc * 4 + ks;
+              if (!(((tt == 0 ? w.mask0 : w.mask1) >> j) & 1u)) continue;
+              const int base = (tt == 0 ? w.s0_0 : w.s0_1) + m + p.kstep * j;
+              uint32_t r[16];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                r[e] = ph[base + (TF ? 1 : 2) * e];
+                r[8 + e] = pl[base + (TF ? 1 : 2) * e];
+              }
+              tmem_st16(lane_addr + (uint32_t)slot * 128 + (uint32_t)(tt * 4 + ks) * 16, r);
+            }
+          }
+          tmem_wait_st();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&s_full[slot]);  // one arrival per warp
         }
-        tmem_wait_st();
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&s_full[slot]);  // one arrival per warp
+        // a failed wait reaches the other builders at the next row's barrier
       }
     }
   } else {
@@ -504,58 +575,71 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int tt = ew >> 3;
     const int nb = ((ew >> 2) & 1) * kCols;
     const int et = threadIdx.x - 32 * (2 + kBuilderWarps);  // 0..511
-    if (et < 128) {
-      // output row offset of B row n (-1: outside the output)
-      const int n = et;
-      int pp, dy;
-      if (p.mats_mode) {
-        pp = n % p.P;
-        dy = dy0 + n / p.P;
-      } else {
-        pp = n / p.DY;
-        dy = dy0 + (p.DY - 1) - (n % p.DY);
-      }
-      const int k = p0 + pp, sy = dy + p.Hr - 1;
-      row_base[n] = (k < p.pm.K && sy >= 0 && sy < p.Sy)
-                        ? (((long long)l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx
-                        : -1LL;
-    }
-    asm volatile("bar.sync 2, %0;" ::"r"(32 * kEpiWarps) : "memory");
-    float acc[kCols];
-#pragma unroll
-    for (int i = 0; i < kCols; ++i) acc[i] = 0.0f;
-    const bool live = (tt == 0 ? mask0 : mask1) != 0u;
+    int d_all = 0, n_done = 0;
     bool ok = true;
-    for (int d = 0; d < n_drains; ++d) {
-      bool w = wait_or_abort_sleep(t_full, d & 1, abort_flag, p.flags, 16);
-      w = __all_sync(0xffffffffu, w);  // tcgen05.ld below must stay warp-uniform
-      if (!w) {
-        ok = false;
-        break;
+    for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
+      const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
+      if (pos >= n_items) continue;
+      TcItem w;
+      if (!tc_item(p, p.items[pos], &w)) continue;
+      long long* rbase = row_base + (n_done & 1) * 128;
+      if (et < 128) {
+        // output row offset of B row n (-1: outside the output)
+        const int n = et;
+        int pp, dy;
+        if (p.mats_mode) {
+          pp = n % p.P;
+          dy = w.dy0 + n / p.P;
+        } else {
+          pp = n / p.DY;
+          dy = w.dy0 + (p.DY - 1) - (n % p.DY);
+        }
+        const int k = w.p0 + pp, sy = dy + p.Hr - 1;
+        rbase[n] = (k < p.pm.K && sy >= 0 && sy < p.Sy)
+                       ? (((long long)w.l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx
+                       : -1LL;
       }
-      tc_fence_after();
-      if (live) {
-        const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(tt * 128 + nb);
+      // publishes the table; every epilogue thread has finished the item
+      // that used this half of it two items ago
+      asm volatile("bar.sync 2, %0;" ::"r"(32 * kEpiWarps) : "memory");
+      float acc[kCols];
 #pragma unroll
-        for (int j = 0; j < kCols; j += 8) {
-          float v[8];
-          tmem_ld8(col0 + (uint32_t)j, v);
-          tmem_wait_ld();
+      for (int i = 0; i < kCols; ++i) acc[i] = 0.0f;
+      const uint32_t tmask = tt == 0 ? w.mask0 : w.mask1;
+      const bool live = tmask != 0u;
+      const int n_drains = (w.n_rows + p.flush_rows - 1) / p.flush_rows;
+      for (int d = 0; d < n_drains; ++d, ++d_all) {
+        bool wt = wait_or_abort_sleep(t_full, d_all & 1, abort_flag, p.flags, 16);
+        wt = __all_sync(0xffffffffu, wt);  // tcgen05.ld below must stay warp-uniform
+        if (!wt) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        if (live) {
+          const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(tt * 128 + nb);
 #pragma unroll
-          for (int i = 0; i < 8; ++i) acc[j + i] += v[i];
+          for (int j = 0; j < kCols; j += 8) {
+            float v[8];
+            tmem_ld8(col0 + (uint32_t)j, v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[j + i] += v[i];
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(t_empty);  // one arrival per warp
+      }
+      const int sx = (tt == 0 ? w.s0_0 : w.s0_1) + 32 * q + lane;
+      if (ok && live && sx < p.Sx) {
+#pragma unroll
+        for (int i = 0; i < kCols; ++i) {
+          const long long rb = rbase[nb + i];
+          if (rb >= 0) red_add(p.out + rb + sx, acc[i]);
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(t_empty);  // one arrival per warp
-    }
-    const int sx = (tt == 0 ? s0_0 : s0_1) + 32 * q + lane;
-    if (ok && live && sx < p.Sx) {
-#pragma unroll
-      for (int i = 0; i < kCols; ++i) {
-        const long long rb = row_base[nb + i];
-        if (rb >= 0) red_add(p.out + rb + sx, acc[i]);
-      }
+      ++n_done;
     }
   }
 
@@ -756,9 +840,12 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, lp_len, pitch;
+  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, lp_len, pitch, n_chunks;
+  long long n_items;
   int smem_bytes;
 };
+
+int chunk_rows();
 
 bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   if (g.Sx > 512 || g.Wr > 256) return false;  // four 128-shift tiles, 16 K-steps
@@ -775,7 +862,9 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   t->nkc = (g.Wr + chunk - 1) / chunk;
   t->lp_len = 128 * t->n_tiles + 4 * t->kstep * t->nkc;
   t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
-  t->smem_bytes = 1024 + kStages * kStageBytes + 4 * kMaxLp * 4 + 128 * 8 + kBarBytes;
+  t->n_chunks = div_up(t->DY - 1 + std::min(g.Hl, g.Hr), chunk_rows());
+  t->n_items = (long long)t->n_halves * t->n_chunks * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
+  t->smem_bytes = 1024 + kStages * kStageBytes + 4 * kMaxLp * 4 + 2 * 128 * 8 + kBarBytes;
   return t->lp_len <= kMaxLp && t->smem_bytes <= 227 * 1024;
 }
 
@@ -803,7 +892,7 @@ int flush_rows(int nkc) {
   return std::max(1, std::min(32, 192 / (12 * nkc)));
 }
 int chunk_rows() {
-  static int v = env_int("XC_TC_CHUNK_ROWS", 32);
+  static int v = std::min(kMaxChunkRows, env_int("XC_TC_CHUNK_ROWS", 32));
   return v;
 }
 
@@ -815,6 +904,7 @@ struct TcWs {
   float* CR;        // n_right x (Hr+1) x Wr
   void* hi;         // n_right x Hr x pitch, BF16 or TF32-rounded FP32
   void* lo;
+  int* items;       // the kernel's work list
   size_t bytes;
 };
 
@@ -837,6 +927,7 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * g.Wr));
   w.hi = take((size_t)t.es * plane);
   w.lo = take((size_t)t.es * plane);
+  w.items = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items + 1)));  // list + its length
   w.bytes = off + 256;
   return w;
 }
@@ -946,12 +1037,21 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.kstep = t.kstep;
   prm.flush_rows = flush_rows(t.nkc);
   prm.chunk_rows = chunk_rows();
-  prm.n_chunks = div_up(t.DY - 1 + std::min(g.Hl, g.Hr), prm.chunk_rows);
+  prm.n_chunks = t.n_chunks;
   prm.flags = device_flags();
 
-  const long long blocks =
-      (long long)t.n_halves * prm.n_chunks * prm.n_dytiles * pm.n_left * prm.n_pgroups;
-  if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+  // the work list: non-empty items, most left rows first, built on the device
+  if (t.n_items > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+  prm.items = w.items;
+  prm.n_live = w.items + t.n_items;
+  worklist_kernel<<<1, 1024, 0, stream>>>(prm, t.n_items, w.items, w.items + t.n_items);
+  XC_CUDA_TRY(cudaGetLastError());
+  // persistent: one CTA per SM (211 KB of shared memory and all 512 TMEM
+  // columns each), walking the items round-robin
+  int dev = 0, sms = 0;
+  XC_CUDA_TRY(cudaGetDevice(&dev));
+  XC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const long long blocks = std::max(1LL, std::min<long long>(t.n_items, sms));
   auto kern = tf32 ? tc_kernel<true> : tc_kernel<false>;
   XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
   const int slot = kernel_timer_begin(stream);
