@@ -53,6 +53,21 @@ struct ThreadCache {
   void* d_ws = nullptr;
   size_t left_bytes = 0, right_bytes = 0, out_bytes = 0, ws_bytes = 0;
   int device = -1;
+  // xc_correlate_host pipeline: copy-in and copy-out streams, per-chunk events
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_in[4] = {}, ev_comp[4] = {};
+
+  xc_status ensure_streams() {
+    if (s_in != nullptr) return XC_OK;
+    XC_CUDA_TRY(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
+    XC_CUDA_TRY(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
+    XC_CUDA_TRY(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
+    for (int i = 0; i < 4; ++i) {
+      XC_CUDA_TRY(cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming));
+      XC_CUDA_TRY(cudaEventCreateWithFlags(&ev_comp[i], cudaEventDisableTiming));
+    }
+    return XC_OK;
+  }
 
   void release() {
     plans.clear();
@@ -62,6 +77,16 @@ struct ThreadCache {
     cudaFree(d_ws);
     d_left = d_right = d_out = d_ws = nullptr;
     left_bytes = right_bytes = out_bytes = ws_bytes = 0;
+    if (s_in != nullptr) {
+      cudaStreamDestroy(s_in);
+      cudaStreamDestroy(s_out);
+      cudaEventDestroy(ev_start);
+      for (int i = 0; i < 4; ++i) {
+        cudaEventDestroy(ev_in[i]);
+        cudaEventDestroy(ev_comp[i]);
+      }
+      s_in = s_out = nullptr;
+    }
   }
   ~ThreadCache() {
     // Process teardown may already have destroyed the CUDA context; only the
@@ -323,11 +348,53 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
   uint64_t n_out;
   XC_TRY(xc_output_count(mode, n_left, n_right, &n_out));
   const size_t es = elem_size(dtype);
-  const size_t lb = (size_t)left.x * left.y * n_left * es;
-  const size_t rb = (size_t)right.x * right.y * n_right * es;
-  const size_t ob = (size_t)(left.x + right.x - 1) * (left.y + right.y - 1) * n_out * es;
+  const size_t lsz = (size_t)left.x * left.y * es, rsz = (size_t)right.x * right.y * es;
+  const size_t osz = (size_t)(left.x + right.x - 1) * (left.y + right.y - 1) * es;
+  const size_t lb = lsz * n_left, rb = rsz * n_right, ob = osz * n_out;
+
+  // Pipelining: the problem is cut into chunks along one axis of the pair
+  // map -- the partners (one_to_many, n_to_mn) or the left matrices (n_to_m)
+  // -- each a problem of the same mode.  Chunk i's input copy, correlation
+  // and output copy run on three streams, so copies overlap the correlation
+  // of neighbouring chunks.  A chunk carries about 32 MiB of output or more: each
+  // correlation call has a fixed cost (prep kernels, a partly filled last
+  // wave), which smaller chunks would pay more often than the overlap saves
+  // (64 outputs of 511x511 FP32: two chunks win, four lose).
+  PairMap pm;
+  uint64_t tmp = 0;
+  make_pair_map(mode, n_left, n_right, &pm, &tmp);
+  const bool by_left = mode == XC_N_TO_M;
+  const int axis = mode == XC_ONE_TO_ONE ? 1 : (by_left ? (int)n_left : pm.K);
+  int n_chunks = (int)std::min<size_t>(std::min<size_t>(4, (size_t)axis), (ob + ((size_t)16 << 20)) / ((size_t)32 << 20));
+  if (n_chunks < 1) n_chunks = 1;
+  const int per = (axis + n_chunks - 1) / n_chunks;
+  n_chunks = (axis + per - 1) / per;
+  auto chunk_shape = [&](int i, uint32_t* nl, uint32_t* nr, size_t* l_off, size_t* r_off, size_t* o_off,
+                         size_t* l_len, size_t* r_len, size_t* o_len) {
+    const int a0 = i * per, a1 = std::min(axis, a0 + per), na = a1 - a0;
+    if (n_chunks == 1) {
+      *nl = n_left; *nr = n_right; *l_off = *r_off = *o_off = 0; *l_len = lb; *r_len = rb; *o_len = ob;
+    } else if (by_left) {  // n_to_m: lefts [a0, a1), every right, outputs l*K + k
+      *nl = (uint32_t)na; *nr = n_right;
+      *l_off = lsz * a0; *l_len = lsz * na; *r_off = 0; *r_len = i == 0 ? rb : 0;
+      *o_off = osz * (size_t)a0 * n_right; *o_len = osz * (size_t)na * n_right;
+    } else {  // one_to_many / n_to_mn: partners [a0, a1) of every left
+      const int n = pm.n_left;
+      *nl = n_left; *nr = (uint32_t)(na * n);
+      *l_off = 0; *l_len = i == 0 ? lb : 0;
+      *r_off = rsz * (size_t)a0 * n; *r_len = rsz * (size_t)na * n;
+      *o_off = osz * (size_t)a0 * n; *o_len = osz * (size_t)na * n;
+    }
+  };
   size_t wb = 0;
-  XC_TRY(xc_workspace_size(mode, dtype, method, left, n_left, right, n_right, &wb));
+  for (int i = 0; i < n_chunks; ++i) {
+    uint32_t nl, nr;
+    size_t a, b, c2, d, e, f;
+    chunk_shape(i, &nl, &nr, &a, &b, &c2, &d, &e, &f);
+    size_t w = 0;
+    XC_TRY(xc_workspace_size(mode, dtype, method, left, nl, right, nr, &w));
+    wb = std::max(wb, w);
+  }
   ThreadCache& c = cache();
   auto grow = [](void** p, size_t* have, size_t need) -> xc_status {
     if (need <= *have) return XC_OK;
@@ -342,12 +409,36 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
   XC_TRY(grow(&c.d_right, &c.right_bytes, rb));
   XC_TRY(grow(&c.d_out, &c.out_bytes, ob));
   if (wb > 0) XC_TRY(grow(&c.d_ws, &c.ws_bytes, wb));
+  XC_TRY(c.ensure_streams());
   cudaStream_t s = as_stream(stream);
-  XC_CUDA_TRY(cudaMemcpyAsync(c.d_left, h_left, lb, cudaMemcpyHostToDevice, s));
-  XC_CUDA_TRY(cudaMemcpyAsync(c.d_right, h_right, rb, cudaMemcpyHostToDevice, s));
-  XC_TRY(xc_correlate(mode, dtype, method, c.d_left, left, n_left, c.d_right, right, n_right, c.d_out, c.d_ws,
-                      c.ws_bytes, stream));
-  XC_CUDA_TRY(cudaMemcpyAsync(h_out, c.d_out, ob, cudaMemcpyDeviceToHost, s));
+  // the copy streams start after work already queued on the caller's stream
+  XC_CUDA_TRY(cudaEventRecord(c.ev_start, s));
+  XC_CUDA_TRY(cudaStreamWaitEvent(c.s_in, c.ev_start, 0));
+  XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, c.ev_start, 0));
+  char* dl = static_cast<char*>(c.d_left);
+  char* dr = static_cast<char*>(c.d_right);
+  char* dout = static_cast<char*>(c.d_out);
+  for (int i = 0; i < n_chunks; ++i) {
+    uint32_t nl, nr;
+    size_t l_off, r_off, o_off, l_len, r_len, o_len;
+    chunk_shape(i, &nl, &nr, &l_off, &r_off, &o_off, &l_len, &r_len, &o_len);
+    if (l_len) XC_CUDA_TRY(cudaMemcpyAsync(dl + l_off, static_cast<const char*>(h_left) + l_off, l_len,
+                                           cudaMemcpyHostToDevice, c.s_in));
+    if (r_len) XC_CUDA_TRY(cudaMemcpyAsync(dr + r_off, static_cast<const char*>(h_right) + r_off, r_len,
+                                           cudaMemcpyHostToDevice, c.s_in));
+    XC_CUDA_TRY(cudaEventRecord(c.ev_in[i], c.s_in));
+    XC_CUDA_TRY(cudaStreamWaitEvent(s, c.ev_in[i], 0));
+    // a chunk reads every left (partner chunks) or every right (n_to_m):
+    // those were copied with chunk 0, which this stream has already waited for
+    const char* cl = by_left ? dl + l_off : dl;
+    const char* cr = by_left ? dr : dr + r_off;
+    XC_TRY(xc_correlate(mode, dtype, method, cl, left, nl, cr, right, nr, dout + o_off, c.d_ws, c.ws_bytes, stream));
+    XC_CUDA_TRY(cudaEventRecord(c.ev_comp[i], s));
+    XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, c.ev_comp[i], 0));
+    XC_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(h_out) + o_off, dout + o_off, o_len, cudaMemcpyDeviceToHost,
+                                c.s_out));
+  }
+  XC_CUDA_TRY(cudaStreamSynchronize(c.s_out));
   XC_CUDA_TRY(cudaStreamSynchronize(s));
   return check_device_flags(s);
 }
