@@ -129,7 +129,12 @@ xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const voi
  * device->host copy and free, i.e. the reference's whole
  * prepare/transfer/run/finalize/free sequence (src/main.cpp:123-174).
  * Synchronises `stream` before returning. Device buffers are cached per
- * thread between calls of the same size. */
+ * thread between calls of the same size.  Problems with about 48 MiB of
+ * output or more run in up to four chunks of partners (left matrices in
+ * n_to_m), each chunk's copy-in, correlation and copy-out on its own stream
+ * so that copies overlap the neighbouring chunks' correlations; with
+ * XC_METHOD_AUTO each chunk picks its own method. Host buffers should be
+ * pinned for the copies to overlap. */
 xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
                             uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
                             void* stream);
