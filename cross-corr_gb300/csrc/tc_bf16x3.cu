@@ -25,10 +25,12 @@
 // shift axis lies along M, so K-steps whose 128 shifts see only zeros are
 // skipped (a quarter of them at Wl = Wr).
 //
-// Each CTA owns two shift tiles (256 shifts) of one (partner group, row-shift
-// group, chunk of left rows); a second CTA owns the other two when
-// Sx > 256.  Tensor memory holds the two FP32 accumulator tiles (256
-// columns) and a two-slot ring of split Toeplitz operands (256 columns).
+// A work item is two shift tiles (256 shifts) of one (partner group,
+// row-shift group, chunk of left rows); a second item covers the other two
+// when Sx > 256.  The kernel is persistent (one CTA per SM) and walks a
+// device-built list of the items.  Tensor memory holds the two FP32
+// accumulator tiles (256 columns) and a two-slot ring of split Toeplitz
+// operands (256 columns).
 // Every `flush_rows` left rows the epilogue warps drain the accumulators into
 // FP32 registers; at the end they add them to the output with coalesced
 // red.global.add (consecutive lanes are consecutive shifts).
@@ -47,11 +49,17 @@
 // then added to.  The drains bound every accumulator's chain at
 // 192 MMAs.
 //
-// Warp roles (704 threads, one CTA per SM):
+// Warp roles (736 threads, one CTA per SM):
 //   warp 0      TMA producer of the right-row tiles (hi and lo planes)
-//   warp 1      TMEM allocation and the single-thread MMA issuer
+//   warp 1      TMEM allocation; one thread issues the MMAs of shift tile 0
+//   warp 22     one thread issues the MMAs of shift tile 1
 //   warps 2-5   Toeplitz builders (one per TMEM lane quadrant)
 //   warps 6-21  epilogue: 4 per lane quadrant, 64 accumulator columns each
+// Two issuers: a single thread cannot issue a 128x128x16 MMA every 64
+// cycles once it also waits on barriers and walks the loop (measured: ~85
+// cycles per MMA from one thread against 64 for the pipe alone); the two
+// tiles' accumulators are independent, so each issuer feeds one of them and
+// the tensor pipe interleaves their instructions.
 // All waits are bounded: an expired wait records a flag, the CTA winds down,
 // waits (bounded) for its own copies and MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
@@ -74,10 +82,11 @@ constexpr int kTileBytes = 128 * 128;  // 128 rows x 64 bf16 (one plane)
 constexpr int kStageBytes = 2 * kTileBytes;
 constexpr int kBuilderWarps = 4;       // one per TMEM lane quadrant
 constexpr int kEpiWarps = 16;          // four per TMEM lane quadrant
-constexpr int kThreads = 32 * (2 + kBuilderWarps + kEpiWarps);
+// warp 0 producer, warps 1 and 22 MMA issuers, 2-5 builders, 6-21 epilogue
+constexpr int kThreads = 32 * (3 + kBuilderWarps + kEpiWarps);
 constexpr int kMaxLp = 512 + 256;      // staged left row pairs: 128 * tiles + 64 * chunks
 constexpr uint32_t kRingCol = 256;     // first TMEM column of the Toeplitz ring
-constexpr int kBarBytes = 256;         // 15 mbarriers, the abort flag, the TMEM address slot
+constexpr int kBarBytes = 256;         // 20 mbarriers, the abort flag, the TMEM address slot
 constexpr int kMaxChunkRows = 1024;    // left rows per work item at most
 
 struct TcParams {
@@ -127,8 +136,7 @@ __device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, ui
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 // Round to TF32 (10 explicit mantissa bits), nearest with ties away.
@@ -138,15 +146,16 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float(r);
 }
 
-// D[tmem] (+)= A[tmem] * B[smem]^T.
+// D[tmem] (+)= A[tmem] * B[smem]^T.  No memory clobber: the MMA reads
+// shared and tensor memory asynchronously, and volatile keeps it in order with
+// the barrier waits and commits around it.
 __device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
                                             uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
+      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ uint64_t make_desc(uint32_t lo, uint32_t hi) {
@@ -314,7 +323,7 @@ __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.
 
 __device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
 
-// 22 warps: at most 6 on one SM sub-partition, whose 16K registers cap a
+// 23 warps: at most 6 on one SM sub-partition, whose 16K registers cap a
 // thread at 80.  TF: TF32 operands (K = 8 per MMA) instead of BF16 (K = 16).
 template <bool TF>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -335,9 +344,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* s_empty = s_full + 2;         // [2] ring slot consumed
   uint64_t* t_full = s_empty + 2;         // accumulators ready to drain
   uint64_t* t_empty = t_full + 1;         // accumulators drained
-  uint64_t* mma_done = t_empty + 1;
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 1);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 2);
+  uint64_t* mma_done = t_empty + 1;     // [2] one per issuer
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 2);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 3);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   // Persistent: the work list is sorted by left rows (heaviest first) and
@@ -348,17 +357,19 @@ __global__ void __launch_bounds__(kThreads, 1)
   const long long n_items = *p.n_live;
 
   if (threadIdx.x == 0) {
+    // consumed / accumulated barriers take one commit from each issuer
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&a_full[s], 1);
-      mbar_init(&a_empty[s], 1);
+      mbar_init(&a_empty[s], 2);
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&s_full[s], kBuilderWarps);
-      mbar_init(&s_empty[s], 1);
+      mbar_init(&s_empty[s], 2);
     }
-    mbar_init(t_full, 1);
+    mbar_init(t_full, 2);
     mbar_init(t_empty, kEpiWarps);
-    mbar_init(mma_done, 1);
+    mbar_init(&mma_done[0], 1);
+    mbar_init(&mma_done[1], 1);
     *abort_flag = 0;
     fence_mbar_init();
     prefetch_tensormap(&map_hi);
@@ -417,77 +428,90 @@ __global__ void __launch_bounds__(kThreads, 1)
           mbar_wait_bounded(&a_full[q % kStages], (q / kStages) & 1, 1u << 16);
       }
     }
-  } else if (warp == 1) {
-    // ------------------------------------------------------------ MMA issuer
+  } else if (warp == 1 || warp == 2 + kBuilderWarps + kEpiWarps) {
+    // ------------------------------------------------------------ MMA issuers
+    // Both walk the same items, rows and K-chunks and wait on the same
+    // barriers; each issues the MMAs of its own shift tile and commits to
+    // the shared consumed / accumulated barriers.
+    const int my_tt = warp == 1 ? 0 : 1;
     if (lane == 0) {
+      // The issue loop is on the critical path (a 128x128x16 MMA takes 64
+      // cycles of tensor pipe): every per-item value lives in a scalar, the
+      // stage / slot counters advance without divisions.
       constexpr uint32_t kDescHi = (1024u >> 4) | (1u << 14) | (2u << 29);  // SBO 1024 B, 128-byte swizzle
       const uint32_t idesc = TF ? idesc_tf32_f32(128, 128) : idesc_bf16_f32(128, 128);
       const uint32_t b_lo_word = ((smem_u32(b_tiles) >> 4) & 0x3FFFu) | (1u << 16);
-      int it = 0, windows = 0;
+      const uint32_t d_tmem = tmem_base + (uint32_t)my_tt * 128;
+      const uint32_t a_base = tmem_base + kRingCol + (uint32_t)my_tt * 64;  // this tile's 4 K-steps of a slot
+      int s = 0, slot = 0;                    // stage and ring slot of the next K-chunk
+      uint32_t s_phase = 0, r_phase = 0, t_phase = 1;  // parities awaited on a_full, s_full, t_empty
       bool ok = true;
       for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
         const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
         if (pos >= n_items) continue;
         TcItem w;
         if (!tc_item(p, p.items[pos], &w)) continue;
-        const int first0 = w.mask0 ? __ffs(w.mask0) - 1 : -1;
-        const int first1 = w.mask1 ? __ffs(w.mask1) - 1 : -1;
+        const uint32_t my_mask = my_tt == 0 ? w.mask0 : w.mask1;
+        const int first = my_mask ? __ffs(my_mask) - 1 : -1;
+        const int n_rows = w.n_rows;
         int rows_in = 0;
-        for (int ai = 0; ai < w.n_rows && ok; ++ai) {
+        for (int ai = 0; ai < n_rows && ok; ++ai) {
           if (rows_in == 0) {
             // the epilogue must have drained the previous window
-            if (!wait_or_abort(t_empty, (windows & 1) ^ 1, abort_flag, p.flags, 14)) {
+            if (!wait_or_abort(t_empty, t_phase, abort_flag, p.flags, 14)) {
               ok = false;
               break;
             }
+            t_phase ^= 1u;
           }
-          for (int kc = 0; kc < p.nkc; ++kc, ++it) {
-            const int s = it % kStages, slot = it & 1;
-            if (!wait_or_abort(&a_full[s], (it / kStages) & 1, abort_flag, p.flags, 13) ||
-                !wait_or_abort(&s_full[slot], (it >> 1) & 1, abort_flag, p.flags, 12)) {
+          for (int kc = 0; kc < p.nkc; ++kc) {
+            if (!wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13) ||
+                !wait_or_abort(&s_full[slot], r_phase, abort_flag, p.flags, 12)) {
               ok = false;
               break;
             }
             tc_fence_after();
+            const uint32_t pat = (my_mask >> (4 * kc)) & 0xFu;
+            const int rk = (rows_in == 0 && (first >> 2) == kc) ? (first & 3) : -1;  // K-step that resets
             const uint32_t bw = b_lo_word + (uint32_t)s * (kStageBytes >> 4);
-            const uint32_t ring = tmem_base + kRingCol + (uint32_t)slot * 128;
+            const uint32_t ra = a_base + (uint32_t)slot * 128;
 #pragma unroll
             for (int ks = 0; ks < 4; ++ks) {
-              const int j = kc * 4 + ks;
+              if (!(pat & (1u << ks))) continue;
               const uint64_t bhi = make_desc(bw + ks * 2, kDescHi);
               const uint64_t blo = make_desc(bw + (kTileBytes >> 4) + ks * 2, kDescHi);
-#pragma unroll
-              for (int tt = 0; tt < 2; ++tt) {
-                if (!(((tt == 0 ? w.mask0 : w.mask1) >> j) & 1u)) continue;
-                const bool reset = rows_in == 0 && j == (tt == 0 ? first0 : first1);
-                const uint32_t ahi = ring + (uint32_t)(tt * 4 + ks) * 16, alo = ahi + 8;
-                const uint32_t d = tmem_base + (uint32_t)tt * 128;
-                if constexpr (TF) {
-                  mma_tf32_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
-                  mma_tf32_ts(d, ahi, blo, idesc, 1u);
-                  mma_tf32_ts(d, alo, bhi, idesc, 1u);
-                } else {
-                  mma_bf16_ts(d, ahi, bhi, idesc, reset ? 0u : 1u);
-                  mma_bf16_ts(d, ahi, blo, idesc, 1u);
-                  mma_bf16_ts(d, alo, bhi, idesc, 1u);
-                }
+              const uint32_t ahi = ra + (uint32_t)ks * 16, alo = ahi + 8;
+              const uint32_t acc0 = ks == rk ? 0u : 1u;
+              if constexpr (TF) {
+                mma_tf32_ts(d_tmem, ahi, bhi, idesc, acc0);
+                mma_tf32_ts(d_tmem, ahi, blo, idesc, 1u);
+                mma_tf32_ts(d_tmem, alo, bhi, idesc, 1u);
+              } else {
+                mma_bf16_ts(d_tmem, ahi, bhi, idesc, acc0);
+                mma_bf16_ts(d_tmem, ahi, blo, idesc, 1u);
+                mma_bf16_ts(d_tmem, alo, bhi, idesc, 1u);
               }
             }
             mma_commit(&a_empty[s]);
             mma_commit(&s_empty[slot]);
+            if (++s == kStages) {
+              s = 0;
+              s_phase ^= 1u;
+            }
+            slot ^= 1;
+            if (slot == 0) r_phase ^= 1u;
           }
           if (!ok) break;
           ++rows_in;
-          if (rows_in == p.flush_rows || ai == w.n_rows - 1) {
+          if (rows_in == p.flush_rows || ai == n_rows - 1) {
             mma_commit(t_full);
-            ++windows;
             rows_in = 0;
           }
         }
       }
       // All MMAs issued by this thread must finish before TMEM is released.
-      mma_commit(mma_done);
-      mbar_wait_bounded(mma_done, 0, 1u << 22);
+      mma_commit(&mma_done[my_tt]);
+      mbar_wait_bounded(&mma_done[my_tt], 0, 1u << 22);
     }
   } else if (warp < 2 + kBuilderWarps) {
     // ------------------------------------------------------------ Toeplitz builders
@@ -566,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // a failed wait reaches the other builders at the next row's barrier
       }
     }
-  } else {
+  } else if (warp < 2 + kBuilderWarps + kEpiWarps) {
     // ------------------------------------------------------------ epilogue
     // Warp w (index ew = w - 6): lane quadrant q = w % 4, accumulator
     // columns [64 * (ew / 4), +64): tile tt = ew / 8, B rows nb.. of it.
