@@ -11,55 +11,67 @@
 // Formulation (implicit GEMM).  For a left row a and a right row b the
 // contribution to output row sy = a - b + Hr - 1 is a 1D correlation, a
 // Toeplitz matrix-vector product.  One tcgen05.mma computes
-//     D[m][n] += sum_k A[m][k] * B[n][k]        (M=128, N=128, K=16, BF16)
+//     D[m][n] += sum_k A[m][k] * B[n][k]        (M=128, N=256, K=16, BF16)
 // with
 //   m -> column shift sx = s0 + m of a 128-shift tile:
 //        A[m][k] = Lp_a[s0 + m + k0 + k], Lp_a[j] = L[a][j - (Wr-1)] (zero
-//        outside the row).  A is a Toeplitz matrix; builder warps write it
-//        straight into tensor memory (tcgen05.st), one lane per shift, from
-//        a staged copy of the left row.
+//        outside the row).
 //   n -> (partner matrix p, row shift dy): B[n][k] = R_p[a - dy][k0 + k]
 //        (right rows, staged by TMA with 128-byte swizzle, K-major).
-// N = 128 keeps each MMA at the tensor pipe's full rate (narrower MMAs are
-// bound by a per-instruction cost of ~44 cycles on GB300, measured), and the
-// shift axis lies along M, so K-steps whose 128 shifts see only zeros are
-// skipped (a quarter of them at Wl = Wr).
+//
+// The Toeplitz operand A is read from shared memory through an ordinary
+// matrix descriptor.  In the K-major layout without swizzle an 8-row x
+// 16-byte core matrix (r, t) sits at start + 16 r + e t (e = element bytes)
+// and core matrices are LBO apart along K and SBO apart along M.  Element
+// (m, k) lands at 128 (m/8 + k/8) + 16 (m%8) + 2 (k%8) for BF16 with
+// LBO = SBO = 128 bytes, and its value Lp[c + m + k] depends only on
+// 8 (m/8 + k/8) + m%8 + k%8, so one buffer T[q][r][t] = X[8 q + r + t] of
+// 8-element core matrices serves every shift tile and K-step as an offset of
+// the start address: builder warps write T once per left row (16 KB for the
+// hi and lo parts) instead of a Toeplitz matrix per K-step.  TF32 (4-element
+// core-matrix rows): T[q][r][t] = X[4 q + r + t], LBO = 128, SBO = 256.
+// N = 256: a 128x256x16 MMA reads 4 KB of A and 8 KB of B in 128 cycles,
+// 96 bytes per clock of the 128 shared memory delivers; at N = 128 the same
+// operands would need all of it.  Measured on GB300, this operand form runs
+// at 4095 MAC/clk/SM (the tensor pipe's peak).  The shift axis lies along M,
+// so K-steps whose 128 shifts see only zeros are skipped (a quarter of them
+// at Wl = Wr).
 //
 // A work item is two shift tiles (256 shifts) of one (partner group,
 // row-shift group, chunk of left rows); a second item covers the other two
 // when Sx > 256.  The kernel is persistent (one CTA per SM) and walks a
-// device-built list of the items.  Tensor memory holds the two FP32
-// accumulator tiles (256 columns) and a two-slot ring of split Toeplitz
-// operands (256 columns).
-// Every `flush_rows` left rows the epilogue warps drain the accumulators into
-// FP32 registers; at the end they add them to the output with coalesced
+// device-built list of the items.  Tensor memory holds the two 128x256 FP32
+// accumulators (all 512 columns).  Every few left rows (the window, chosen
+// per left matrix and partner group from the data's statistics) the epilogue
+// warps read the accumulators and add them to the output with coalesced
 // red.global.add (consecutive lanes are consecutive shifts).
+//
+// Right tiles come in stages of one plane (hi or lo) of one 128-byte column
+// chunk (256 rows x 128 bytes).  Per chunk the MMAs that read the hi plane
+// (A_hi B_hi and A_lo B_hi) run first, then those that read the lo plane
+// (A_hi B_lo), so each stage is released as soon as its own MMAs finish.
 //
 // Accuracy.  Tensor-core FP32 accumulation drops low bits on every MMA with a
 // consistent sign, so the error of a long chain grows linearly with its
-// length and with the magnitude of the partial sums (measured on GB300:
-// ~1.2e-6 of max|out| per 48-MMA left row for uniform [0,1) data).  Each
-// matrix is therefore shifted by its mean before the split
-// (L' = L - mu_L, R' = R - mu_R): the tensor cores correlate the centred data,
-// whose partial sums are small random walks, and the exact remainder
+// length and with the magnitude of the partial sums.  Each matrix is
+// therefore shifted by its mean before the split (L' = L - mu_L,
+// R' = R - mu_R): the tensor cores correlate the centred data, whose partial
+// sums are small random walks, and the exact remainder
 //   out = corr(L', R') + mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area
 // (S = sum of the centred matrix over the overlap of a shift, from column
 // prefix sums of the centred matrices, scanned along the row per output row)
 // is written first by a correction kernel, which the tensor-core results are
-// then added to.  The drains bound every accumulator's chain at
-// 192 MMAs.
+// then added to.
 //
-// Warp roles (736 threads, one CTA per SM):
-//   warp 0      TMA producer of the right-row tiles (hi and lo planes)
+// Warp roles (704 threads, one CTA per SM):
+//   warp 0      TMA producer of the right-row tiles
 //   warp 1      TMEM allocation; one thread issues the MMAs of shift tile 0
 //   warp 22     one thread issues the MMAs of shift tile 1
-//   warps 2-5   Toeplitz builders (one per TMEM lane quadrant)
-//   warps 6-21  epilogue: 4 per lane quadrant, 64 accumulator columns each
-// Two issuers: a single thread cannot issue a 128x128x16 MMA every 64
-// cycles once it also waits on barriers and walks the loop (measured: ~85
-// cycles per MMA from one thread against 64 for the pipe alone); the two
-// tiles' accumulators are independent, so each issuer feeds one of them and
-// the tensor pipe interleaves their instructions.
+//   warps 2-5   builders of the Toeplitz core-matrix buffer (two row buffers)
+//   warps 6-21  epilogue: 4 per TMEM lane quadrant, 128 accumulator columns each
+// Each tile's accumulator is drained on its own schedule, the two offset by
+// half a window: while the epilogue drains one tile, the other tile's issuer
+// keeps the tensor pipe busy (as far as the shared right-tile stages allow).
 // All waits are bounded: an expired wait records a flag, the CTA winds down,
 // waits (bounded) for its own copies and MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
@@ -77,17 +89,27 @@ namespace xc {
 
 namespace {
 
-constexpr int kStages = 6;             // right-row tile pipeline depth
-constexpr int kTileBytes = 128 * 128;  // 128 rows x 64 bf16 (one plane)
-constexpr int kStageBytes = 2 * kTileBytes;
-constexpr int kBuilderWarps = 4;       // one per TMEM lane quadrant
-constexpr int kEpiWarps = 16;          // four per TMEM lane quadrant
+constexpr int kN = 256;                 // B rows per MMA: P partners x DY row shifts
+constexpr int kStageBytes = kN * 128;   // one plane of one 128-byte column chunk
+constexpr int kBuilderWarps = 4;
+constexpr int kEpiWarps = 16;           // four per TMEM lane quadrant
 // warp 0 producer, warps 1 and 22 MMA issuers, 2-5 builders, 6-21 epilogue
 constexpr int kThreads = 32 * (3 + kBuilderWarps + kEpiWarps);
-constexpr int kMaxLp = 512 + 256;      // staged left row pairs: 128 * tiles + 64 * chunks
-constexpr uint32_t kRingCol = 256;     // first TMEM column of the Toeplitz ring
-constexpr int kBarBytes = 256;         // 20 mbarriers, the abort flag, the TMEM address slot
-constexpr int kMaxChunkRows = 1024;    // left rows per work item at most
+constexpr int kXLen = 520;              // staged row elements: the 511 a two-tile item reads, padded
+constexpr int kBarBytes = 256;          // 20 mbarriers at most, the abort flag, the TMEM address slot
+constexpr int kMaxChunkRows = 1024;     // left rows per work item at most
+
+// Per operand type: right-tile stages and the Toeplitz buffer (hi or lo part
+// of one left row): 64 core matrices of 8 BF16 or 128 of 4 FP32.
+template <bool TF>
+struct TcCfg {
+  static constexpr int kStages = TF ? 4 : 5;
+  static constexpr int kCm = TF ? 4 : 8;            // elements per 16-byte core-matrix row
+  static constexpr int kQ = TF ? 128 : 64;          // core matrices in T
+  static constexpr int kTBytes = kQ * 128;          // one plane of T
+  static constexpr int kEs = TF ? 4 : 2;            // element bytes
+  static constexpr int kSmem = 1024 + kStages * kStageBytes + 4 * kTBytes + 4 * kXLen * 4 + kBarBytes;
+};
 
 struct TcParams {
   const float* left;
@@ -95,15 +117,14 @@ struct TcParams {
   float* out;
   int Hl, Wl, Hr, Wr, Sy, Sx;
   PairMap pm;
-  int P, DY;        // partners x row shifts per B tile, P*DY = 128
+  int P, DY;        // partners x row shifts per B tile, P*DY = 256
   int mats_mode;    // 1: one TMA box per row shift spans P partners; 0: one box per partner spans DY rows
   int n_pgroups;    // ceil(K / P)
   int n_dytiles;    // ceil(Sy / DY)
-  int n_halves;     // CTAs per work item (two 128-shift tiles each)
+  int n_halves;     // work items across the shifts (two 128-shift tiles each)
   int nkc;          // 128-byte column chunks of a right row (64 BF16 or 32 TF32 columns)
   int kstep;        // columns per K-step: 16 (BF16) or 8 (TF32)
-  int lp_len;       // staged left row length
-  int flush_rows;   // drain TMEM every this many left rows
+  const int* flush_tab;  // drain TMEM every this many left rows, per (left matrix, partner group)
   int chunk_rows;   // left rows per work item (a longer row range is split over items)
   const int* items;  // non-empty work items, most left rows first (index encoding of tc_item)
   const int* n_live; // entries of `items` (written on the device)
@@ -129,16 +150,6 @@ __host__ __device__ constexpr uint32_t idesc_tf32_f32(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// D[tmem] (+)= A[tmem] * B[smem]^T, TF32 operands (K = 8 per instruction).
-__device__ __forceinline__ void mma_tf32_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
-                                            uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-
 // Round to TF32 (10 explicit mantissa bits), nearest with ties away.
 __device__ __forceinline__ float tf32_round(float x) {
   uint32_t r;
@@ -146,16 +157,24 @@ __device__ __forceinline__ float tf32_round(float x) {
   return __uint_as_float(r);
 }
 
-// D[tmem] (+)= A[tmem] * B[smem]^T.  No memory clobber: the MMA reads
-// shared and tensor memory asynchronously, and volatile keeps it in order with
-// the barrier waits and commits around it.
-__device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
-                                            uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(accumulate));
+// D[tmem] (+)= A[smem] * B[smem]^T, both operands through descriptors.  No
+// memory clobber: the MMA reads shared memory asynchronously, and volatile
+// keeps it in order with the barrier waits and commits around it.
+template <bool TF>
+__device__ __forceinline__ void mma_ss(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  if constexpr (TF)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ uint64_t make_desc(uint32_t lo, uint32_t hi) {
@@ -177,6 +196,21 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
                : "r"(taddr));
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 32 consecutive columns of this warp's 32 lanes: one register each.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
@@ -310,18 +344,20 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   }
 }
 
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* r) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15, %16};" ::"r"(taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-      "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-      : "memory");
+// Accumulator windows of an item: tile 0 drains after every `flush` left
+// rows, tile 1 first after (flush + 1) / 2 rows and then every `flush`; both
+// drain after the item's last row.  True when row ai (0-based) ends a window.
+__device__ __forceinline__ bool window_end(int tt, int ai, int n_rows, int flush) {
+  if (ai == n_rows - 1) return true;
+  const int off = tt == 0 ? 0 : flush - (flush + 1) / 2;
+  return (ai + 1 + off) % flush == 0;
 }
 
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
-__device__ __forceinline__ uint32_t bf16x2_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
+__device__ __forceinline__ int window_count(int tt, int n_rows, int flush) {
+  int n = 0;
+  for (int ai = 0; ai < n_rows; ++ai) n += window_end(tt, ai, n_rows, flush) ? 1 : 0;
+  return n;
+}
 
 // 23 warps: at most 6 on one SM sub-partition, whose 16K registers cap a
 // thread at 80.  TF: TF32 operands (K = 8 per MMA) instead of BF16 (K = 16).
@@ -329,22 +365,21 @@ template <bool TF>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
               const TcParams p) {
-  constexpr int kCols = 64;  // accumulator columns per epilogue warp
+  using C = TcCfg<TF>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* b_tiles = smem;                                                  // kStages x (hi, lo) x 16 KB
-  // split left row as overlapping BF16 pairs, two rows: pairs[row][hi/lo][j] = (x_j, x_j+1)
-  uint32_t* pairs = reinterpret_cast<uint32_t*>(smem + kStages * kStageBytes);    // 2 x 2 x kMaxLp
-  long long* row_base = reinterpret_cast<long long*>(pairs + 4 * kMaxLp);         // 2 x 128 output row offsets
-  uint64_t* bars = reinterpret_cast<uint64_t*>(row_base + 256);
-  uint64_t* a_full = bars;              // [kStages] right-row tiles landed
-  uint64_t* a_empty = bars + kStages;   // [kStages] tiles consumed
-  uint64_t* s_full = bars + 2 * kStages;  // [2] Toeplitz ring slot written
-  uint64_t* s_empty = s_full + 2;         // [2] ring slot consumed
-  uint64_t* t_full = s_empty + 2;         // accumulators ready to drain
-  uint64_t* t_empty = t_full + 1;         // accumulators drained
-  uint64_t* mma_done = t_empty + 1;     // [2] one per issuer
+  unsigned char* b_tiles = smem;                                       // kStages x (256 rows x 128 B)
+  unsigned char* t_buf = b_tiles + C::kStages * kStageBytes;           // [row buffer][hi, lo] Toeplitz core matrices
+  float* xs = reinterpret_cast<float*>(t_buf + 4 * C::kTBytes);        // [row buffer][hi, lo] x kXLen staged row
+  uint64_t* bars = reinterpret_cast<uint64_t*>(xs + 4 * kXLen);
+  uint64_t* a_full = bars;                   // [kStages] right-row tile landed
+  uint64_t* a_empty = bars + C::kStages;     // [kStages] tile consumed
+  uint64_t* r_full = bars + 2 * C::kStages;  // [2] Toeplitz row buffer written
+  uint64_t* r_empty = r_full + 2;            // [2] row buffer consumed
+  uint64_t* t_full = r_empty + 2;            // [2] a tile's accumulator ready to drain
+  uint64_t* t_empty = t_full + 2;            // [2] a tile's accumulator drained
+  uint64_t* mma_done = t_empty + 2;          // [2] one per issuer
   volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 2);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 3);
 
@@ -357,19 +392,18 @@ __global__ void __launch_bounds__(kThreads, 1)
   const long long n_items = *p.n_live;
 
   if (threadIdx.x == 0) {
-    // consumed / accumulated barriers take one commit from each issuer
-    for (int s = 0; s < kStages; ++s) {
+    // consumed barriers take one commit from each issuer
+    for (int s = 0; s < C::kStages; ++s) {
       mbar_init(&a_full[s], 1);
       mbar_init(&a_empty[s], 2);
     }
     for (int s = 0; s < 2; ++s) {
-      mbar_init(&s_full[s], kBuilderWarps);
-      mbar_init(&s_empty[s], 2);
+      mbar_init(&r_full[s], kBuilderWarps);
+      mbar_init(&r_empty[s], 2);
+      mbar_init(&t_full[s], 1);
+      mbar_init(&t_empty[s], kEpiWarps / 2);
+      mbar_init(&mma_done[s], 1);
     }
-    mbar_init(t_full, 2);
-    mbar_init(t_empty, kEpiWarps);
-    mbar_init(&mma_done[0], 1);
-    mbar_init(&mma_done[1], 1);
     *abort_flag = 0;
     fence_mbar_init();
     prefetch_tensormap(&map_hi);
@@ -388,6 +422,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (warp == 0) {
     // ------------------------------------------------------------ producer
+    // per (row, column chunk): the hi plane, then the lo plane
     if (lane == 0) {
       int it = 0;
       bool ok = true;
@@ -398,113 +433,118 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!tc_item(p, p.items[pos], &w)) continue;
         for (int ai = 0; ai < w.n_rows && ok; ++ai) {
           const int a = w.a_lo + ai;
-          for (int kc = 0; kc < p.nkc && ok; ++kc, ++it) {
-            const int s = it % kStages;
-            if (!wait_or_abort_sleep(&a_empty[s], ((it / kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
-              ok = false;
-              break;
-            }
-            mbar_arrive_expect_tx(&a_full[s], kStageBytes);
-            unsigned char* hi = b_tiles + s * kStageBytes;
-            unsigned char* lo = hi + kTileBytes;
-            if (p.mats_mode) {
-              for (int d = 0; d < p.DY; ++d) {
-                const int b = a - (w.dy0 + d);
-                tma_load_4d(hi + d * p.P * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b, w.rdim2, w.p0);
-                tma_load_4d(lo + d * p.P * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b, w.rdim2, w.p0);
+          for (int kc = 0; kc < p.nkc && ok; ++kc) {
+            for (int pl = 0; pl < 2; ++pl, ++it) {
+              const int s = it % C::kStages;
+              if (!wait_or_abort_sleep(&a_empty[s], ((it / C::kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
+                ok = false;
+                break;
               }
-            } else {
-              const int b0 = a - w.dy0 - (p.DY - 1);
-              for (int q = 0; q < p.P; ++q) {
-                tma_load_4d(hi + q * p.DY * 128, &map_hi, &a_full[s], kc * 4 * p.kstep, b0, w.rdim2, w.p0 + q);
-                tma_load_4d(lo + q * p.DY * 128, &map_lo, &a_full[s], kc * 4 * p.kstep, b0, w.rdim2, w.p0 + q);
+              mbar_arrive_expect_tx(&a_full[s], kStageBytes);
+              unsigned char* dst = b_tiles + s * kStageBytes;
+              const CUtensorMap* map = pl == 0 ? &map_hi : &map_lo;
+              const int x = kc * 4 * p.kstep;  // first column of the chunk
+              if (p.mats_mode) {
+                for (int d = 0; d < p.DY; ++d)
+                  tma_load_4d(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0);
+              } else {
+                const int b0 = a - w.dy0 - (p.DY - 1);
+                for (int q = 0; q < p.P; ++q)
+                  tma_load_4d(dst + q * p.DY * 128, map, &a_full[s], x, b0, w.rdim2, w.p0 + q);
               }
             }
           }
         }
       }
       if (!ok) {
-        for (int q = max(0, it - kStages); q < it; ++q)
-          mbar_wait_bounded(&a_full[q % kStages], (q / kStages) & 1, 1u << 16);
+        for (int q = max(0, it - C::kStages); q < it; ++q)
+          mbar_wait_bounded(&a_full[q % C::kStages], (q / C::kStages) & 1, 1u << 16);
       }
     }
   } else if (warp == 1 || warp == 2 + kBuilderWarps + kEpiWarps) {
     // ------------------------------------------------------------ MMA issuers
-    // Both walk the same items, rows and K-chunks and wait on the same
-    // barriers; each issues the MMAs of its own shift tile and commits to
-    // the shared consumed / accumulated barriers.
+    // Both walk the same items, rows and stages; each issues its own tile's
+    // MMAs and commits to the shared consumed barriers.
     const int my_tt = warp == 1 ? 0 : 1;
     if (lane == 0) {
-      // The issue loop is on the critical path (a 128x128x16 MMA takes 64
-      // cycles of tensor pipe): every per-item value lives in a scalar, the
-      // stage / slot counters advance without divisions.
-      constexpr uint32_t kDescHi = (1024u >> 4) | (1u << 14) | (2u << 29);  // SBO 1024 B, 128-byte swizzle
-      const uint32_t idesc = TF ? idesc_tf32_f32(128, 128) : idesc_bf16_f32(128, 128);
-      const uint32_t b_lo_word = ((smem_u32(b_tiles) >> 4) & 0x3FFFu) | (1u << 16);
-      const uint32_t d_tmem = tmem_base + (uint32_t)my_tt * 128;
-      const uint32_t a_base = tmem_base + kRingCol + (uint32_t)my_tt * 64;  // this tile's 4 K-steps of a slot
-      int s = 0, slot = 0;                    // stage and ring slot of the next K-chunk
-      uint32_t s_phase = 0, r_phase = 0, t_phase = 1;  // parities awaited on a_full, s_full, t_empty
+      // B: SBO 1024 B (8 rows x 128 B), 128-byte swizzle.  A (Toeplitz
+      // buffer): no swizzle, LBO 128 B along K, SBO 128 B (BF16) or 256 B
+      // (TF32) along M.
+      constexpr uint32_t kBHi = (1024u >> 4) | (1u << 14) | (2u << 29);
+      constexpr uint32_t kAHi = ((TF ? 256u : 128u) >> 4) | (1u << 14);
+      const uint32_t idesc = TF ? idesc_tf32_f32(128, kN) : idesc_bf16_f32(128, kN);
+      const uint32_t b_word = ((smem_u32(b_tiles) >> 4) & 0x3FFFu) | (1u << 16);
+      const uint32_t t_word = ((smem_u32(t_buf) >> 4) & 0x3FFFu) | ((128u >> 4) << 16);
+      constexpr uint32_t kTileQ = 128 / C::kCm;   // core matrices between the two shift tiles
+      int s = 0, rb = 0;                      // stage, Toeplitz row buffer
+      uint32_t s_phase = 0, r_phase = 0, t_phase = 1;
       bool ok = true;
       for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
         const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
         if (pos >= n_items) continue;
         TcItem w;
         if (!tc_item(p, p.items[pos], &w)) continue;
-        const uint32_t my_mask = my_tt == 0 ? w.mask0 : w.mask1;
-        const int first = my_mask ? __ffs(my_mask) - 1 : -1;
+        const uint32_t mm = my_tt == 0 ? w.mask0 : w.mask1;
+        const int first = mm ? __ffs(mm) - 1 : -1;
         const int n_rows = w.n_rows;
+        const int flush = p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P];
+        const uint32_t d = tmem_base + (uint32_t)my_tt * kN;
+        const uint32_t tq = (uint32_t)my_tt * kTileQ;
         int rows_in = 0;
         for (int ai = 0; ai < n_rows && ok; ++ai) {
           if (rows_in == 0) {
-            // the epilogue must have drained the previous window
-            if (!wait_or_abort(t_empty, t_phase, abort_flag, p.flags, 14)) {
+            // the epilogue must have drained this tile's previous window
+            if (!wait_or_abort(&t_empty[my_tt], t_phase, abort_flag, p.flags, 14)) {
               ok = false;
               break;
             }
             t_phase ^= 1u;
           }
-          for (int kc = 0; kc < p.nkc; ++kc) {
-            if (!wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13) ||
-                !wait_or_abort(&s_full[slot], r_phase, abort_flag, p.flags, 12)) {
-              ok = false;
-              break;
-            }
-            tc_fence_after();
-            const uint32_t pat = (my_mask >> (4 * kc)) & 0xFu;
+          if (!wait_or_abort(&r_full[rb], r_phase, abort_flag, p.flags, 12)) {
+            ok = false;
+            break;
+          }
+          // this row's Toeplitz buffers (hi, lo), 16-byte units
+          const uint32_t th = t_word + (uint32_t)rb * (2 * C::kTBytes >> 4);
+          const uint32_t tl = th + (C::kTBytes >> 4);
+          for (int kc = 0; kc < p.nkc && ok; ++kc) {
+            const uint32_t pat = (mm >> (4 * kc)) & 0xFu;
             const int rk = (rows_in == 0 && (first >> 2) == kc) ? (first & 3) : -1;  // K-step that resets
-            const uint32_t bw = b_lo_word + (uint32_t)s * (kStageBytes >> 4);
-            const uint32_t ra = a_base + (uint32_t)slot * 128;
+            for (int pl = 0; pl < 2; ++pl) {
+              if (!wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              const uint32_t bw = b_word + (uint32_t)s * (kStageBytes >> 4);
 #pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-              if (!(pat & (1u << ks))) continue;
-              const uint64_t bhi = make_desc(bw + ks * 2, kDescHi);
-              const uint64_t blo = make_desc(bw + (kTileBytes >> 4) + ks * 2, kDescHi);
-              const uint32_t ahi = ra + (uint32_t)ks * 16, alo = ahi + 8;
-              const uint32_t acc0 = ks == rk ? 0u : 1u;
-              if constexpr (TF) {
-                mma_tf32_ts(d_tmem, ahi, bhi, idesc, acc0);
-                mma_tf32_ts(d_tmem, ahi, blo, idesc, 1u);
-                mma_tf32_ts(d_tmem, alo, bhi, idesc, 1u);
-              } else {
-                mma_bf16_ts(d_tmem, ahi, bhi, idesc, acc0);
-                mma_bf16_ts(d_tmem, ahi, blo, idesc, 1u);
-                mma_bf16_ts(d_tmem, alo, bhi, idesc, 1u);
+              for (int ks = 0; ks < 4; ++ks) {
+                if (!((pat >> ks) & 1u)) continue;
+                const uint64_t bd = make_desc(bw + ks * 2, kBHi);
+                // A for (tile, K-step j) starts 2 j + 128/kCm tt core matrices in
+                const uint32_t qa = (uint32_t)(2 * (4 * kc + ks)) + tq;
+                const uint64_t ahi = make_desc(th + qa * (128u >> 4), kAHi);
+                if (pl == 0) {
+                  mma_ss<TF>(d, ahi, bd, idesc, ks == rk ? 0u : 1u);
+                  mma_ss<TF>(d, make_desc(tl + qa * (128u >> 4), kAHi), bd, idesc, 1u);
+                } else {
+                  mma_ss<TF>(d, ahi, bd, idesc, 1u);
+                }
+              }
+              mma_commit(&a_empty[s]);
+              if (++s == C::kStages) {
+                s = 0;
+                s_phase ^= 1u;
               }
             }
-            mma_commit(&a_empty[s]);
-            mma_commit(&s_empty[slot]);
-            if (++s == kStages) {
-              s = 0;
-              s_phase ^= 1u;
-            }
-            slot ^= 1;
-            if (slot == 0) r_phase ^= 1u;
           }
           if (!ok) break;
+          mma_commit(&r_empty[rb]);
+          rb ^= 1;
+          if (rb == 0) r_phase ^= 1u;
           ++rows_in;
-          if (rows_in == p.flush_rows || ai == n_rows - 1) {
-            mma_commit(t_full);
+          if (window_end(my_tt, ai, n_rows, flush)) {
+            mma_commit(&t_full[my_tt]);
             rows_in = 0;
           }
         }
@@ -515,125 +555,108 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp < 2 + kBuilderWarps) {
     // ------------------------------------------------------------ Toeplitz builders
-    // Lane m of TMEM quadrant q (m = 32 q + lane) is shift s0 + m; per K-step
-    // it writes 8 columns of packed hi pairs and 8 of lo pairs, read from
-    // the row's overlapping pair arrays (one 32-bit load per column).
+    // Per left row: stage the centred, split row X[i] = Lp[s0 + i] (hi and lo
+    // parts), then write the core-matrix buffer T[q][r][t] = X[kCm q + r + t]
+    // of both parts into the free row buffer.
     const int bt = threadIdx.x - 64;  // 0..127
-    const int qd = warp & 3;
-    const int m = 32 * qd + lane;
-    const uint32_t lane_addr = tmem_base + ((uint32_t)(32 * qd) << 16) + kRingCol;
-    int it = 0, rows_done = 0;
+    constexpr int kChunks = 2 * C::kQ * 8;  // 16-byte rows of T, both parts
+    int rows_done = 0;
     bool ok = true;
-    for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
+    for (long long round = 0; round * gridDim.x < n_items; ++round) {
       const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
       if (pos >= n_items) continue;
       TcItem w;
       if (!tc_item(p, p.items[pos], &w)) continue;
       const float* lrow_base = p.left + (long long)w.l * p.Hl * p.Wl;
-      const float mu = p.mu_left[w.l];
-      for (int ai = 0; ai < w.n_rows; ++ai, ++rows_done) {
-        // split the centred, zero-padded left row x_j = L[a][j - (Wr-1)] - mu
-        // into pairs (x_j, x_j+1) of BF16 hi parts and of BF16 lo parts
-        uint32_t* ph = pairs + (rows_done & 1) * (2 * kMaxLp);
-        uint32_t* pl = ph + kMaxLp;
+      const float mu = __ldg(p.mu_left + w.l);
+      const int x_off = w.s0_0 - (p.Wr - 1);  // left column of X[0]
+      int ai = 0;
+      for (; ai < w.n_rows; ++ai, ++rows_done) {
+        const int rbuf = rows_done & 1;
+        float* xh = xs + rbuf * (2 * kXLen);
+        float* xl = xh + kXLen;
         const float* src = lrow_base + (long long)(w.a_lo + ai) * p.Wl;
-        for (int j = bt; j < p.lp_len; j += 32 * kBuilderWarps) {
-          const int x = j - (p.Wr - 1);
-          const float x0 = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
+        for (int i = bt; i < kXLen; i += 32 * kBuilderWarps) {
+          const int x = x_off + i;
+          const float v = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
+          float h, l;
           if constexpr (TF) {
-            // TF32: one element per column, hi and lo parts
-            const float h = tf32_round(x0);
-            ph[j] = __float_as_uint(h);
-            pl[j] = __float_as_uint(tf32_round(x0 - h));
+            h = tf32_round(v);
+            l = tf32_round(v - h);
           } else {
-            const float x1 = (x + 1 >= 0 && x + 1 < p.Wl) ? __ldg(src + x + 1) - mu : 0.0f;
-            const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-            ph[j] = bf16x2_bits(h);
-            pl[j] = bf16x2_bits(__floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h)));
+            h = __bfloat162float(__float2bfloat16_rn(v));
+            l = v - h;
           }
+          xh[i] = h;
+          xl[i] = l;
         }
-        // the builder threads leave together (they share a named barrier)
+        // the staged row is complete; the builder threads also leave together here
         if (bar_red_or(!ok, 1, 32 * kBuilderWarps)) {
           ok = false;
           break;
         }
-        for (int kc = 0; kc < p.nkc; ++kc, ++it) {
-          const int slot = it & 1;
-          bool wt = wait_or_abort_sleep(&s_empty[slot], ((it >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
-          wt = __all_sync(0xffffffffu, wt);  // tcgen05.st below must stay warp-uniform
-          if (!wt) {
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-#pragma unroll
-          for (int tt = 0; tt < 2; ++tt) {
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-              const int j = kc * 4 + ks;
-              if (!(((tt == 0 ? w.mask0 : w.mask1) >> j) & 1u)) continue;
-              const int base = (tt == 0 ? w.s0_0 : w.s0_1) + m + p.kstep * j;
-              uint32_t r[16];
-#pragma unroll
-              for (int e = 0; e < 8; ++e) {
-                r[e] = ph[base + (TF ? 1 : 2) * e];
-                r[8 + e] = pl[base + (TF ? 1 : 2) * e];
-              }
-              tmem_st16(lane_addr + (uint32_t)slot * 128 + (uint32_t)(tt * 4 + ks) * 16, r);
+        bool wt = wait_or_abort_sleep(&r_empty[rbuf], ((rows_done >> 1) & 1) ^ 1, abort_flag, p.flags, 15);
+        ok = __all_sync(0xffffffffu, wt);
+        if (ok) {
+          unsigned char* tb = t_buf + rbuf * (2 * C::kTBytes);
+          for (int c = bt; c < kChunks; c += 32 * kBuilderWarps) {
+            const int part = c / (C::kQ * 8), q = (c >> 3) % C::kQ, r = c & 7;
+            const float* x = (part ? xl : xh) + C::kCm * q + r;
+            uint4 v;
+            if constexpr (TF) {
+              v.x = __float_as_uint(x[0]);
+              v.y = __float_as_uint(x[1]);
+              v.z = __float_as_uint(x[2]);
+              v.w = __float_as_uint(x[3]);
+            } else {
+              auto pk = [](float lo_half, float hi_half) {
+                const __nv_bfloat162 b = __floats2bfloat162_rn(lo_half, hi_half);
+                return *reinterpret_cast<const uint32_t*>(&b);
+              };
+              v.x = pk(x[0], x[1]);
+              v.y = pk(x[2], x[3]);
+              v.z = pk(x[4], x[5]);
+              v.w = pk(x[6], x[7]);
             }
+            *reinterpret_cast<uint4*>(tb + part * C::kTBytes + q * 128 + r * 16) = v;
           }
-          tmem_wait_st();
-          tc_fence_before();
+          // generic-proxy writes become visible to the tensor core's reads
+          fence_proxy_async_shared();
           __syncwarp();
-          if (lane == 0) mbar_arrive(&s_full[slot]);  // one arrival per warp
+          if (lane == 0) mbar_arrive(&r_full[rbuf]);  // one arrival per warp
         }
-        // a failed wait reaches the other builders at the next row's barrier
       }
+      if (ai < w.n_rows) break;  // a failed wait: every builder left at the same barrier
     }
   } else if (warp < 2 + kBuilderWarps + kEpiWarps) {
     // ------------------------------------------------------------ epilogue
     // Warp w (index ew = w - 6): lane quadrant q = w % 4, accumulator
-    // columns [64 * (ew / 4), +64): tile tt = ew / 8, B rows nb.. of it.
+    // columns [128 * (ew / 4), +128): tile tt = ew / 8, B rows nb.. of it.
+    constexpr int kCols = 128;
     const int ew = warp - (2 + kBuilderWarps);
     const int q = warp & 3;
     const int tt = ew >> 3;
     const int nb = ((ew >> 2) & 1) * kCols;
-    const int et = threadIdx.x - 32 * (2 + kBuilderWarps);  // 0..511
-    int d_all = 0, n_done = 0;
+    int d_all = 0;
     bool ok = true;
     for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
       const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
       if (pos >= n_items) continue;
       TcItem w;
       if (!tc_item(p, p.items[pos], &w)) continue;
-      long long* rbase = row_base + (n_done & 1) * 128;
-      if (et < 128) {
-        // output row offset of B row n (-1: outside the output)
-        const int n = et;
-        int pp, dy;
-        if (p.mats_mode) {
-          pp = n % p.P;
-          dy = w.dy0 + n / p.P;
-        } else {
-          pp = n / p.DY;
-          dy = w.dy0 + (p.DY - 1) - (n % p.DY);
-        }
-        const int k = w.p0 + pp, sy = dy + p.Hr - 1;
-        rbase[n] = (k < p.pm.K && sy >= 0 && sy < p.Sy)
-                       ? (((long long)w.l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx
-                       : -1LL;
-      }
-      // publishes the table; every epilogue thread has finished the item
-      // that used this half of it two items ago
-      asm volatile("bar.sync 2, %0;" ::"r"(32 * kEpiWarps) : "memory");
-      float acc[kCols];
-#pragma unroll
-      for (int i = 0; i < kCols; ++i) acc[i] = 0.0f;
-      const uint32_t tmask = tt == 0 ? w.mask0 : w.mask1;
-      const bool live = tmask != 0u;
-      const int n_drains = (w.n_rows + p.flush_rows - 1) / p.flush_rows;
+      // Output offset of B row n: ((l*o_l + k*o_k)*Sy + sy)*Sx with k = p0 + pp,
+      // sy = dy + Hr - 1.  Rows are partner-major inside a row shift (P >= 8:
+      // n = d*P + pp, dy = dy0 + d) or row-shift-major inside a partner
+      // (P < 8: n = pp*DY + d, dy = dy0 + DY-1 - d).  Computed per 32-row
+      // batch (no table lookups: shared memory is busy serving the MMAs).
+      const long long row_l = (long long)w.l * p.pm.o_l;
+      const long long kstride = (long long)p.pm.o_k * p.Sy * p.Sx;
+      const int lgP = __ffs(p.P) - 1, lgDY = __ffs(p.DY) - 1;
+      const bool live = (tt == 0 ? w.mask0 : w.mask1) != 0u;
+      const int sx = (tt == 0 ? w.s0_0 : w.s0_1) + 32 * q + lane;
+      const int n_drains = window_count(tt, w.n_rows, p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P]);
       for (int d = 0; d < n_drains; ++d, ++d_all) {
-        bool wt = wait_or_abort_sleep(t_full, d_all & 1, abort_flag, p.flags, 16);
+        bool wt = wait_or_abort_sleep(&t_full[tt], d_all & 1, abort_flag, p.flags, 16);
         wt = __all_sync(0xffffffffu, wt);  // tcgen05.ld below must stay warp-uniform
         if (!wt) {
           ok = false;
@@ -641,29 +664,55 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         tc_fence_after();
         if (live) {
-          const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(tt * 128 + nb);
-#pragma unroll
-          for (int j = 0; j < kCols; j += 8) {
-            float v[8];
-            tmem_ld8(col0 + (uint32_t)j, v);
+          const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(tt * kN + nb);
+          for (int j = 0; j < kCols; j += 32) {
+            float v[32];
+            tmem_ld32(col0 + (uint32_t)j, v);
             tmem_wait_ld();
+            if (sx >= p.Sx) continue;
+            const int n0 = nb + j;
+            if (p.P >= 32 || !p.mats_mode) {
+              // the batch lies inside one row shift (P >= 32) or one partner
+              // (DY >= 64): offsets o0 + i * stride for i in [i_lo, i_hi)
+              long long o0, stride;
+              int i_lo = 0, i_hi = 32;
+              if (p.mats_mode) {
+                const int k0 = w.p0 + (n0 & (p.P - 1));
+                const int sy = w.dy0 + (n0 >> lgP) + p.Hr - 1;
+                if (sy < 0 || sy >= p.Sy) continue;
+                i_hi = min(32, p.pm.K - k0);
+                o0 = ((row_l + (long long)k0 * p.pm.o_k) * p.Sy + sy) * p.Sx;
+                stride = kstride;
+              } else {
+                const int k = w.p0 + (n0 >> lgDY);
+                if (k >= p.pm.K) continue;
+                const int sy0 = w.dy0 + (p.DY - 1) - (n0 & (p.DY - 1)) + p.Hr - 1;
+                i_lo = max(0, sy0 - (p.Sy - 1));
+                i_hi = min(32, sy0 + 1);
+                o0 = ((row_l + (long long)k * p.pm.o_k) * p.Sy + sy0) * p.Sx;
+                stride = -(long long)p.Sx;
+              }
+              float* o = p.out + o0 + sx;
 #pragma unroll
-            for (int i = 0; i < 8; ++i) acc[j + i] += v[i];
+              for (int i = 0; i < 32; ++i)
+                if (i >= i_lo && i < i_hi) red_add(o + i * stride, v[i]);
+            } else {
+              // P = 8 or 16: several row shifts per batch
+#pragma unroll
+              for (int i = 0; i < 32; ++i) {
+                const int n = n0 + i;
+                const int k = w.p0 + (n & (p.P - 1));
+                const int sy = w.dy0 + (n >> lgP) + p.Hr - 1;
+                if (k < p.pm.K && sy >= 0 && sy < p.Sy)
+                  red_add(p.out + ((row_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx + sx, v[i]);
+              }
+            }
           }
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(t_empty);  // one arrival per warp
+        if (lane == 0) mbar_arrive(&t_empty[tt]);  // one arrival per warp
       }
-      const int sx = (tt == 0 ? w.s0_0 : w.s0_1) + 32 * q + lane;
-      if (ok && live && sx < p.Sx) {
-#pragma unroll
-        for (int i = 0; i < kCols; ++i) {
-          const long long rb = rbase[nb + i];
-          if (rb >= 0) red_add(p.out + rb + sx, acc[i]);
-        }
-      }
-      ++n_done;
     }
   }
 
@@ -675,28 +724,75 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Matrix sums for the means: grid (matrix, slice); FP64 partial sums of a
-// slice, block-reduced, added into sums[m] (zeroed before the launch).
+// Matrix sums and sums of squares (means and spreads): grid (matrix, slice);
+// FP64 partial sums of a slice, block-reduced, added into sums[m] and sq[m]
+// (zeroed before the launch).
 __global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src, long long area, int slices,
-                                                  double* __restrict__ sums) {
-  __shared__ double red[8];
+                                                  double* __restrict__ sums, double* __restrict__ sq) {
+  __shared__ double red[8], red2[8];
   const int m = blockIdx.x / slices, sl = blockIdx.x % slices;
   const long long per = (area + slices - 1) / slices;
   const long long lo = sl * per, hi = min(area, lo + per);
   const float* a = src + (long long)m * area;
   // FP32 within a thread (at most a few dozen terms; FP64 arithmetic is slow
   // on this GPU), FP64 across threads and blocks
-  float part = 0.0f;
-  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) part += __ldg(a + i);
-  double acc = (double)part;
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  float part = 0.0f, part2 = 0.0f;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const float x = __ldg(a + i);
+    part += x;
+    part2 = fmaf(x, x, part2);
+  }
+  double acc = (double)part, acc2 = (double)part2;
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_down_sync(0xffffffffu, acc, o);
+    acc2 += __shfl_down_sync(0xffffffffu, acc2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[threadIdx.x >> 5] = acc;
+    red2[threadIdx.x >> 5] = acc2;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int j = 0; j < 8; ++j) t += red[j];
+    double t = 0.0, t2 = 0.0;
+    for (int j = 0; j < 8; ++j) {
+      t += red[j];
+      t2 += red2[j];
+    }
     atomicAdd(&sums[m], t);
+    atomicAdd(&sq[m], t2);
   }
+}
+
+// Accumulation window (left rows between drains) per (left matrix, partner
+// group).  The tensor-core accumulation error grows with the window and with
+// the partial sums of the centred data relative to the result.  With
+// rho = s_L s_R / (|m_L m_R| + s_L s_R) (means m, standard deviations s; at
+// most 1, for zero-mean data), the centred partial sums are at most rho of
+// the result's scale even when they add coherently, so the window may be
+// 1/rho times the zero-mean one.  Largest rho over the group's partners.
+__global__ void flush_kernel(const double* __restrict__ sums, const double* __restrict__ sq, int n_left,
+                             double left_area, double right_area, PairMap pm, int n_pgroups, int P, int base_rows,
+                             int max_rows, int fixed, int* __restrict__ flush) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_left * n_pgroups) return;
+  const int l = i / n_pgroups, pg = i % n_pgroups;
+  int rows = max_rows;
+  if (fixed > 0) {
+    rows = fixed;
+  } else {
+    const double ml = sums[l] / left_area;
+    const double sl = sqrt(fmax(0.0, sq[l] / left_area - ml * ml));
+    double rho = 0.0;
+    for (int k = pg * P; k < min(pm.K, pg * P + P); ++k) {
+      const long long r = (long long)l * pm.r_l + (long long)k * pm.r_k + n_left;
+      const double mr = sums[r] / right_area;
+      const double sr = sqrt(fmax(0.0, sq[r] / right_area - mr * mr));
+      const double den = fabs(ml * mr) + sl * sr;
+      if (den > 0.0) rho = fmax(rho, sl * sr / den);
+    }
+    if (rho > 0.0) rows = (int)fmin((double)max_rows, fmax((double)base_rows, base_rows / rho));
+  }
+  flush[i] = max(1, rows);
 }
 
 __global__ void mean_kernel(const double* __restrict__ sums, int n_left, double left_area, int n_total,
@@ -864,7 +960,7 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, lp_len, pitch, n_chunks;
+  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, pitch, n_chunks;
   long long n_items;
   int smem_bytes;
 };
@@ -874,9 +970,9 @@ int chunk_rows();
 bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   if (g.Sx > 512 || g.Wr > 256) return false;  // four 128-shift tiles, 16 K-steps
   int P = 1;
-  while (P < 128 && P < pm.K) P *= 2;
+  while (P < kN && P < pm.K) P *= 2;
   t->P = P;
-  t->DY = 128 / P;
+  t->DY = kN / P;
   t->mats_mode = P >= 8 ? 1 : 0;
   t->n_tiles = (g.Sx + 127) / 128;
   t->n_halves = (t->n_tiles + 1) / 2;
@@ -884,12 +980,11 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   t->kstep = tf32 ? 8 : 16;             // columns per MMA K-step (32 bytes)
   const int chunk = 128 / t->es;        // columns per 128-byte TMA box row
   t->nkc = (g.Wr + chunk - 1) / chunk;
-  t->lp_len = 128 * t->n_tiles + 4 * t->kstep * t->nkc;
   t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
   t->n_chunks = div_up(t->DY - 1 + std::min(g.Hl, g.Hr), chunk_rows());
   t->n_items = (long long)t->n_halves * t->n_chunks * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
-  t->smem_bytes = 1024 + kStages * kStageBytes + 4 * kMaxLp * 4 + 2 * 128 * 8 + kBarBytes;
-  return t->lp_len <= kMaxLp && t->smem_bytes <= 227 * 1024;
+  t->smem_bytes = tf32 ? TcCfg<true>::kSmem : TcCfg<false>::kSmem;
+  return t->smem_bytes <= 227 * 1024;
 }
 
 long long n_right_of(const PairMap& pm) {
@@ -903,17 +998,18 @@ int env_int(const char* name, int def) {
   return v > 0 ? v : def;
 }
 
-// Left rows accumulated in tensor memory between two drains: at most 192
-// MMAs (12 per 64-column chunk of a right row: 4 K-steps x 3 products) feed
-// one accumulator between drains, which keeps the truncation error of the
-// tensor-core accumulation (about 5e-8 of the partial sum per MMA, measured)
-// near 5e-8 x 192 ~ 1e-5 of the largest partial sum, even for zero-mean data
-// whose partial sums are as large as the result.
-// XC_TC_FLUSH_ROWS / XC_TC_CHUNK_ROWS override the defaults (studies).
-int flush_rows(int nkc) {
+// The zero-mean window: left rows accumulated in tensor memory between two
+// drains when the data has zero mean, at most 240 MMAs (12 per 128-byte
+// chunk of a right row: 4 K-steps x 3 products) per accumulator.  Measured on
+// zero-mean 256x256 data: windows of 5 rows (240 MMAs) 6.0e-6 of max|out|,
+// 8 rows 8e-6, 12 rows 1.1e-5, 32 rows 3e-5 (the split alone gives ~6e-6).
+// flush_kernel widens it for data whose means dominate.  Every drain stalls
+// the MMAs while the epilogue reads the accumulators.
+// XC_TC_FLUSH_ROWS fixes the window, XC_TC_CHUNK_ROWS the item length (studies).
+int flush_rows(int nkc) { return std::max(1, std::min(32, 240 / (12 * nkc))); }
+int flush_fixed() {
   static const int v = env_int("XC_TC_FLUSH_ROWS", 0);
-  if (v > 0) return v;
-  return std::max(1, std::min(32, 192 / (12 * nkc)));
+  return v;
 }
 int chunk_rows() {
   static int v = std::min(kMaxChunkRows, env_int("XC_TC_CHUNK_ROWS", 32));
@@ -924,6 +1020,8 @@ int chunk_rows() {
 struct TcWs {
   float* mu;        // n_left + n_right means
   double* sums;     // n_left + n_right matrix sums
+  double* sq;       // n_left + n_right sums of squares
+  int* flush;       // n_left x n_pgroups accumulation windows
   float* CL;        // n_left x (Hl+1) x Wl centred column prefix sums
   float* CR;        // n_right x (Hr+1) x Wr
   void* hi;         // n_right x Hr x pitch, BF16 or TF32-rounded FP32
@@ -947,6 +1045,8 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   };
   w.mu = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
   w.sums = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
+  w.sq = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
+  w.flush = reinterpret_cast<int*>(take(sizeof(int) * (size_t)pm.n_left * div_up(pm.K, t.P)));
   w.CL = reinterpret_cast<float*>(take(sizeof(float) * (size_t)pm.n_left * (g.Hl + 1) * g.Wl));
   w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * g.Wr));
   w.hi = take((size_t)t.es * plane);
@@ -984,12 +1084,18 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
     // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
     const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
     XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, sizeof(double) * (nl + nr), stream));
-    sum_kernel<<<(unsigned)(nl * ls), 256, 0, stream>>>(left, la, ls, w.sums);
+    XC_CUDA_TRY(cudaMemsetAsync(w.sq, 0, sizeof(double) * (nl + nr), stream));
+    sum_kernel<<<(unsigned)(nl * ls), 256, 0, stream>>>(left, la, ls, w.sums, w.sq);
     XC_CUDA_TRY(cudaGetLastError());
-    sum_kernel<<<(unsigned)(nr * rs), 256, 0, stream>>>(right, ra, rs, w.sums + nl);
+    sum_kernel<<<(unsigned)(nr * rs), 256, 0, stream>>>(right, ra, rs, w.sums + nl, w.sq + nl);
     XC_CUDA_TRY(cudaGetLastError());
     mean_kernel<<<(unsigned)((nl + nr + 255) / 256), 256, 0, stream>>>(w.sums, nl, (double)la, (int)(nl + nr),
                                                                         (double)ra, w.mu);
+    XC_CUDA_TRY(cudaGetLastError());
+    const int npg = div_up(pm.K, t.P);
+    flush_kernel<<<(unsigned)((nl * npg + 255) / 256), 256, 0, stream>>>(
+        w.sums, w.sq, nl, (double)la, (double)ra, pm, npg, t.P, flush_rows(t.nkc), chunk_rows(), flush_fixed(),
+        w.flush);
     XC_CUDA_TRY(cudaGetLastError());
   }
   colsum_kernel<<<(unsigned)(nl * ((g.Wl + 31) / 32)), 256, 0, stream>>>(left, g.Hl, g.Wl, w.mu, w.CL);
@@ -1057,9 +1163,8 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.n_dytiles = div_up(g.Sy, t.DY);
   prm.n_halves = t.n_halves;
   prm.nkc = t.nkc;
-  prm.lp_len = t.lp_len;
   prm.kstep = t.kstep;
-  prm.flush_rows = flush_rows(t.nkc);
+  prm.flush_tab = w.flush;
   prm.chunk_rows = chunk_rows();
   prm.n_chunks = t.n_chunks;
   prm.flags = device_flags();
@@ -1070,7 +1175,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.n_live = w.items + t.n_items;
   worklist_kernel<<<1, 1024, 0, stream>>>(prm, t.n_items, w.items, w.items + t.n_items);
   XC_CUDA_TRY(cudaGetLastError());
-  // persistent: one CTA per SM (211 KB of shared memory and all 512 TMEM
+  // persistent: one CTA per SM (about 205 KB of shared memory and all 512 TMEM
   // columns each), walking the items round-robin
   int dev = 0, sms = 0;
   XC_CUDA_TRY(cudaGetDevice(&dev));
