@@ -126,7 +126,8 @@ struct TcParams {
   int kstep;        // columns per K-step: 16 (BF16) or 8 (TF32)
   const int* flush_tab;  // drain TMEM every this many left rows, per (left matrix, partner group)
   int chunk_rows;   // left rows per work item (a longer row range is split over items)
-  const int* items;  // non-empty work items, most left rows first (index encoding of tc_item)
+  const int* items;  // non-empty work items (pairs when paired), most left rows first (tc_item encoding)
+  int paired;        // 1: clusters of two CTAs take the two halves of an item pair, sharing right tiles
   const int* n_live; // entries of `items` (written on the device)
   int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
   DeviceFlags* flags;
@@ -317,15 +318,18 @@ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem
 }
 
 // Lists the non-empty work items, most left rows first (a counting sort by
-// row count): one block.  Every CTA of tc_kernel reads the same list.
+// row count): one block.  Every CTA of tc_kernel reads the same list.  When
+// paired, the entries are item pairs (the two halves of the shifts, which
+// have the same rows): pair i holds items 2 i and 2 i + 1.
 __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long long n_total, int* __restrict__ items,
                                                         int* __restrict__ n_live) {
+  const int step = p.paired ? 2 : 1;
   __shared__ int cnt[kMaxChunkRows + 1];
   for (int r = threadIdx.x; r <= kMaxChunkRows; r += blockDim.x) cnt[r] = 0;
   __syncthreads();
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
-    if (tc_item(p, idx, &w)) atomicAdd(&cnt[w.n_rows], 1);
+    if (tc_item(p, idx * step, &w)) atomicAdd(&cnt[w.n_rows], 1);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -340,8 +344,52 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   __syncthreads();
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
-    if (tc_item(p, idx, &w)) items[atomicAdd(&cnt[w.n_rows], 1)] = (int)idx;
+    if (tc_item(p, idx * step, &w)) items[atomicAdd(&cnt[w.n_rows], 1)] = (int)idx;
   }
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// The item a CTA takes in `round`: list entries are dealt to the CTAs (or
+// to the clusters when paired) in snake order, round r giving position
+// r*G + c or r*G + G-1-c; in a cluster, CTA rank h takes half h of the pair.
+__device__ __forceinline__ bool round_item(const TcParams& p, long long n_live, long long round, TcItem* w) {
+  const int cs = p.paired ? 2 : 1;
+  const long long G = gridDim.x / cs, c = blockIdx.x / cs;
+  const long long pos = round * G + ((round & 1) ? G - 1 - c : c);
+  if (pos >= n_live) return false;
+  const long long idx = p.paired ? 2LL * p.items[pos] + cluster_rank() : (long long)p.items[pos];
+  return tc_item(p, idx, w);
+}
+
+__device__ __forceinline__ long long n_rounds(const TcParams& p, long long n_live) {
+  const long long G = gridDim.x / (p.paired ? 2 : 1);
+  return (n_live + G - 1) / G;
+}
+
+// Arrives on the mbarrier at the same shared-memory offset in every CTA of
+// `mask` once this thread's MMAs are complete.
+__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
+}
+
+// TMA load of a 4D box delivered to the same shared-memory offset in every
+// CTA of `mask`, each arriving (complete_tx) on its own barrier at `bar`'s offset.
+__device__ __forceinline__ void tma_load_4d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
+                                               int c2, int c3, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster "
+      "[%0], [%1, {%3, %4, %5, %6}], [%2], %7;" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "h"(mask)
+      : "memory");
 }
 
 // Accumulator windows of an item: tile 0 drains after every `flush` left
@@ -390,12 +438,17 @@ __global__ void __launch_bounds__(kThreads, 1)
   // pipeline counters running across them, so the next item's loads and
   // MMAs overlap the previous item's final adds.
   const long long n_items = *p.n_live;
-
+  const long long n_round = n_rounds(p, n_items);
+  // Paired: the rank-0 CTA of the cluster loads every right tile for both
+  // CTAs (multicast), and a stage is free again once all four issuers of the
+  // cluster have consumed it.
+  const uint16_t cl_mask = p.paired ? 3 : 1;
+  const bool loader = !p.paired || cluster_rank() == 0;
   if (threadIdx.x == 0) {
     // consumed barriers take one commit from each issuer
     for (int s = 0; s < C::kStages; ++s) {
       mbar_init(&a_full[s], 1);
-      mbar_init(&a_empty[s], 2);
+      mbar_init(&a_empty[s], p.paired ? 4 : 2);
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&r_full[s], kBuilderWarps);
@@ -408,6 +461,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_mbar_init();
     prefetch_tensormap(&map_hi);
     prefetch_tensormap(&map_lo);
+  }
+  // the peer's barriers must be initialised before this CTA's multicast
+  // loads and commits reach them
+  if (p.paired) {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -426,11 +485,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (lane == 0) {
       int it = 0;
       bool ok = true;
-      for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
-        const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
-        if (pos >= n_items) continue;
+      for (long long round = 0; round < n_round && ok; ++round) {
         TcItem w;
-        if (!tc_item(p, p.items[pos], &w)) continue;
+        if (!round_item(p, n_items, round, &w)) continue;
         for (int ai = 0; ai < w.n_rows && ok; ++ai) {
           const int a = w.a_lo + ai;
           for (int kc = 0; kc < p.nkc && ok; ++kc) {
@@ -441,16 +498,25 @@ __global__ void __launch_bounds__(kThreads, 1)
                 break;
               }
               mbar_arrive_expect_tx(&a_full[s], kStageBytes);
+              if (!loader) continue;  // the peer's loads arrive here too
               unsigned char* dst = b_tiles + s * kStageBytes;
               const CUtensorMap* map = pl == 0 ? &map_hi : &map_lo;
               const int x = kc * 4 * p.kstep;  // first column of the chunk
               if (p.mats_mode) {
-                for (int d = 0; d < p.DY; ++d)
-                  tma_load_4d(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0);
+                for (int d = 0; d < p.DY; ++d) {
+                  if (p.paired)
+                    tma_load_4d_mc(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0, cl_mask);
+                  else
+                    tma_load_4d(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0);
+                }
               } else {
                 const int b0 = a - w.dy0 - (p.DY - 1);
-                for (int q = 0; q < p.P; ++q)
-                  tma_load_4d(dst + q * p.DY * 128, map, &a_full[s], x, b0, w.rdim2, w.p0 + q);
+                for (int q = 0; q < p.P; ++q) {
+                  if (p.paired)
+                    tma_load_4d_mc(dst + q * p.DY * 128, map, &a_full[s], x, b0, w.rdim2, w.p0 + q, cl_mask);
+                  else
+                    tma_load_4d(dst + q * p.DY * 128, map, &a_full[s], x, b0, w.rdim2, w.p0 + q);
+                }
               }
             }
           }
@@ -479,11 +545,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       int s = 0, rb = 0;                      // stage, Toeplitz row buffer
       uint32_t s_phase = 0, r_phase = 0, t_phase = 1;
       bool ok = true;
-      for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
-        const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
-        if (pos >= n_items) continue;
+      for (long long round = 0; round < n_round && ok; ++round) {
         TcItem w;
-        if (!tc_item(p, p.items[pos], &w)) continue;
+        if (!round_item(p, n_items, round, &w)) continue;
         const uint32_t mm = my_tt == 0 ? w.mask0 : w.mask1;
         const int first = mm ? __ffs(mm) - 1 : -1;
         const int n_rows = w.n_rows;
@@ -531,7 +595,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                   mma_ss<TF>(d, ahi, bd, idesc, 1u);
                 }
               }
-              mma_commit(&a_empty[s]);
+              if (p.paired)
+                mma_commit_mc(&a_empty[s], cl_mask);
+              else
+                mma_commit(&a_empty[s]);
               if (++s == C::kStages) {
                 s = 0;
                 s_phase ^= 1u;
@@ -562,11 +629,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     constexpr int kChunks = 2 * C::kQ * 8;  // 16-byte rows of T, both parts
     int rows_done = 0;
     bool ok = true;
-    for (long long round = 0; round * gridDim.x < n_items; ++round) {
-      const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
-      if (pos >= n_items) continue;
+    for (long long round = 0; round < n_round; ++round) {
       TcItem w;
-      if (!tc_item(p, p.items[pos], &w)) continue;
+      if (!round_item(p, n_items, round, &w)) continue;
       const float* lrow_base = p.left + (long long)w.l * p.Hl * p.Wl;
       const float mu = __ldg(p.mu_left + w.l);
       const int x_off = w.s0_0 - (p.Wr - 1);  // left column of X[0]
@@ -639,11 +704,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int nb = ((ew >> 2) & 1) * kCols;
     int d_all = 0;
     bool ok = true;
-    for (long long round = 0; round * gridDim.x < n_items && ok; ++round) {
-      const long long pos = round * gridDim.x + ((round & 1) ? gridDim.x - 1 - blockIdx.x : blockIdx.x);
-      if (pos >= n_items) continue;
+    for (long long round = 0; round < n_round && ok; ++round) {
       TcItem w;
-      if (!tc_item(p, p.items[pos], &w)) continue;
+      if (!round_item(p, n_items, round, &w)) continue;
       // Output offset of B row n: ((l*o_l + k*o_k)*Sy + sy)*Sx with k = p0 + pp,
       // sy = dy + Hr - 1.  Rows are partner-major inside a row shift (P >= 8:
       // n = d*P + pp, dy = dy0 + d) or row-shift-major inside a partner
@@ -721,6 +784,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512) : "memory");
+  }
+  // neither CTA of a pair leaves while the other may still load into or
+  // arrive on its shared memory
+  if (p.paired) {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
 }
 
@@ -1007,6 +1076,10 @@ int env_int(const char* name, int def) {
 // the MMAs while the epilogue reads the accumulators.
 // XC_TC_FLUSH_ROWS fixes the window, XC_TC_CHUNK_ROWS the item length (studies).
 int flush_rows(int nkc) { return std::max(1, std::min(32, 240 / (12 * nkc))); }
+bool paired_enabled() {
+  static const bool v = std::getenv("XC_TC_PAIRED") != nullptr && std::atoi(std::getenv("XC_TC_PAIRED")) != 0;
+  return v;
+}
 int flush_fixed() {
   static const int v = env_int("XC_TC_FLUSH_ROWS", 0);
   return v;
@@ -1169,24 +1242,55 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.n_chunks = t.n_chunks;
   prm.flags = device_flags();
 
-  // the work list: non-empty items, most left rows first, built on the device
+  // Items come in pairs (the two halves of the shifts, Sx > 256) that read
+  // the same right tiles: with XC_TC_PAIRED=1 a cluster of two CTAs takes a
+  // pair, and one TMA load delivers each tile to both (halving the L2-to-SM
+  // traffic).  Off by default: at 256x256 x 64 the right tiles come from L2
+  // fast enough (1.62 ms unpaired, 1.65 ms paired), and the lockstep of the
+  // two CTAs costs more than the traffic it saves.
+  prm.paired = (t.n_halves == 2 && paired_enabled()) ? 1 : 0;
+  const long long n_list = prm.paired ? t.n_items / 2 : t.n_items;
+
+  // the work list: non-empty items (or pairs), most left rows first, built on the device
   if (t.n_items > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
   prm.items = w.items;
   prm.n_live = w.items + t.n_items;
-  worklist_kernel<<<1, 1024, 0, stream>>>(prm, t.n_items, w.items, w.items + t.n_items);
+  worklist_kernel<<<1, 1024, 0, stream>>>(prm, n_list, w.items, w.items + t.n_items);
   XC_CUDA_TRY(cudaGetLastError());
   // persistent: one CTA per SM (about 205 KB of shared memory and all 512 TMEM
-  // columns each), walking the items round-robin
-  int dev = 0, sms = 0;
-  XC_CUDA_TRY(cudaGetDevice(&dev));
-  XC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const long long blocks = std::max(1LL, std::min<long long>(t.n_items, sms));
+  // columns each), walking the list in snake order
   auto kern = tf32 ? tc_kernel<true> : tc_kernel<false>;
   XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = (size_t)t.smem_bytes;
+  cfg.stream = stream;
+  long long blocks;
+  if (prm.paired) {
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    // as many clusters as can be resident at once (a GPC with an odd number
+    // of free SMs leaves one out)
+    cfg.gridDim = dim3(2);
+    int clusters = 0;
+    XC_CUDA_TRY(cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg));
+    if (clusters < 1) return fail(XC_ERR_CUDA, "no resident cluster of two CTAs for the tensor-core kernel");
+    blocks = 2 * std::max(1LL, std::min<long long>(n_list, clusters));
+  } else {
+    int dev = 0, sms = 0;
+    XC_CUDA_TRY(cudaGetDevice(&dev));
+    XC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    blocks = std::max(1LL, std::min<long long>(n_list, sms));
+  }
+  cfg.gridDim = dim3((unsigned)blocks);
   const int slot = kernel_timer_begin(stream);
-  kern<<<(unsigned)blocks, kThreads, t.smem_bytes, stream>>>(mhi, mlo, prm);
+  XC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, mhi, mlo, prm));
   kernel_timer_end(slot, stream);
-  XC_CUDA_TRY(cudaGetLastError());
   return XC_OK;
 }
 
