@@ -839,9 +839,8 @@ __global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src,
 // most 1, for zero-mean data), the centred partial sums are at most rho of
 // the result's scale even when they add coherently, so the window may be
 // 1/rho times the zero-mean one.  Largest rho over the group's partners.
-__global__ void flush_kernel(const double* __restrict__ sums, const double* __restrict__ sq, int n_left,
-                             double left_area, double right_area, PairMap pm, int n_pgroups, int P, int base_rows,
-                             int max_rows, int fixed, int* __restrict__ flush) {
+__global__ void flush_kernel(const float* __restrict__ mu, const float* __restrict__ sd, int n_left, PairMap pm,
+                             int n_pgroups, int P, int base_rows, int max_rows, int fixed, int* __restrict__ flush) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_left * n_pgroups) return;
   const int l = i / n_pgroups, pg = i % n_pgroups;
@@ -849,25 +848,30 @@ __global__ void flush_kernel(const double* __restrict__ sums, const double* __re
   if (fixed > 0) {
     rows = fixed;
   } else {
-    const double ml = sums[l] / left_area;
-    const double sl = sqrt(fmax(0.0, sq[l] / left_area - ml * ml));
-    double rho = 0.0;
+    const float ml = mu[l], sl = sd[l];
+    float rho = 0.0f;
     for (int k = pg * P; k < min(pm.K, pg * P + P); ++k) {
       const long long r = (long long)l * pm.r_l + (long long)k * pm.r_k + n_left;
-      const double mr = sums[r] / right_area;
-      const double sr = sqrt(fmax(0.0, sq[r] / right_area - mr * mr));
-      const double den = fabs(ml * mr) + sl * sr;
-      if (den > 0.0) rho = fmax(rho, sl * sr / den);
+      const float den = fabsf(ml * mu[r]) + sl * sd[r];
+      if (den > 0.0f) rho = fmaxf(rho, sl * sd[r] / den);
     }
-    if (rho > 0.0) rows = (int)fmin((double)max_rows, fmax((double)base_rows, base_rows / rho));
+    if (rho > 0.0f) rows = (int)fminf((float)max_rows, fmaxf((float)base_rows, base_rows / rho));
   }
   flush[i] = max(1, rows);
 }
 
-__global__ void mean_kernel(const double* __restrict__ sums, int n_left, double left_area, int n_total,
-                            double right_area, float* __restrict__ mu) {
+// Means and standard deviations (FP64 from the sums; the variance is a
+// difference of nearly equal terms for data far from zero).
+__global__ void mean_kernel(const double* __restrict__ sums, const double* __restrict__ sq, int n_left,
+                            double left_area, int n_total, double right_area, float* __restrict__ mu,
+                            float* __restrict__ sd) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m < n_total) mu[m] = (float)(sums[m] / (m < n_left ? left_area : right_area));
+  if (m < n_total) {
+    const double area = m < n_left ? left_area : right_area;
+    const double mean = sums[m] / area;
+    mu[m] = (float)mean;
+    sd[m] = (float)sqrt(fmax(0.0, sq[m] / area - mean * mean));
+  }
 }
 
 // Column prefix sums of the centred matrices fl32(M - mu) (the values the
@@ -1029,12 +1033,13 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, pitch, n_chunks;
+  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, pitch, n_chunks, chunk_rows;
   long long n_items;
   int smem_bytes;
 };
 
-int chunk_rows();
+int chunk_rows_fixed();
+int sm_count();
 
 bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   if (g.Sx > 512 || g.Wr > 256) return false;  // four 128-shift tiles, 16 K-steps
@@ -1050,7 +1055,14 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   const int chunk = 128 / t->es;        // columns per 128-byte TMA box row
   t->nkc = (g.Wr + chunk - 1) / chunk;
   t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
-  t->n_chunks = div_up(t->DY - 1 + std::min(g.Hl, g.Hr), chunk_rows());
+  // left rows per item: at most 32, fewer when that leaves fewer than two
+  // items per SM (small problems), at least 4
+  const long long span = t->DY - 1 + std::min(g.Hl, g.Hr);
+  const long long rows_all = span * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, P) * t->n_halves;
+  t->chunk_rows = chunk_rows_fixed() > 0
+                      ? chunk_rows_fixed()
+                      : (int)std::max(4LL, std::min(32LL, rows_all / (2LL * sm_count())));
+  t->n_chunks = (int)div_up(span, (long long)t->chunk_rows);
   t->n_items = (long long)t->n_halves * t->n_chunks * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
   t->smem_bytes = tf32 ? TcCfg<true>::kSmem : TcCfg<false>::kSmem;
   return t->smem_bytes <= 227 * 1024;
@@ -1084,14 +1096,22 @@ int flush_fixed() {
   static const int v = env_int("XC_TC_FLUSH_ROWS", 0);
   return v;
 }
-int chunk_rows() {
-  static int v = std::min(kMaxChunkRows, env_int("XC_TC_CHUNK_ROWS", 32));
+int chunk_rows_fixed() {
+  static int v = std::min(kMaxChunkRows, env_int("XC_TC_CHUNK_ROWS", 0));
   return v;
+}
+int sm_count() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms <= 0)
+    return 152;
+  return sms;
 }
 
 // Workspace layout (each part 256-byte aligned).
 struct TcWs {
   float* mu;        // n_left + n_right means
+  float* sd;        // n_left + n_right standard deviations
   double* sums;     // n_left + n_right matrix sums
   double* sq;       // n_left + n_right sums of squares
   int* flush;       // n_left x n_pgroups accumulation windows
@@ -1117,6 +1137,7 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
     return ptr;
   };
   w.mu = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
+  w.sd = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
   w.sums = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
   w.sq = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
   w.flush = reinterpret_cast<int*>(take(sizeof(int) * (size_t)pm.n_left * div_up(pm.K, t.P)));
@@ -1162,13 +1183,12 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
     XC_CUDA_TRY(cudaGetLastError());
     sum_kernel<<<(unsigned)(nr * rs), 256, 0, stream>>>(right, ra, rs, w.sums + nl, w.sq + nl);
     XC_CUDA_TRY(cudaGetLastError());
-    mean_kernel<<<(unsigned)((nl + nr + 255) / 256), 256, 0, stream>>>(w.sums, nl, (double)la, (int)(nl + nr),
-                                                                        (double)ra, w.mu);
+    mean_kernel<<<(unsigned)((nl + nr + 255) / 256), 256, 0, stream>>>(w.sums, w.sq, nl, (double)la,
+                                                                        (int)(nl + nr), (double)ra, w.mu, w.sd);
     XC_CUDA_TRY(cudaGetLastError());
     const int npg = div_up(pm.K, t.P);
     flush_kernel<<<(unsigned)((nl * npg + 255) / 256), 256, 0, stream>>>(
-        w.sums, w.sq, nl, (double)la, (double)ra, pm, npg, t.P, flush_rows(t.nkc), chunk_rows(), flush_fixed(),
-        w.flush);
+        w.mu, w.sd, nl, pm, npg, t.P, flush_rows(t.nkc), t.chunk_rows, flush_fixed(), w.flush);
     XC_CUDA_TRY(cudaGetLastError());
   }
   colsum_kernel<<<(unsigned)(nl * ((g.Wl + 31) / 32)), 256, 0, stream>>>(left, g.Hl, g.Wl, w.mu, w.CL);
@@ -1238,7 +1258,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   prm.nkc = t.nkc;
   prm.kstep = t.kstep;
   prm.flush_tab = w.flush;
-  prm.chunk_rows = chunk_rows();
+  prm.chunk_rows = t.chunk_rows;
   prm.n_chunks = t.n_chunks;
   prm.flags = device_flags();
 
