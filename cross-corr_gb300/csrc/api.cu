@@ -4,6 +4,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <map>
 #include <memory>
@@ -356,16 +357,18 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
   // map -- the partners (one_to_many, n_to_mn) or the left matrices (n_to_m)
   // -- each a problem of the same mode.  Chunk i's input copy, correlation
   // and output copy run on three streams, so copies overlap the correlation
-  // of neighbouring chunks.  A chunk carries about 32 MiB of output or more: each
-  // correlation call has a fixed cost (prep kernels, a partly filled last
-  // wave), which smaller chunks would pay more often than the overlap saves
-  // (64 outputs of 511x511 FP32: two chunks win, four lose).
+  // of neighbouring chunks.  Each correlation call has a fixed cost (prep
+  // kernels, a partly filled last wave): at 64 outputs of 511x511 FP32
+  // (67 MB) one chunk measured 28.4k correlations/s, two 27.3k, four 21.0k,
+  // so a chunk carries at least 192 MiB of output.  XC_HOST_CHUNKS fixes the
+  // count (studies, tests).
   PairMap pm;
   uint64_t tmp = 0;
   make_pair_map(mode, n_left, n_right, &pm, &tmp);
   const bool by_left = mode == XC_N_TO_M;
   const int axis = mode == XC_ONE_TO_ONE ? 1 : (by_left ? (int)n_left : pm.K);
-  int n_chunks = (int)std::min<size_t>(std::min<size_t>(4, (size_t)axis), (ob + ((size_t)16 << 20)) / ((size_t)32 << 20));
+  int n_chunks = (int)std::min<size_t>(std::min<size_t>(4, (size_t)axis), ob / ((size_t)192 << 20));
+  if (const char* e = std::getenv("XC_HOST_CHUNKS")) n_chunks = std::min(std::max(1, std::atoi(e)), std::min(4, axis));
   if (n_chunks < 1) n_chunks = 1;
   const int per = (axis + n_chunks - 1) / n_chunks;
   n_chunks = (axis + per - 1) / per;

@@ -226,20 +226,22 @@ def test_errors_are_reported_not_fatal():
     assert out.shape == (1, 7, 7)
 
 
-@pytest.mark.parametrize("mode,n_l,n_r,side", [
-    ("one_to_many", 1, 7, 800),   # 7 partners, 71.5 MB out: 2 chunks of 4, 3
-    ("n_to_mn", 3, 39, 256),      # 13 partners of each left, 40.7 MB out: 1 chunk
-    ("n_to_mn", 3, 99, 256),      # 33 partners of each left, 103 MB out: 3 chunks of 11
-    ("n_to_m", 13, 7, 256),       # 13 lefts, 95 MB out: 3 chunks of 5, 5, 3
+@pytest.mark.parametrize("mode,n_l,n_r,side,chunks", [
+    ("one_to_many", 1, 7, 120, 2),   # 7 partners: chunks of 4, 3
+    ("n_to_mn", 3, 15, 64, 3),       # 5 partners of each left: chunks of 2, 2, 1
+    ("n_to_m", 5, 3, 64, 4),         # 5 lefts: chunks of 2, 2, 1
+    ("n_to_m", 5, 3, 64, 1),
 ])
-def test_host_buffer_entry_point_pipelined(mode, n_l, n_r, side):
-    """Outputs of 48 MiB and more go through the chunked copy-in / correlate
-    / copy-out pipeline; every chunk must land where the one-shot device call
-    puts it."""
+def test_host_buffer_entry_point_pipelined(mode, n_l, n_r, side, chunks, monkeypatch):
+    """The chunked copy-in / correlate / copy-out pipeline (XC_HOST_CHUNKS
+    fixes the chunk count): every chunk must land where the one-shot device
+    call puts it."""
+    monkeypatch.setenv("XC_HOST_CHUNKS", str(chunks))
     left = seeded((n_l, side, side), 41)
     right = seeded((n_r, side, side), 42)
-    out = xcorr.correlate_host(mode, left, right, method="direct")
-    ref = xcorr.correlate(mode, dev(left), dev(right), method="direct").cpu().numpy()
-    # a chunk holds fewer partners, so the plain kernel may pick another tile
-    # shape: same products, possibly another summation order
-    assert rel_to_max(out, ref) <= 1e-5
+    for method in ("direct", "tc_bf16x3"):
+        out = xcorr.correlate_host(mode, left, right, method=method)
+        ref = xcorr.correlate(mode, dev(left), dev(right), method=method).cpu().numpy()
+        # a chunk holds fewer partners, so a kernel may pick another tile shape
+        # (and the split path other means): same products, possibly another order
+        assert rel_to_max(out, ref) <= 1e-5
