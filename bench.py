@@ -329,6 +329,9 @@ def run_ours(args, rank, world, local_rank):
                 "h2d_bytes_per_step": int(left.nbytes + right.nbytes), "d2h_bytes_per_step": int(ho.numel() * 4),
                 "api": "xc_correlate_host (pinned host buffers)", "max_abs_diff_vs_device_run": e2e_err},
         "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                     # a split product costs 3 tensor-core products: the split path's ceiling is peak / 3
+                     "split_products": 3 if method.startswith("tc_") else None,
+                     "frac_of_split_ceiling": (achieved * 3 / peak) if method.startswith("tc_") else None,
                      "traffic": profiled_traffic(kernel_name), "kernel": kernel_name,
                      "algorithmic_flops_per_launch": flops, "peak_source": peak_note,
                      "kernel_ms": kernel_ms, "kernel_launches_timed": kt.launches,
