@@ -841,23 +841,25 @@ __global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src,
 // 1/rho times the zero-mean one.  Largest rho over the group's partners.
 __global__ void flush_kernel(const float* __restrict__ mu, const float* __restrict__ sd, int n_left, PairMap pm,
                              int n_pgroups, int P, int base_rows, int max_rows, int fixed, int* __restrict__ flush) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_left * n_pgroups) return;
-  const int l = i / n_pgroups, pg = i % n_pgroups;
-  int rows = max_rows;
-  if (fixed > 0) {
-    rows = fixed;
-  } else {
-    const float ml = mu[l], sl = sd[l];
-    float rho = 0.0f;
-    for (int k = pg * P; k < min(pm.K, pg * P + P); ++k) {
-      const long long r = (long long)l * pm.r_l + (long long)k * pm.r_k + n_left;
-      const float den = fabsf(ml * mu[r]) + sl * sd[r];
-      if (den > 0.0f) rho = fmaxf(rho, sl * sd[r] / den);
-    }
-    if (rho > 0.0f) rows = (int)fminf((float)max_rows, fmaxf((float)base_rows, base_rows / rho));
+  // one warp per (left matrix, partner group), lanes over the partners
+  const long long i = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= (long long)n_left * n_pgroups) return;  // warp-uniform
+  const int l = (int)(i / n_pgroups), pg = (int)(i % n_pgroups);
+  const float ml = mu[l], sl = sd[l];
+  float rho = 0.0f;
+  for (int k = pg * P + lane; k < min(pm.K, pg * P + P); k += 32) {
+    const long long r = (long long)l * pm.r_l + (long long)k * pm.r_k + n_left;
+    const float den = fabsf(ml * mu[r]) + sl * sd[r];
+    if (den > 0.0f) rho = fmaxf(rho, sl * sd[r] / den);
   }
-  flush[i] = max(1, rows);
+  for (int o = 16; o > 0; o >>= 1) rho = fmaxf(rho, __shfl_xor_sync(0xffffffffu, rho, o));
+  int rows = max_rows;
+  if (fixed > 0)
+    rows = fixed;
+  else if (rho > 0.0f)
+    rows = (int)fminf((float)max_rows, fmaxf((float)base_rows, base_rows / rho));
+  if (lane == 0) flush[i] = max(1, rows);
 }
 
 // Means and standard deviations (FP64 from the sums; the variance is a
@@ -874,9 +876,11 @@ __global__ void mean_kernel(const double* __restrict__ sums, const double* __res
   }
 }
 
-// Column prefix sums of the centred matrices fl32(M - mu) (the values the
-// split sees): C[m][y][x] = sum_{i<y} fl32(M[m][i][x] - mu_m), (H+1) x W per
-// matrix, FP32.  Centred, these sums are random walks of modest size, so FP32
+// Summed-area tables of the centred matrices fl32(M - mu) (the values the
+// split sees): S[m][y][x] = sum_{i<y, j<x} fl32(M[m][i][j] - mu_m),
+// (H+1) x (W+1) per matrix, FP32, in two passes.  This one writes the column
+// prefix sums C[y][x] = sum_{i<y} into S[y][x+1]; rowscan_kernel then scans
+// each row.  Centred, these sums are random walks of modest size, so FP32
 // holds them to ~1e-7; the summation is blocked (8-row segments, a carry per
 // 64-row chunk), which keeps every FP32 chain short.  One block per (matrix,
 // 32-column strip); each of its 8 warps loads 8 consecutive rows of a chunk
@@ -891,7 +895,7 @@ __global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ s
   const int x = (blockIdx.x % strips) * 32 + lane;
   const int w = threadIdx.x >> 5;
   const float* a = src + (long long)m * H * W;
-  float* c = C + (long long)m * (H + 1) * W;
+  float* c = C + (long long)m * (H + 1) * (W + 1) + 1;  // column x of C is column x + 1 of S
   const float mv = mu[m];
   if (w == 0) {
     carry[lane] = 0.0f;
@@ -914,7 +918,7 @@ __global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ s
     if (x < W) {
 #pragma unroll
       for (int i = 0; i < 8; ++i)
-        if (yb + i < H) c[(long long)(yb + i + 1) * W + x] = off + run[i];
+        if (yb + i < H) c[(long long)(yb + i + 1) * (W + 1) + x] = off + run[i];
     }
     __syncthreads();
     if (w == 0) {
@@ -971,19 +975,41 @@ __global__ void split_kernel(const float* __restrict__ src, const float* __restr
   }
 }
 
+// Second pass of the summed-area tables: row y of matrix m (one warp per
+// row, 8 rows per block) becomes its inclusive prefix sum over x, S[y][0] = 0.
+// The warp scans 32 consecutive columns at a time (coalesced), carrying the
+// running total (FP32 chains of at most W/32 + 5 terms).
+__global__ void __launch_bounds__(256) rowscan_kernel(float* __restrict__ S, long long n_rows, int W) {
+  const int lane = threadIdx.x & 31;
+  const long long row = blockIdx.x * 8LL + (threadIdx.x >> 5);
+  if (row >= n_rows) return;  // warp-uniform
+  float* q = S + row * (W + 1) + 1;
+  if (lane == 0) q[-1] = 0.0f;
+  float carry = 0.0f;
+  for (int c = 0; c < W; c += 32) {
+    float v = c + lane < W ? q[c + lane] : 0.0f;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    v += carry;
+    if (c + lane < W) q[c + lane] = v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
+  }
+}
+
 // out[o][sy][sx] = mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area over the
-// overlap of shift (sy, sx), where S' are sums of the centred matrices; one
-// warp per output row (8 rows per block, no block-wide barrier).  The band
-// sums of the overlapping rows, b[x] = C[y1][x] - C[y0][x] (centred column
-// prefix sums), are scanned along x in the warp's shared-memory slice;
-// everything is FP32 (the centred sums are small, and the result's rounding
-// stays near 1e-7 of max|out|).
-__global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out, const float* __restrict__ CL,
-                                                         const float* __restrict__ CR,
+// overlap of shift (sy, sx), where S' are sums of the centred matrices over
+// the overlap, four summed-area-table reads each; one warp per output row
+// (8 rows per block), consecutive lanes on consecutive shifts.  FP32 (the
+// centred sums are small, and the result's rounding stays near 1e-7 of
+// max|out|).
+__global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out, const float* __restrict__ SL,
+                                                         const float* __restrict__ SR,
                                                          const float* __restrict__ mu_l,
                                                          const float* __restrict__ mu_r, int Hl, int Wl, int Hr,
                                                          int Wr, int Sy, int Sx, long long n_rows, PairMap pm) {
-  extern __shared__ float qs[];  // 8 x ((Wl + 1) + (Wr + 1))
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long long row = blockIdx.x * 8LL + wid;  // o * Sy + sy
   if (row >= n_rows) return;  // warp-uniform
@@ -1004,21 +1030,10 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
   const long long r = l * pm.r_l + k * pm.r_k;
   const int dy = sy - (Hr - 1);
   const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
-  const float* cl0 = CL + (l * (Hl + 1) + y0) * (long long)Wl;
-  const float* cl1 = CL + (l * (Hl + 1) + y1) * (long long)Wl;
-  const float* cr0 = CR + (r * (Hr + 1) + (y0 - dy)) * (long long)Wr;
-  const float* cr1 = CR + (r * (Hr + 1) + (y1 - dy)) * (long long)Wr;
-  float* ql = qs + wid * (Wl + Wr + 2);
-  float* qr = ql + (Wl + 1);
-  for (int x = lane; x < Wl; x += 32) ql[x + 1] = cl1[x] - cl0[x];
-  for (int x = lane; x < Wr; x += 32) qr[x + 1] = cr1[x] - cr0[x];
-  if (lane == 0) {
-    ql[0] = 0.0f;
-    qr[0] = 0.0f;
-  }
-  __syncwarp();
-  warp_scan_inplace(ql, Wl, lane);
-  warp_scan_inplace(qr, Wr, lane);
+  const float* l0 = SL + (l * (Hl + 1) + y0) * (long long)(Wl + 1);
+  const float* l1 = SL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
+  const float* r0 = SR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
+  const float* r1 = SR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
   const float ml = mu_l[l], mr = mu_r[r];
   const float mlr = ml * mr;
   const float rows = (float)(y1 - y0);
@@ -1026,8 +1041,8 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
   for (int sx = lane; sx < Sx; sx += 32) {
     const int dx = sx - (Wr - 1);
     const int x0 = max(0, dx), x1 = min(Wl, Wr + dx);
-    const float sl = ql[x1] - ql[x0];
-    const float sr = qr[x1 - dx] - qr[x0 - dx];
+    const float sl = (__ldg(l1 + x1) - __ldg(l0 + x1)) - (__ldg(l1 + x0) - __ldg(l0 + x0));
+    const float sr = (__ldg(r1 + x1 - dx) - __ldg(r0 + x1 - dx)) - (__ldg(r1 + x0 - dx) - __ldg(r0 + x0 - dx));
     orow[sx] = fmaf(mr, sl, fmaf(ml, sr, mlr * (rows * (float)(x1 - x0))));
   }
 }
@@ -1115,8 +1130,8 @@ struct TcWs {
   double* sums;     // n_left + n_right matrix sums
   double* sq;       // n_left + n_right sums of squares
   int* flush;       // n_left x n_pgroups accumulation windows
-  float* CL;        // n_left x (Hl+1) x Wl centred column prefix sums
-  float* CR;        // n_right x (Hr+1) x Wr
+  float* CL;        // n_left x (Hl+1) x (Wl+1) summed-area tables of the centred matrices
+  float* CR;        // n_right x (Hr+1) x (Wr+1)
   void* hi;         // n_right x Hr x pitch, BF16 or TF32-rounded FP32
   void* lo;
   int* items;       // the kernel's work list
@@ -1141,8 +1156,8 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   w.sums = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
   w.sq = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
   w.flush = reinterpret_cast<int*>(take(sizeof(int) * (size_t)pm.n_left * div_up(pm.K, t.P)));
-  w.CL = reinterpret_cast<float*>(take(sizeof(float) * (size_t)pm.n_left * (g.Hl + 1) * g.Wl));
-  w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * g.Wr));
+  w.CL = reinterpret_cast<float*>(take(sizeof(float) * (size_t)pm.n_left * (g.Hl + 1) * (g.Wl + 1)));
+  w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * (g.Wr + 1)));
   w.hi = take((size_t)t.es * plane);
   w.lo = take((size_t)t.es * plane);
   w.items = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items + 1)));  // list + its length
@@ -1187,7 +1202,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
                                                                         (int)(nl + nr), (double)ra, w.mu, w.sd);
     XC_CUDA_TRY(cudaGetLastError());
     const int npg = div_up(pm.K, t.P);
-    flush_kernel<<<(unsigned)((nl * npg + 255) / 256), 256, 0, stream>>>(
+    flush_kernel<<<(unsigned)((32LL * nl * npg + 255) / 256), 256, 0, stream>>>(
         w.mu, w.sd, nl, pm, npg, t.P, flush_rows(t.nkc), t.chunk_rows, flush_fixed(), w.flush);
     XC_CUDA_TRY(cudaGetLastError());
   }
@@ -1195,6 +1210,14 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   XC_CUDA_TRY(cudaGetLastError());
   colsum_kernel<<<(unsigned)(nr * ((g.Wr + 31) / 32)), 256, 0, stream>>>(right, g.Hr, g.Wr, w.mu + nl, w.CR);
   XC_CUDA_TRY(cudaGetLastError());
+  {
+    // second pass: every row of the left and of the right tables
+    const long long lrows = (long long)nl * (g.Hl + 1), rrows = nr * (g.Hr + 1);
+    rowscan_kernel<<<(unsigned)((lrows + 7) / 8), 256, 0, stream>>>(w.CL, lrows, g.Wl);
+    XC_CUDA_TRY(cudaGetLastError());
+    rowscan_kernel<<<(unsigned)((rrows + 7) / 8), 256, 0, stream>>>(w.CR, rrows, g.Wr);
+    XC_CUDA_TRY(cudaGetLastError());
+  }
   // 3. split of the centred right matrices
   {
     const long long rows = nr * g.Hr;
@@ -1211,9 +1234,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   // 4. the mean terms initialise the output
   {
     const long long n_rows = (long long)n_out * g.Sy;
-    const size_t smem = sizeof(float) * 8 * (g.Wl + g.Wr + 2);
-    XC_CUDA_TRY(cudaFuncSetAttribute(correction_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    correction_kernel<<<(unsigned)((n_rows + 7) / 8), 256, smem, stream>>>(
+    correction_kernel<<<(unsigned)((n_rows + 7) / 8), 256, 0, stream>>>(
         out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, n_rows, pm);
   }
   XC_CUDA_TRY(cudaGetLastError());
