@@ -220,6 +220,21 @@ __device__ __forceinline__ void red_add(float* addr, float v) {
   asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v) : "memory");
 }
 
+// Non-blocking look at a phase: the MMA issuers ask for the next stage
+// early and use the answer after the current stage's MMAs, so the barrier
+// round trip overlaps them.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait that also gives up as soon as another role aborted.
 __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
                                               DeviceFlags* flags, unsigned where) {
@@ -544,6 +559,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       constexpr uint32_t kTileQ = 128 / C::kCm;   // core matrices between the two shift tiles
       int s = 0, rb = 0;                      // stage, Toeplitz row buffer
       uint32_t s_phase = 0, r_phase = 0, t_phase = 1;
+      bool s_ready = false;                   // stage s seen landed ahead of time
       bool ok = true;
       for (long long round = 0; round < n_round && ok; ++round) {
         TcItem w;
@@ -575,11 +591,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint32_t pat = (mm >> (4 * kc)) & 0xFu;
             const int rk = (rows_in == 0 && (first >> 2) == kc) ? (first & 3) : -1;  // K-step that resets
             for (int pl = 0; pl < 2; ++pl) {
-              if (!wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13)) {
+              if (!s_ready && !wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13)) {
                 ok = false;
                 break;
               }
               tc_fence_after();
+              {
+                // ask for the following stage now, use the answer after this one's MMAs
+                const int s2 = s + 1 == C::kStages ? 0 : s + 1;
+                s_ready = mbar_test_wait(&a_full[s2], s2 == 0 ? s_phase ^ 1u : s_phase);
+              }
               const uint32_t bw = b_word + (uint32_t)s * (kStageBytes >> 4);
 #pragma unroll
               for (int ks = 0; ks < 4; ++ks) {
