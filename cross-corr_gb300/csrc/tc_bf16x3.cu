@@ -190,15 +190,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-#pragma unroll
-  for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // 32 consecutive columns of this warp's 32 lanes: one register each.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   uint32_t r[32];
@@ -949,28 +940,6 @@ __global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ s
     }
     __syncthreads();
   }
-}
-
-// Exclusive prefix of q[1..n] in place by one warp (q[0] = 0 on entry):
-// afterwards q[x] = sum of the first x band values.  Each lane scans a
-// contiguous segment, then a shuffle scan combines the segment totals.
-__device__ __forceinline__ void warp_scan_inplace(float* q, int n, int lane) {
-  const int per = (n + 31) / 32;
-  const int lo = 1 + lane * per, hi = min(n + 1, lo + per);
-  float acc = 0.0f;
-  for (int i = lo; i < hi; ++i) {
-    acc += q[i];
-    q[i] = acc;
-  }
-  float v = acc;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const float u = __shfl_up_sync(0xffffffffu, v, o);
-    if (lane >= o) v += u;
-  }
-  const float off = v - acc;
-  for (int i = lo; i < hi; ++i) q[i] += off;
-  __syncwarp();
 }
 
 // Splits the centred right matrices fl32(R - mu_R) into hi/lo planes with a
