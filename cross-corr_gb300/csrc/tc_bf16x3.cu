@@ -211,6 +211,17 @@ __device__ __forceinline__ void red_add(float* addr, float v) {
   asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v) : "memory");
 }
 
+// The same under a predicate (no branch: a drain's 32 adds stay one straight
+// block the compiler can schedule; the address of a false one is not used).
+__device__ __forceinline__ void red_add_if(float* addr, float v, uint32_t pred) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %2, 0;\n\t"
+      "@p red.global.add.f32 [%0], %1;\n\t}" ::"l"(addr),
+      "f"(v), "r"(pred)
+      : "memory");
+}
+
 // Non-blocking look at a phase: the MMA issuers ask for the next stage
 // early and use the answer after the current stage's MMAs, so the barrier
 // round trip overlaps them.
@@ -768,9 +779,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                 stride = -(long long)p.Sx;
               }
               float* o = p.out + o0 + sx;
+              // rows i_lo <= i < i_hi of the batch are inside the output
+              const uint32_t below_hi = i_hi >= 32 ? 0xffffffffu : (i_hi <= 0 ? 0u : (1u << i_hi) - 1u);
+              const uint32_t from_lo = i_lo <= 0 ? 0xffffffffu : (i_lo >= 32 ? 0u : ~((1u << i_lo) - 1u));
+              const uint32_t valid = below_hi & from_lo;
 #pragma unroll
-              for (int i = 0; i < 32; ++i)
-                if (i >= i_lo && i < i_hi) red_add(o + i * stride, v[i]);
+              for (int i = 0; i < 32; ++i) red_add_if(o + i * stride, v[i], (valid >> i) & 1u);
             } else {
               // P = 8 or 16: several row shifts per batch
 #pragma unroll
