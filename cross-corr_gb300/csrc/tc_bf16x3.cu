@@ -151,6 +151,27 @@ __host__ __device__ constexpr uint32_t idesc_tf32_f32(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// The same, issued only when `exec` is non-zero (a guard predicate instead
+// of a branch keeps a stage's MMAs one straight block of code).
+template <bool TF>
+__device__ __forceinline__ void mma_ss_if(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate, uint32_t exec) {
+  if constexpr (TF)
+    asm volatile(
+        "{\n\t.reg .pred p, e;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "setp.ne.b32 e, %5, 0;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate), "r"(exec));
+  else
+    asm volatile(
+        "{\n\t.reg .pred p, e;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "setp.ne.b32 e, %5, 0;\n\t"
+        "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate), "r"(exec));
+}
+
 // Round to TF32 (10 explicit mantissa bits), nearest with ties away.
 __device__ __forceinline__ float tf32_round(float x) {
   uint32_t r;
@@ -592,6 +613,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int kc = 0; kc < p.nkc && ok; ++kc) {
             const uint32_t pat = (mm >> (4 * kc)) & 0xFu;
             const int rk = (rows_in == 0 && (first >> 2) == kc) ? (first & 3) : -1;  // K-step that resets
+#pragma unroll
             for (int pl = 0; pl < 2; ++pl) {
               if (!s_ready && !wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13)) {
                 ok = false;
@@ -606,16 +628,17 @@ __global__ void __launch_bounds__(kThreads, 1)
               const uint32_t bw = b_word + (uint32_t)s * (kStageBytes >> 4);
 #pragma unroll
               for (int ks = 0; ks < 4; ++ks) {
-                if (!((pat >> ks) & 1u)) continue;
+                // K-steps whose shifts meet only zeros are skipped (guard predicate)
+                const uint32_t on = (pat >> ks) & 1u;
                 const uint64_t bd = make_desc(bw + ks * 2, kBHi);
                 // A for (tile, K-step j) starts 2 j + 128/kCm tt core matrices in
                 const uint32_t qa = (uint32_t)(2 * (4 * kc + ks)) + tq;
                 const uint64_t ahi = make_desc(th + qa * (128u >> 4), kAHi);
                 if (pl == 0) {
-                  mma_ss<TF>(d, ahi, bd, idesc, ks == rk ? 0u : 1u);
-                  mma_ss<TF>(d, make_desc(tl + qa * (128u >> 4), kAHi), bd, idesc, 1u);
+                  mma_ss_if<TF>(d, ahi, bd, idesc, ks == rk ? 0u : 1u, on);
+                  mma_ss_if<TF>(d, make_desc(tl + qa * (128u >> 4), kAHi), bd, idesc, 1u, on);
                 } else {
-                  mma_ss<TF>(d, ahi, bd, idesc, 1u);
+                  mma_ss_if<TF>(d, ahi, bd, idesc, 1u, on);
                 }
               }
               if (p.paired)
