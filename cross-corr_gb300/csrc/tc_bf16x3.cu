@@ -419,6 +419,18 @@ __device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
       : "memory");
 }
 
+// mma_commit_mc when `multicast` is non-zero, else mma_commit: both forms
+// under guard predicates, so the issue loop has no branch here.
+__device__ __forceinline__ void mma_commit_sel(uint64_t* bar, uint16_t mask, int multicast) {
+  asm volatile(
+      "{\n\t.reg .pred m;\n\t"
+      "setp.ne.b32 m, %2, 0;\n\t"
+      "@m tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;\n\t"
+      "@!m tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(smem_u32(bar)),
+      "h"(mask), "r"(multicast)
+      : "memory");
+}
+
 // TMA load of a 4D box delivered to the same shared-memory offset in every
 // CTA of `mask`, each arriving (complete_tx) on its own barrier at `bar`'s offset.
 __device__ __forceinline__ void tma_load_4d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
@@ -641,14 +653,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                   mma_ss_if<TF>(d, ahi, bd, idesc, 1u, on);
                 }
               }
-              if (p.paired)
-                mma_commit_mc(&a_empty[s], cl_mask);
-              else
-                mma_commit(&a_empty[s]);
-              if (++s == C::kStages) {
-                s = 0;
-                s_phase ^= 1u;
-              }
+              mma_commit_sel(&a_empty[s], cl_mask, p.paired);
+              // next stage, without a branch
+              s = s + 1 == C::kStages ? 0 : s + 1;
+              s_phase ^= s == 0 ? 1u : 0u;
             }
           }
           if (!ok) break;
