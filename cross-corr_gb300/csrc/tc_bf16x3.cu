@@ -93,8 +93,14 @@ constexpr int kN = 256;                 // B rows per MMA: P partners x DY row s
 constexpr int kStageBytes = kN * 128;   // one plane of one 128-byte column chunk
 constexpr int kBuilderWarps = 4;
 constexpr int kEpiWarps = 16;           // four per TMEM lane quadrant
-// warp 0 producer, warps 1 and 22 MMA issuers, 2-5 builders, 6-21 epilogue
-constexpr int kThreads = 32 * (3 + kBuilderWarps + kEpiWarps);
+// MMA issuer threads: 2 (one per shift tile, warps 1 and 22) or 1 (warp 1
+// issues both tiles)
+#ifndef XC_TC_ISSUERS
+#define XC_TC_ISSUERS 2
+#endif
+constexpr int kIssuers = XC_TC_ISSUERS;
+// warp 0 producer, warps 1 (and 22) MMA issuers, 2-5 builders, 6-21 epilogue
+constexpr int kThreads = 32 * (2 + (kIssuers - 1) + kBuilderWarps + kEpiWarps);
 constexpr int kXLen = 520;              // staged row elements: the 511 a two-tile item reads, padded
 constexpr int kBarBytes = 256;          // 20 mbarriers at most, the abort flag, the TMEM address slot
 constexpr int kMaxChunkRows = 1024;     // left rows per work item at most
@@ -447,7 +453,8 @@ __device__ __forceinline__ void tma_load_4d_mc(void* dst, const CUtensorMap* map
 // drain after the item's last row.  True when row ai (0-based) ends a window.
 __device__ __forceinline__ bool window_end(int tt, int ai, int n_rows, int flush) {
   if (ai == n_rows - 1) return true;
-  const int off = tt == 0 ? 0 : flush - (flush + 1) / 2;
+  // one issuer drains both tiles together
+  const int off = (tt == 0 || kIssuers == 1) ? 0 : flush - (flush + 1) / 2;
   return (ai + 1 + off) % flush == 0;
 }
 
@@ -498,11 +505,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     // consumed barriers take one commit from each issuer
     for (int s = 0; s < C::kStages; ++s) {
       mbar_init(&a_full[s], 1);
-      mbar_init(&a_empty[s], p.paired ? 4 : 2);
+      mbar_init(&a_empty[s], (p.paired ? 2 : 1) * kIssuers);
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&r_full[s], kBuilderWarps);
-      mbar_init(&r_empty[s], 2);
+      mbar_init(&r_empty[s], kIssuers);
       mbar_init(&t_full[s], 1);
       mbar_init(&t_empty[s], kEpiWarps / 2);
       mbar_init(&mma_done[s], 1);
@@ -577,11 +584,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           mbar_wait_bounded(&a_full[q % C::kStages], (q / C::kStages) & 1, 1u << 16);
       }
     }
-  } else if (warp == 1 || warp == 2 + kBuilderWarps + kEpiWarps) {
+  } else if (warp == 1 || (kIssuers == 2 && warp == 2 + kBuilderWarps + kEpiWarps)) {
     // ------------------------------------------------------------ MMA issuers
-    // Both walk the same items, rows and stages; each issues its own tile's
-    // MMAs and commits to the shared consumed barriers.
-    const int my_tt = warp == 1 ? 0 : 1;
+    // With two issuers, both walk the same items, rows and stages; each
+    // issues its own tile's MMAs and commits to the shared consumed barriers.
+    // With one, it issues both tiles' MMAs.
+    constexpr int kT = 3 - kIssuers;          // tiles per issuer
+    const int t_first = warp == 1 ? 0 : 1;    // first tile of this issuer
     if (lane == 0) {
       // B: SBO 1024 B (8 rows x 128 B), 128-byte swizzle.  A (Toeplitz
       // buffer): no swizzle, LBO 128 B along K, SBO 128 B (BF16) or 256 B
@@ -599,20 +608,23 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long round = 0; round < n_round && ok; ++round) {
         TcItem w;
         if (!round_item(p, n_items, round, &w)) continue;
-        const uint32_t mm = my_tt == 0 ? w.mask0 : w.mask1;
-        const int first = mm ? __ffs(mm) - 1 : -1;
+        uint32_t mm[kT];
+        int first[kT];
+#pragma unroll
+        for (int t = 0; t < kT; ++t) {
+          mm[t] = t_first + t == 0 ? w.mask0 : w.mask1;
+          first[t] = mm[t] ? __ffs(mm[t]) - 1 : -1;
+        }
         const int n_rows = w.n_rows;
         const int flush = p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P];
-        const uint32_t d = tmem_base + (uint32_t)my_tt * kN;
-        const uint32_t tq = (uint32_t)my_tt * kTileQ;
         int rows_in = 0;
         for (int ai = 0; ai < n_rows && ok; ++ai) {
           if (rows_in == 0) {
-            // the epilogue must have drained this tile's previous window
-            if (!wait_or_abort(&t_empty[my_tt], t_phase, abort_flag, p.flags, 14)) {
-              ok = false;
-              break;
-            }
+            // the epilogue must have drained the previous window
+#pragma unroll
+            for (int t = 0; t < kT; ++t)
+              if (!wait_or_abort(&t_empty[t_first + t], t_phase, abort_flag, p.flags, 14)) ok = false;
+            if (!ok) break;
             t_phase ^= 1u;
           }
           if (!wait_or_abort(&r_full[rb], r_phase, abort_flag, p.flags, 12)) {
@@ -623,8 +635,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t th = t_word + (uint32_t)rb * (2 * C::kTBytes >> 4);
           const uint32_t tl = th + (C::kTBytes >> 4);
           for (int kc = 0; kc < p.nkc && ok; ++kc) {
-            const uint32_t pat = (mm >> (4 * kc)) & 0xFu;
-            const int rk = (rows_in == 0 && (first >> 2) == kc) ? (first & 3) : -1;  // K-step that resets
+            uint32_t pat[kT];
+            int rk[kT];
+#pragma unroll
+            for (int t = 0; t < kT; ++t) {
+              pat[t] = (mm[t] >> (4 * kc)) & 0xFu;
+              rk[t] = (rows_in == 0 && (first[t] >> 2) == kc) ? (first[t] & 3) : -1;  // K-step that resets
+            }
 #pragma unroll
             for (int pl = 0; pl < 2; ++pl) {
               if (!s_ready && !wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13)) {
@@ -640,17 +657,22 @@ __global__ void __launch_bounds__(kThreads, 1)
               const uint32_t bw = b_word + (uint32_t)s * (kStageBytes >> 4);
 #pragma unroll
               for (int ks = 0; ks < 4; ++ks) {
-                // K-steps whose shifts meet only zeros are skipped (guard predicate)
-                const uint32_t on = (pat >> ks) & 1u;
                 const uint64_t bd = make_desc(bw + ks * 2, kBHi);
-                // A for (tile, K-step j) starts 2 j + 128/kCm tt core matrices in
-                const uint32_t qa = (uint32_t)(2 * (4 * kc + ks)) + tq;
-                const uint64_t ahi = make_desc(th + qa * (128u >> 4), kAHi);
-                if (pl == 0) {
-                  mma_ss_if<TF>(d, ahi, bd, idesc, ks == rk ? 0u : 1u, on);
-                  mma_ss_if<TF>(d, make_desc(tl + qa * (128u >> 4), kAHi), bd, idesc, 1u, on);
-                } else {
-                  mma_ss_if<TF>(d, ahi, bd, idesc, 1u, on);
+#pragma unroll
+                for (int t = 0; t < kT; ++t) {
+                  const int tt = t_first + t;
+                  // K-steps whose shifts meet only zeros are skipped (guard predicate)
+                  const uint32_t on = (pat[t] >> ks) & 1u;
+                  const uint32_t d = tmem_base + (uint32_t)tt * kN;
+                  // A for (tile, K-step j) starts 2 j + 128/kCm tt core matrices in
+                  const uint32_t qa = (uint32_t)(2 * (4 * kc + ks)) + (uint32_t)tt * kTileQ;
+                  const uint64_t ahi = make_desc(th + qa * (128u >> 4), kAHi);
+                  if (pl == 0) {
+                    mma_ss_if<TF>(d, ahi, bd, idesc, ks == rk[t] ? 0u : 1u, on);
+                    mma_ss_if<TF>(d, make_desc(tl + qa * (128u >> 4), kAHi), bd, idesc, 1u, on);
+                  } else {
+                    mma_ss_if<TF>(d, ahi, bd, idesc, 1u, on);
+                  }
                 }
               }
               mma_commit_sel(&a_empty[s], cl_mask, p.paired);
@@ -664,15 +686,16 @@ __global__ void __launch_bounds__(kThreads, 1)
           rb ^= 1;
           if (rb == 0) r_phase ^= 1u;
           ++rows_in;
-          if (window_end(my_tt, ai, n_rows, flush)) {
-            mma_commit(&t_full[my_tt]);
+          if (window_end(t_first, ai, n_rows, flush)) {
+#pragma unroll
+            for (int t = 0; t < kT; ++t) mma_commit(&t_full[t_first + t]);
             rows_in = 0;
           }
         }
       }
       // All MMAs issued by this thread must finish before TMEM is released.
-      mma_commit(&mma_done[my_tt]);
-      mbar_wait_bounded(&mma_done[my_tt], 0, 1u << 22);
+      mma_commit(&mma_done[t_first]);
+      mbar_wait_bounded(&mma_done[t_first], 0, 1u << 22);
     }
   } else if (warp < 2 + kBuilderWarps) {
     // ------------------------------------------------------------ Toeplitz builders
