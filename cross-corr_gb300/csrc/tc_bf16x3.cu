@@ -886,10 +886,22 @@ __global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src,
   // FP32 within a thread (at most a few dozen terms; FP64 arithmetic is slow
   // on this GPU), FP64 across threads and blocks
   float part = 0.0f, part2 = 0.0f;
-  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    const float x = __ldg(a + i);
-    part += x;
-    part2 = fmaf(x, x, part2);
+  if ((area & 3) == 0 && (per & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+    // float4 loads, four in flight per thread
+    const float4* a4 = reinterpret_cast<const float4*>(a);
+    const long long lo4 = lo >> 2, hi4 = hi >> 2;
+#pragma unroll 4
+    for (long long i = lo4 + threadIdx.x; i < hi4; i += blockDim.x) {
+      const float4 x = __ldg(a4 + i);
+      part += (x.x + x.y) + (x.z + x.w);
+      part2 = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, part2))));
+    }
+  } else {
+    for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+      const float x = __ldg(a + i);
+      part += x;
+      part2 = fmaf(x, x, part2);
+    }
   }
   double acc = (double)part, acc2 = (double)part2;
   for (int o = 16; o > 0; o >>= 1) {
@@ -1012,24 +1024,56 @@ __global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ s
 
 // Splits the centred right matrices fl32(R - mu_R) into hi/lo planes with a
 // padded pitch: BF16 (T = __nv_bfloat16) or TF32-rounded FP32 (T = float).
+// A thread writes one 16-byte chunk of each plane (8 BF16 or 4 FP32 values);
+// when the rows are 16-byte multiples (and aligned) it reads them as float4.
 template <typename T>
-__global__ void split_kernel(const float* __restrict__ src, const float* __restrict__ mu, T* __restrict__ hi,
-                             T* __restrict__ lo, long long rows, int rows_per_matrix, int cols, int pitch) {
-  const long long total = rows * pitch;
+__global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ src, const float* __restrict__ mu,
+                                                    T* __restrict__ hi, T* __restrict__ lo, long long rows,
+                                                    int rows_per_matrix, int cols, int pitch) {
+  constexpr int E = 16 / (int)sizeof(T);
+  const int cpr = pitch / E;  // chunks per row
+  const long long total = rows * cpr;
+  const bool vec = (cols % 4) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
-    const long long r = i / pitch;
-    const int c = (int)(i % pitch);
-    const float v = c < cols ? src[r * cols + c] - mu[r / rows_per_matrix] : 0.0f;
-    if constexpr (sizeof(T) == 4) {
-      const float h = tf32_round(v);
-      hi[i] = h;
-      lo[i] = tf32_round(v - h);
+    const long long r = i / cpr;
+    const int c0 = (int)(i - r * cpr) * E;
+    const float m = __ldg(mu + r / rows_per_matrix);
+    const float* row = src + r * cols;
+    float v[E];
+    if (vec && c0 + E <= cols) {
+#pragma unroll
+      for (int q = 0; q < E; q += 4) {
+        const float4 f = __ldg(reinterpret_cast<const float4*>(row + c0 + q));
+        v[q] = f.x;
+        v[q + 1] = f.y;
+        v[q + 2] = f.z;
+        v[q + 3] = f.w;
+      }
     } else {
-      const __nv_bfloat16 h = __float2bfloat16_rn(v);
-      hi[i] = h;
-      lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
+#pragma unroll
+      for (int q = 0; q < E; ++q) v[q] = c0 + q < cols ? __ldg(row + c0 + q) : m;
     }
+    uint4 oh, ol;
+    uint32_t* ph = reinterpret_cast<uint32_t*>(&oh);
+    uint32_t* pl = reinterpret_cast<uint32_t*>(&ol);
+#pragma unroll
+    for (int q = 0; q < E; q += (sizeof(T) == 4 ? 1 : 2)) {
+      if constexpr (sizeof(T) == 4) {
+        const float x = c0 + q < cols ? v[q] - m : 0.0f;
+        const float h = tf32_round(x);
+        ph[q] = __float_as_uint(h);
+        pl[q] = __float_as_uint(tf32_round(x - h));
+      } else {
+        const float x0 = c0 + q < cols ? v[q] - m : 0.0f, x1 = c0 + q + 1 < cols ? v[q + 1] - m : 0.0f;
+        const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+        const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h));
+        ph[q / 2] = *reinterpret_cast<const uint32_t*>(&h);
+        pl[q / 2] = *reinterpret_cast<const uint32_t*>(&l);
+      }
+    }
+    reinterpret_cast<uint4*>(hi)[i] = oh;
+    reinterpret_cast<uint4*>(lo)[i] = ol;
   }
 }
 
@@ -1211,8 +1255,8 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   };
   w.mu = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
   w.sd = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
-  w.sums = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
-  w.sq = reinterpret_cast<double*>(take(sizeof(double) * (pm.n_left + nr)));
+  w.sums = reinterpret_cast<double*>(take(2 * sizeof(double) * (pm.n_left + nr)));
+  w.sq = w.sums ? w.sums + (pm.n_left + nr) : nullptr;  // zeroed together with the sums
   w.flush = reinterpret_cast<int*>(take(sizeof(int) * (size_t)pm.n_left * div_up(pm.K, t.P)));
   w.CL = reinterpret_cast<float*>(take(sizeof(float) * (size_t)pm.n_left * (g.Hl + 1) * (g.Wl + 1)));
   w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * (g.Wr + 1)));
@@ -1250,8 +1294,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
     const long long la = (long long)g.Hl * g.Wl, ra = (long long)g.Hr * g.Wr;
     // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
     const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
-    XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, sizeof(double) * (nl + nr), stream));
-    XC_CUDA_TRY(cudaMemsetAsync(w.sq, 0, sizeof(double) * (nl + nr), stream));
+    XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, 2 * sizeof(double) * (nl + nr), stream));
     sum_kernel<<<(unsigned)(nl * ls), 256, 0, stream>>>(left, la, ls, w.sums, w.sq);
     XC_CUDA_TRY(cudaGetLastError());
     sum_kernel<<<(unsigned)(nr * rs), 256, 0, stream>>>(right, ra, rs, w.sums + nl, w.sq + nl);
@@ -1279,7 +1322,7 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   // 3. split of the centred right matrices
   {
     const long long rows = nr * g.Hr;
-    long long blocks = (rows * t.pitch + 255) / 256;
+    long long blocks = (rows * (t.pitch / (16 / t.es)) + 255) / 256;
     if (blocks > 152 * 32) blocks = 152 * 32;
     if (tf32)
       split_kernel<float><<<(unsigned)blocks, 256, 0, stream>>>(right, w.mu + nl, (float*)w.hi, (float*)w.lo, rows,
