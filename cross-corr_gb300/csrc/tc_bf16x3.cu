@@ -58,20 +58,24 @@
 // R' = R - mu_R): the tensor cores correlate the centred data, whose partial
 // sums are small random walks, and the exact remainder
 //   out = corr(L', R') + mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area
-// (S = sum of the centred matrix over the overlap of a shift, from column
-// prefix sums of the centred matrices, scanned along the row per output row)
-// is written first by a correction kernel, which the tensor-core results are
-// then added to.
+// (S = sum of the centred matrix over the overlap of a shift, four reads of
+// a summed-area table of the centred matrix) is written first by a
+// correction kernel, which the tensor-core results are then added to.
 //
-// Warp roles (704 threads, one CTA per SM):
+// Warp roles (736 threads, one CTA per SM):
 //   warp 0      TMA producer of the right-row tiles
 //   warp 1      TMEM allocation; one thread issues the MMAs of shift tile 0
 //   warp 22     one thread issues the MMAs of shift tile 1
+//               (with XC_TC_ISSUERS=1, 704 threads: warp 1 issues both)
 //   warps 2-5   builders of the Toeplitz core-matrix buffer (two row buffers)
 //   warps 6-21  epilogue: 4 per TMEM lane quadrant, 128 accumulator columns each
 // Each tile's accumulator is drained on its own schedule, the two offset by
 // half a window: while the epilogue drains one tile, the other tile's issuer
 // keeps the tensor pipe busy (as far as the shared right-tile stages allow).
+// The issue loops are on the critical path (a lone thread barely keeps up
+// with 128x256x16 MMAs): a stage's MMAs are one straight block under guard
+// predicates, and the next stage's barrier is looked at before the current
+// stage's MMAs are issued.
 // All waits are bounded: an expired wait records a flag, the CTA winds down,
 // waits (bounded) for its own copies and MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
