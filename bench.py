@@ -353,9 +353,13 @@ def run_ours(args, rank, world, local_rank):
         line["configs"] = config_studies(torch, xcorr)
     if rank == 0 and not args.no_cpu_baseline:
         rate, dt = cpu_reference_rate(left, right, 16, os.cpu_count() or 1)
+        # the reference's cpu_* are single-threaded by construction: one core too
+        rate1, dt1 = cpu_reference_rate(left, right, 1, 1)
         line["cpu_baseline"] = {"value": rate, "unit": "correlations/s", "cores": os.cpu_count() or 1,
                                 "kind": "port", "sample": f"16 of 64 pairs ({dt:.1f} s), cpu_cross_corr_one_to_many "
-                                                          "restated in C, T=float"}
+                                                          "restated in C, T=float",
+                                "single_core": {"value": rate1, "cores": 1,
+                                                "sample": f"1 of 64 pairs ({dt1:.1f} s), the same loop on one thread"}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
