@@ -44,6 +44,13 @@ TC_SHAPES = [
     ("one_to_many", 1, 3, (12, 40), (10, 200), "uniform"),
     ("one_to_one", 1, 1, (9, 100), (7, 250), "normal"),
     ("n_to_m", 2, 3, (16, 256), (12, 256), "signed"),
+    # partner groups of 8, 32 and 256 (row shifts per B tile 32, 8, 1), three
+    # shift tiles (one item holds a single tile), one shift tile
+    ("one_to_many", 1, 7, (24, 24), (20, 28), "uniform"),
+    ("one_to_many", 1, 20, (18, 30), (16, 22), "normal"),
+    ("one_to_many", 1, 130, (9, 11), (8, 13), "uniform"),
+    ("n_to_mn", 2, 10, (12, 180), (10, 150), "signed"),
+    ("one_to_one", 1, 1, (40, 60), (30, 50), "uniform"),
 ]
 
 
