@@ -108,6 +108,7 @@ constexpr int kThreads = 32 * (2 + (kIssuers - 1) + kBuilderWarps + kEpiWarps);
 constexpr int kXLen = 520;              // staged row elements: the 511 a two-tile item reads, padded
 constexpr int kBarBytes = 256;          // 20 mbarriers at most, the abort flag, the TMEM address slot
 constexpr int kMaxChunkRows = 1024;     // left rows per work item at most
+constexpr int kMaxBands = 8;            // output row bands signalled as they complete
 
 // Per operand type: right-tile stages and the Toeplitz buffer (hi or lo part
 // of one left row): 64 core matrices of 8 BF16 or 128 of 4 FP32.
@@ -138,6 +139,13 @@ struct TcParams {
   int chunk_rows;   // left rows per work item (a longer row range is split over items)
   const int* items;  // non-empty work items (pairs when paired), most left rows first (tc_item encoding)
   int paired;        // 1: clusters of two CTAs take the two halves of an item pair, sharing right tiles
+  // Output row bands: items of row-shift tiles [band_start[b], band_start[b+1])
+  // come before those of band b+1 in the work list, and with band_done set the
+  // epilogue counts each band's finished items there (a host copy can wait
+  // on the count and take the band's rows while the kernel runs on).
+  int n_bands;
+  int band_start[kMaxBands + 1];
+  int* band_done;
   const int* n_live; // entries of `items` (written on the device)
   int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
   DeviceFlags* flags;
@@ -337,6 +345,7 @@ __device__ __forceinline__ uint32_t tile_mask(int s0, const TcParams& p) {
 struct TcItem {
   int l, p0, dy0, a_lo, n_rows, rdim2, s0_0, s0_1;
   uint32_t mask0, mask1;
+  int band;  // output row band of the item's row-shift tile
 };
 
 // idx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_halves + half;
@@ -362,29 +371,36 @@ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem
   w->s0_1 = w->s0_0 + 128;
   w->mask0 = tile_mask(w->s0_0, p);
   w->mask1 = tile_mask(w->s0_1, p);
+  int b = 0;
+  while (b + 1 < p.n_bands && t >= p.band_start[b + 1]) ++b;
+  w->band = b;
   return w->n_rows > 0;
 }
 
-// Lists the non-empty work items, most left rows first (a counting sort by
-// row count): one block.  Every CTA of tc_kernel reads the same list.  When
+// Lists the non-empty work items by output row band, then most left rows
+// first (a counting sort): one block.  Every CTA of tc_kernel reads the same
+// list.  When
 // paired, the entries are item pairs (the two halves of the shifts, which
 // have the same rows): pair i holds items 2 i and 2 i + 1.
 __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long long n_total, int* __restrict__ items,
                                                         int* __restrict__ n_live) {
   const int step = p.paired ? 2 : 1;
-  __shared__ int cnt[kMaxChunkRows + 1];
-  for (int r = threadIdx.x; r <= kMaxChunkRows; r += blockDim.x) cnt[r] = 0;
+  // key = band * (chunk_rows + 1) + (chunk_rows - rows): band first, then
+  // the longest items
+  __shared__ int cnt[kMaxBands * (kMaxChunkRows + 1)];
+  const int stride = p.chunk_rows + 1, n_keys = p.n_bands * stride;
+  for (int r = threadIdx.x; r < n_keys; r += blockDim.x) cnt[r] = 0;
   __syncthreads();
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
-    if (tc_item(p, idx * step, &w)) atomicAdd(&cnt[w.n_rows], 1);
+    if (tc_item(p, idx * step, &w)) atomicAdd(&cnt[w.band * stride + p.chunk_rows - w.n_rows], 1);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     int run = 0;
-    for (int r = p.chunk_rows; r >= 1; --r) {
-      const int c = cnt[r];
-      cnt[r] = run;  // first position of the items with r rows
+    for (int k = 0; k < n_keys; ++k) {
+      const int c = cnt[k];
+      cnt[k] = run;  // first position of the items with key k
       run += c;
     }
     *n_live = run;
@@ -392,8 +408,16 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   __syncthreads();
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
-    if (tc_item(p, idx * step, &w)) items[atomicAdd(&cnt[w.n_rows], 1)] = (int)idx;
+    if (tc_item(p, idx * step, &w))
+      items[atomicAdd(&cnt[w.band * stride + p.chunk_rows - w.n_rows], 1)] = (int)idx;
   }
+}
+
+// After tc_kernel: every band counter to its largest value, so a host copy
+// waiting on one is released even when the kernel gave up early (its
+// device flag then reports the error).
+__global__ void band_release_kernel(int* band_done, int n) {
+  if ((int)threadIdx.x < n) band_done[threadIdx.x] = 0x7fffffff;
 }
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -860,6 +884,19 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&t_empty[tt]);  // one arrival per warp
       }
+      if (p.band_done != nullptr) {
+        // this thread's reductions become visible before the band count moves
+        __threadfence();
+        // the epilogue warps leave together (a failed wait reaches the others here)
+        if (bar_red_or(!ok, 2, 32 * kEpiWarps)) {
+          ok = false;
+          break;
+        }
+        if (warp == 2 + kBuilderWarps && lane == 0) {
+          __threadfence();
+          atomicAdd(&p.band_done[w.band], 1);
+        }
+      }
     }
   }
 
@@ -1279,8 +1316,9 @@ size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32) {
   return ws_layout(nullptr, g, pm, t).bytes;
 }
 
-xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32) {
+xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
+                              const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
+                              int want_bands, int* band_done, TcBands* bands) {
   TcPlan t;
   if (!tc_plan(g, pm, tf32, &t))
     return fail(XC_ERR_UNSUPPORTED,
@@ -1394,8 +1432,48 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   // traffic).  Off by default: at 256x256 x 64 the right tiles come from L2
   // fast enough (1.62 ms unpaired, 1.65 ms paired), and the lockstep of the
   // two CTAs costs more than the traffic it saves.
-  prm.paired = (t.n_halves == 2 && paired_enabled()) ? 1 : 0;
+  prm.paired = (t.n_halves == 2 && paired_enabled() && band_done == nullptr) ? 1 : 0;
   const long long n_list = prm.paired ? t.n_items / 2 : t.n_items;
+
+  // Output row bands: contiguous runs of row-shift tiles with about equal
+  // numbers of left rows (the work), each covering output rows
+  // [tile_lo * DY, tile_hi * DY).  The host knows each band's live item count
+  // (an item is live when its chunk of left rows is not empty).
+  {
+    const int n_tiles_y = div_up(g.Sy, t.DY);
+    std::vector<long long> rows_of(n_tiles_y), live_of(n_tiles_y);
+    long long total = 0;
+    for (int ty = 0; ty < n_tiles_y; ++ty) {
+      const int dy0 = -(g.Hr - 1) + ty * t.DY;
+      const int lo = std::max(0, dy0), hi = std::min(g.Hl, dy0 + t.DY - 1 + g.Hr);
+      rows_of[ty] = std::max(0, hi - lo);
+      live_of[ty] = std::min<long long>(t.n_chunks, div_up(rows_of[ty], t.chunk_rows)) * t.n_halves * pm.n_left *
+                    div_up(pm.K, t.P);
+      total += rows_of[ty];
+    }
+    const int want = band_done ? std::max(1, std::min({want_bands, kMaxBands, n_tiles_y})) : 1;
+    // boundaries where the running row count passes k/want of the total; every
+    // band keeps at least one tile (and every tile has rows, so items)
+    prm.band_start[0] = 0;
+    long long acc = 0;
+    int nb = 1;
+    for (int ty = 0; ty + 1 < n_tiles_y && nb < want; ++ty) {
+      acc += rows_of[ty];
+      if (acc * want >= total * nb) prm.band_start[nb++] = ty + 1;
+    }
+    prm.band_start[nb] = n_tiles_y;
+    prm.n_bands = nb;
+    prm.band_done = band_done;
+    if (bands) {
+      bands->n = nb;
+      for (int k = 0; k < nb; ++k) {
+        bands->items[k] = 0;
+        for (int ty = prm.band_start[k]; ty < prm.band_start[k + 1]; ++ty) bands->items[k] += live_of[ty];
+        bands->row_lo[k] = std::min(g.Sy, prm.band_start[k] * t.DY);
+        bands->row_hi[k] = std::min(g.Sy, prm.band_start[k + 1] * t.DY);
+      }
+    }
+  }
 
   // the work list: non-empty items (or pairs), most left rows first, built on the device
   if (t.n_items > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
@@ -1437,7 +1515,16 @@ xc_status tc_correlate(const float* left, const float* right, float* out, const 
   const int slot = kernel_timer_begin(stream);
   XC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, mhi, mlo, prm));
   kernel_timer_end(slot, stream);
+  if (band_done) {
+    band_release_kernel<<<1, 32, 0, stream>>>(band_done, prm.n_bands);
+    XC_CUDA_TRY(cudaGetLastError());
+  }
   return XC_OK;
+}
+
+xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32) {
+  return tc_correlate_banded(left, right, out, g, pm, workspace, ws_bytes, stream, tf32, 1, nullptr, nullptr);
 }
 
 // ---------------------------------------------------------------------------

@@ -132,4 +132,17 @@ xc_status glue_hadamard_original(xc_dtype dtype, const void* ref, void* deformed
 xc_status glue_hadamard_n_to_m(xc_dtype dtype, const void* left, const void* right, void* out, long long area,
                                int n_left, int n_right, cudaStream_t stream);
 
+// Output row bands of the split tensor-core path.  With `band_done` (device,
+// one int per band) the kernel counts each band's finished work items there;
+// `bands` receives the bands' expected counts and output row ranges, so a
+// copy can wait for a band and take its rows while the kernel runs on.
+struct TcBands {
+  int n;
+  long long items[8];
+  int row_lo[8], row_hi[8];
+};
+xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
+                              const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
+                              int want_bands, int* band_done, TcBands* bands);
+
 }  // namespace xc

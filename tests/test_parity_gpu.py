@@ -245,3 +245,26 @@ def test_host_buffer_entry_point_pipelined(mode, n_l, n_r, side, chunks, monkeyp
         # a chunk holds fewer partners, so a kernel may pick another tile shape
         # (and the split path other means): same products, possibly another order
         assert rel_to_max(out, ref) <= 1e-5
+
+
+@pytest.mark.parametrize("mode,n_l,n_r,side,bands", [
+    ("one_to_many", 1, 9, 96, 3),
+    ("n_to_mn", 2, 6, 80, 4),
+    ("n_to_m", 3, 4, 64, 2),
+    ("one_to_one", 1, 1, 200, 8),
+])
+@pytest.mark.parametrize("method", ["tc_bf16x3", "tc_tf32x3"])
+def test_host_buffer_entry_point_banded(mode, n_l, n_r, side, bands, method, monkeypatch):
+    """Split tensor-core path through the host-buffer call with the output
+    copied out in row bands while the kernel runs (XC_HOST_BANDS fixes the
+    band count): every band's rows must match the one-shot device call."""
+    monkeypatch.setenv("XC_HOST_BANDS", str(bands))
+    monkeypatch.delenv("XC_HOST_CHUNKS", raising=False)
+    left = seeded((n_l, side, side), 51)
+    right = seeded((n_r, side - 7, side + 5), 52)
+    out = xcorr.correlate_host(mode, left, right, method=method)
+    ref = xcorr.correlate(mode, dev(left), dev(right), method=method).cpu().numpy()
+    # the banded work list visits the items in another order: same products,
+    # another order of the reductions into the output
+    assert rel_to_max(out, ref) <= 1e-6
+    assert rel_to_max(out, oracle.run_mode(mode, left, right, dtype="f32acc64", threads=8)) <= 1e-5
