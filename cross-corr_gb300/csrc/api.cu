@@ -148,7 +148,8 @@ xc_status host_banded_tc(ThreadCache& c, xc_mode mode, bool tf32, xc_size2 left,
   XC_TRY(tc_correlate_banded((const float*)c.d_left, (const float*)c.d_right, (float*)c.d_out, g, pm, c.d_ws,
                              c.ws_bytes, s, tf32, n_bands, c.d_bands, &bands));
   const size_t row = (size_t)g.Sx * sizeof(float), mat = row * g.Sy;
-  for (int b = 0; b < bands.n; ++b) {
+  for (int k = 0; k < bands.n; ++k) {
+    const int b = bands.order[k];
     if (wait_value32()(reinterpret_cast<CUstream>(c.s_out), reinterpret_cast<CUdeviceptr>(c.d_bands + b),
                        (cuuint32_t)bands.items[b], CU_STREAM_WAIT_VALUE_GEQ) != CUDA_SUCCESS)
       return fail(XC_ERR_CUDA, "stream wait on an output band failed");

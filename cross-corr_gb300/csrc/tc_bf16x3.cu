@@ -83,7 +83,9 @@
 #include <algorithm>
 #include <cstdlib>
 #include <mutex>
+#include <queue>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "xc_common.cuh"
@@ -139,13 +141,18 @@ struct TcParams {
   int chunk_rows;   // left rows per work item (a longer row range is split over items)
   const int* items;  // non-empty work items (pairs when paired), most left rows first (tc_item encoding)
   int paired;        // 1: clusters of two CTAs take the two halves of an item pair, sharing right tiles
-  // Output row bands: items of row-shift tiles [band_start[b], band_start[b+1])
-  // come before those of band b+1 in the work list, and with band_done set the
+  // Output row bands: band b holds the items of row-shift tiles
+  // [band_start[b], band_start[b+1]); the work list takes the bands one after
+  // another in band_rank order, and with band_done set the
   // epilogue counts each band's finished items there (a host copy can wait
   // on the count and take the band's rows while the kernel runs on).
   int n_bands;
   int band_start[kMaxBands + 1];
+  int band_rank[kMaxBands];  // place of each band in the work list (a permutation of 0..n_bands-1)
   int* band_done;
+  // Host-built schedule (banded launches), or null: CTA c takes entry
+  // r * gridDim.x + c in round r (-1: nothing), *n_live entries in all.
+  const int* sched;
   const int* n_live; // entries of `items` (written on the device)
   int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
   DeviceFlags* flags;
@@ -330,7 +337,7 @@ __host__ __device__ __forceinline__ int centre_out(int r, int n, int tc) {
 // Active K-steps of a 128-shift tile starting at s0: bit j is set when
 // A's K-step j (right columns kstep*j .. kstep*j + kstep - 1) meets a left
 // column.
-__device__ __forceinline__ uint32_t tile_mask(int s0, const TcParams& p) {
+__host__ __device__ __forceinline__ uint32_t tile_mask(int s0, const TcParams& p) {
   uint32_t m = 0;
   if (s0 >= p.Sx) return 0;
   for (int j = 0; j < 4 * p.nkc; ++j) {
@@ -350,7 +357,7 @@ struct TcItem {
 
 // idx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_halves + half;
 // false when the item has no left rows.
-__device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
+__host__ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
   const int half = (int)(idx % p.n_halves);
   const long long bid = idx / p.n_halves;
   const int per_rank = p.pm.n_left * p.n_pgroups;
@@ -377,15 +384,15 @@ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem
   return w->n_rows > 0;
 }
 
-// Lists the non-empty work items by output row band, then most left rows
-// first (a counting sort): one block.  Every CTA of tc_kernel reads the same
+// Lists the non-empty work items by output row band (in the order
+// band_rank gives), then most left rows first (a counting sort): one block.  Every CTA of tc_kernel reads the same
 // list.  When
 // paired, the entries are item pairs (the two halves of the shifts, which
 // have the same rows): pair i holds items 2 i and 2 i + 1.
 __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long long n_total, int* __restrict__ items,
                                                         int* __restrict__ n_live) {
   const int step = p.paired ? 2 : 1;
-  // key = band * (chunk_rows + 1) + (chunk_rows - rows): band first, then
+  // key = rank * (chunk_rows + 1) + (chunk_rows - rows): band first, then
   // the longest items
   __shared__ int cnt[kMaxBands * (kMaxChunkRows + 1)];
   const int stride = p.chunk_rows + 1, n_keys = p.n_bands * stride;
@@ -393,7 +400,7 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   __syncthreads();
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
-    if (tc_item(p, idx * step, &w)) atomicAdd(&cnt[w.band * stride + p.chunk_rows - w.n_rows], 1);
+    if (tc_item(p, idx * step, &w)) atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -409,7 +416,7 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
     if (tc_item(p, idx * step, &w))
-      items[atomicAdd(&cnt[w.band * stride + p.chunk_rows - w.n_rows], 1)] = (int)idx;
+      items[atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1)] = (int)idx;
   }
 }
 
@@ -430,6 +437,12 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 // to the clusters when paired) in snake order, round r giving position
 // r*G + c or r*G + G-1-c; in a cluster, CTA rank h takes half h of the pair.
 __device__ __forceinline__ bool round_item(const TcParams& p, long long n_live, long long round, TcItem* w) {
+  if (p.sched != nullptr) {
+    const long long pos = round * gridDim.x + blockIdx.x;
+    if (pos >= n_live) return false;
+    const int e = p.sched[pos];
+    return e >= 0 && tc_item(p, e, w);
+  }
   const int cs = p.paired ? 2 : 1;
   const long long G = gridDim.x / cs, c = blockIdx.x / cs;
   const long long pos = round * G + ((round & 1) ? G - 1 - c : c);
@@ -1273,6 +1286,7 @@ struct TcWs {
   double* sums;     // n_left + n_right matrix sums
   double* sq;       // n_left + n_right sums of squares
   int* flush;       // n_left x n_pgroups accumulation windows
+  int* sched;       // banded launches: entry count + host-built schedule (n_items + 3 x SMs)
   float* CL;        // n_left x (Hl+1) x (Wl+1) summed-area tables of the centred matrices
   float* CR;        // n_right x (Hr+1) x (Wr+1)
   void* hi;         // n_right x Hr x pitch, BF16 or TF32-rounded FP32
@@ -1304,8 +1318,78 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   w.hi = take((size_t)t.es * plane);
   w.lo = take((size_t)t.es * plane);
   w.items = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items + 1)));  // list + its length
+  w.sched = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items + 3 * (size_t)sm_count() + 1)));
   w.bytes = off + 256;
   return w;
+}
+
+// Pinned staging for the host-built schedule, reused once its last copy has
+// run.
+struct SchedStage {
+  int* host = nullptr;
+  size_t cap = 0;
+  cudaEvent_t copied = nullptr;
+  ~SchedStage() {
+    if (host) cudaFreeHost(host);
+    if (copied) cudaEventDestroy(copied);
+  }
+};
+thread_local SchedStage t_stage;
+
+// Schedule of a banded launch.  The device work list deals its entries out in
+// a fixed snake order, which keeps the CTAs even only while neighbouring
+// entries are about equally long; sorted band by band, each band's short last
+// items sit beside the next band's long ones, and on 64 outputs of 511x511
+// the busiest CTA then carries 7% (two bands) to 16% (four or eight) more than
+// the mean.  Here the items, band by band and longest first, each go to the
+// CTA with the least work so far (cost: (left rows + 3) x active K-steps, the
+// 3 standing for an item's fixed drain), at most ceil(n / G) + 2 items per
+// CTA.  CTA c finds its r-th item at entry r * G + c (-1: none); entry 0 of
+// `region` holds the entry count, so the region needs n_items + 3 G + 1 ints.
+xc_status upload_band_schedule(const TcParams& prm, long long n_list, int G, int* region, cudaStream_t stream) {
+  struct Entry {
+    int rank, rows, idx, cost;
+  };
+  std::vector<Entry> es;
+  es.reserve((size_t)n_list);
+  for (long long idx = 0; idx < n_list; ++idx) {
+    TcItem w;
+    if (!tc_item(prm, idx, &w)) continue;
+    const int ks = __builtin_popcount(w.mask0) + __builtin_popcount(w.mask1);
+    es.push_back({prm.band_rank[w.band], w.n_rows, (int)idx, (w.n_rows + 3) * ks});
+  }
+  std::stable_sort(es.begin(), es.end(), [](const Entry& a, const Entry& b) {
+    return a.rank != b.rank ? a.rank < b.rank : a.rows > b.rows;
+  });
+  const long long n = (long long)es.size();
+  const int cap = (int)((n + G - 1) / G) + 2;
+  using Slot = std::pair<long long, int>;  // (work so far, CTA): the smallest first
+  std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> heap;
+  for (int c = 0; c < G; ++c) heap.push({0, c});
+  std::vector<int> count(G, 0), sched((size_t)G * cap, -1);
+  int rounds = 0;
+  for (const Entry& e : es) {
+    const Slot s = heap.top();  // never empty: G * cap >= n + 2G
+    heap.pop();
+    sched[(size_t)count[s.second] * G + s.second] = e.idx;
+    rounds = std::max(rounds, ++count[s.second]);
+    if (count[s.second] < cap) heap.push({s.first + e.cost, s.second});
+  }
+  const size_t n_ent = (size_t)rounds * G;
+  if (t_stage.copied == nullptr) XC_CUDA_TRY(cudaEventCreateWithFlags(&t_stage.copied, cudaEventDisableTiming));
+  XC_CUDA_TRY(cudaEventSynchronize(t_stage.copied));  // the previous copy has read the staging buffer
+  if (t_stage.cap < n_ent + 1) {
+    if (t_stage.host) XC_CUDA_TRY(cudaFreeHost(t_stage.host));
+    t_stage.host = nullptr;
+    t_stage.cap = 0;
+    XC_CUDA_TRY(cudaMallocHost(&t_stage.host, (n_ent + 1) * sizeof(int)));
+    t_stage.cap = n_ent + 1;
+  }
+  t_stage.host[0] = (int)n_ent;
+  std::copy(sched.begin(), sched.begin() + n_ent, t_stage.host + 1);
+  XC_CUDA_TRY(cudaMemcpyAsync(region, t_stage.host, (n_ent + 1) * sizeof(int), cudaMemcpyHostToDevice, stream));
+  XC_CUDA_TRY(cudaEventRecord(t_stage.copied, stream));
+  return XC_OK;
 }
 
 }  // namespace
@@ -1464,9 +1548,21 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
     prm.band_start[nb] = n_tiles_y;
     prm.n_bands = nb;
     prm.band_done = band_done;
+    // Bands with the most output rows are worked first: the copies still to
+    // run when the kernel ends are then the shortest ones.  (Equal work gives
+    // the edge bands far more rows, since the left rows per row-shift tile
+    // fall off towards both edges.)
+    int order[kMaxBands];
+    for (int k = 0; k < nb; ++k) order[k] = k;
+    const auto rows_out = [&](int k) {
+      return std::min(g.Sy, prm.band_start[k + 1] * t.DY) - std::min(g.Sy, prm.band_start[k] * t.DY);
+    };
+    std::stable_sort(order, order + nb, [&](int a, int b) { return rows_out(a) > rows_out(b); });
+    for (int r = 0; r < nb; ++r) prm.band_rank[order[r]] = r;
     if (bands) {
       bands->n = nb;
       for (int k = 0; k < nb; ++k) {
+        bands->order[k] = order[k];
         bands->items[k] = 0;
         for (int ty = prm.band_start[k]; ty < prm.band_start[k + 1]; ++ty) bands->items[k] += live_of[ty];
         bands->row_lo[k] = std::min(g.Sy, prm.band_start[k] * t.DY);
@@ -1475,12 +1571,7 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
     }
   }
 
-  // the work list: non-empty items (or pairs), most left rows first, built on the device
   if (t.n_items > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
-  prm.items = w.items;
-  prm.n_live = w.items + t.n_items;
-  worklist_kernel<<<1, 1024, 0, stream>>>(prm, n_list, w.items, w.items + t.n_items);
-  XC_CUDA_TRY(cudaGetLastError());
   // persistent: one CTA per SM (about 205 KB of shared memory and all 512 TMEM
   // columns each), walking the list in snake order
   auto kern = tf32 ? tc_kernel<true> : tc_kernel<false>;
@@ -1512,6 +1603,20 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
     blocks = std::max(1LL, std::min<long long>(n_list, sms));
   }
   cfg.gridDim = dim3((unsigned)blocks);
+  prm.items = w.items;
+  prm.sched = nullptr;
+  if (band_done) {
+    // banded: the host deals the items out to the CTAs by least work
+    if (blocks > sm_count()) return fail(XC_ERR_WORKSPACE, "banded launch wider than its schedule space");
+    XC_TRY(upload_band_schedule(prm, n_list, (int)blocks, w.sched, stream));
+    prm.n_live = w.sched;
+    prm.sched = w.sched + 1;
+  } else {
+    // the work list: non-empty items (or pairs), most left rows first, built on the device
+    prm.n_live = w.items + t.n_items;
+    worklist_kernel<<<1, 1024, 0, stream>>>(prm, n_list, w.items, w.items + t.n_items);
+    XC_CUDA_TRY(cudaGetLastError());
+  }
   const int slot = kernel_timer_begin(stream);
   XC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, mhi, mlo, prm));
   kernel_timer_end(slot, stream);

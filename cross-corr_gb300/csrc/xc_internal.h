@@ -140,6 +140,7 @@ struct TcBands {
   int n;
   long long items[8];
   int row_lo[8], row_hi[8];
+  int order[8];  // bands in the order the kernel works (and completes) them
 };
 xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
                               const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
