@@ -475,9 +475,9 @@ def config_studies(torch, xcorr, reps=20):
 
 def gpu_launches(method, steps):
     # kernels per xc_correlate call: direct 1; fft 2 pads + multiply + normalise
-    # (+ cuFFT's own); tc: 2 sums, mean, accumulation windows, 2 column sums, 2 row
-    # scans, split, correction, work list, tcgen05 kernel
-    per_step = {"direct": 1, "fft": 4, "tc_bf16x3": 12, "tc_tf32x3": 12}.get(method, 1)
+    # (+ cuFFT's own); tc: sums, means and accumulation windows, column sums,
+    # row scans (each over both sides), split, correction, work list, tcgen05 kernel
+    per_step = {"direct": 1, "fft": 4, "tc_bf16x3": 8, "tc_tf32x3": 8}.get(method, 1)
     return per_step * steps
 
 

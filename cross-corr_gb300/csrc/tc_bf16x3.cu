@@ -927,13 +927,32 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-// Matrix sums and sums of squares (means and spreads): grid (matrix, slice);
-// FP64 partial sums of a slice, block-reduced, added into sums[m] and sq[m]
-// (zeroed before the launch).
-__global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src, long long area, int slices,
-                                                  double* __restrict__ sums, double* __restrict__ sq) {
+// Matrices of one side (left or right) for the preparation kernels, which
+// take both sides in one launch: blocks [0, a_blocks) work on side a, the
+// rest on side b.
+struct PrepSide {
+  const float* src;  // the matrices, H x W each
+  int H, W;
+  long long area;    // H x W
+  int slices;        // sum_kernel blocks per matrix
+  double* sums;      // per-matrix sums and sums of squares
+  double* sq;
+  const float* mu;   // per-matrix means
+  float* sat;        // (H+1) x (W+1) summed-area table per matrix
+  long long sat_rows;  // matrices x (H+1)
+};
+
+// Matrix sums and sums of squares (means and spreads): blocks over (matrix,
+// slice); FP64 partial sums of a slice, block-reduced, added into sums[m]
+// and sq[m] (zeroed before the launch).
+__device__ __forceinline__ void sum_block(const PrepSide& sd_, int b) {
+  const float* __restrict__ src = sd_.src;
+  const long long area = sd_.area;
+  const int slices = sd_.slices;
+  double* __restrict__ sums = sd_.sums;
+  double* __restrict__ sq = sd_.sq;
   __shared__ double red[8], red2[8];
-  const int m = blockIdx.x / slices, sl = blockIdx.x % slices;
+  const int m = b / slices, sl = b % slices;
   const long long per = (area + slices - 1) / slices;
   const long long lo = sl * per, hi = min(area, lo + per);
   const float* a = src + (long long)m * area;
@@ -978,6 +997,13 @@ __global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src,
   }
 }
 
+__global__ void __launch_bounds__(256) sum_kernel(const PrepSide a, const PrepSide b, unsigned a_blocks) {
+  if (blockIdx.x < a_blocks)
+    sum_block(a, (int)blockIdx.x);
+  else
+    sum_block(b, (int)(blockIdx.x - a_blocks));
+}
+
 // Accumulation window (left rows between drains) per (left matrix, partner
 // group).  The tensor-core accumulation error grows with the window and with
 // the partial sums of the centred data relative to the result.  With
@@ -985,19 +1011,48 @@ __global__ void __launch_bounds__(256) sum_kernel(const float* __restrict__ src,
 // most 1, for zero-mean data), the centred partial sums are at most rho of
 // the result's scale even when they add coherently, so the window may be
 // 1/rho times the zero-mean one.  Largest rho over the group's partners.
-__global__ void flush_kernel(const float* __restrict__ mu, const float* __restrict__ sd, int n_left, PairMap pm,
-                             int n_pgroups, int P, int base_rows, int max_rows, int fixed, int* __restrict__ flush) {
-  // one warp per (left matrix, partner group), lanes over the partners
-  const long long i = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+// Mean and standard deviation of matrix m (FP64 from the sums; the variance
+// is a difference of nearly equal terms for data far from zero).
+struct MeanSd {
+  float mu, sd;
+};
+__device__ __forceinline__ MeanSd mean_sd(const double* __restrict__ sums, const double* __restrict__ sq, int m,
+                                          int n_left, double left_area, double right_area) {
+  const double area = m < n_left ? left_area : right_area;
+  const double mean = sums[m] / area;
+  return {(float)mean, (float)sqrt(fmax(0.0, sq[m] / area - mean * mean))};
+}
+
+// Blocks [0, mean_blocks) write the means and standard deviations of all
+// matrices; the others find the windows (from the same sums, so the values
+// agree bit for bit), one warp per (left matrix, partner group), lanes over
+// the partners.
+__global__ void __launch_bounds__(256) stats_kernel(const double* __restrict__ sums, const double* __restrict__ sq,
+                                                    int n_left, double left_area, int n_total, double right_area,
+                                                    float* __restrict__ mu, float* __restrict__ sd,
+                                                    unsigned mean_blocks, PairMap pm, int n_pgroups, int P,
+                                                    int base_rows, int max_rows, int fixed, int* __restrict__ flush) {
+  if (blockIdx.x < mean_blocks) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m < n_total) {
+      const MeanSd v = mean_sd(sums, sq, m, n_left, left_area, right_area);
+      mu[m] = v.mu;
+      sd[m] = v.sd;
+    }
+    return;
+  }
+  const long long i = ((blockIdx.x - mean_blocks) * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (i >= (long long)n_left * n_pgroups) return;  // warp-uniform
   const int l = (int)(i / n_pgroups), pg = (int)(i % n_pgroups);
-  const float ml = mu[l], sl = sd[l];
+  const MeanSd vl = mean_sd(sums, sq, l, n_left, left_area, right_area);
+  const float ml = vl.mu, sl = vl.sd;
   float rho = 0.0f;
   for (int k = pg * P + lane; k < min(pm.K, pg * P + P); k += 32) {
     const long long r = (long long)l * pm.r_l + (long long)k * pm.r_k + n_left;
-    const float den = fabsf(ml * mu[r]) + sl * sd[r];
-    if (den > 0.0f) rho = fmaxf(rho, sl * sd[r] / den);
+    const MeanSd vr = mean_sd(sums, sq, (int)r, n_left, left_area, right_area);
+    const float den = fabsf(ml * vr.mu) + sl * vr.sd;
+    if (den > 0.0f) rho = fmaxf(rho, sl * vr.sd / den);
   }
   for (int o = 16; o > 0; o >>= 1) rho = fmaxf(rho, __shfl_xor_sync(0xffffffffu, rho, o));
   int rows = max_rows;
@@ -1006,20 +1061,6 @@ __global__ void flush_kernel(const float* __restrict__ mu, const float* __restri
   else if (rho > 0.0f)
     rows = (int)fminf((float)max_rows, fmaxf((float)base_rows, base_rows / rho));
   if (lane == 0) flush[i] = max(1, rows);
-}
-
-// Means and standard deviations (FP64 from the sums; the variance is a
-// difference of nearly equal terms for data far from zero).
-__global__ void mean_kernel(const double* __restrict__ sums, const double* __restrict__ sq, int n_left,
-                            double left_area, int n_total, double right_area, float* __restrict__ mu,
-                            float* __restrict__ sd) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m < n_total) {
-    const double area = m < n_left ? left_area : right_area;
-    const double mean = sums[m] / area;
-    mu[m] = (float)mean;
-    sd[m] = (float)sqrt(fmax(0.0, sq[m] / area - mean * mean));
-  }
 }
 
 // Summed-area tables of the centred matrices fl32(M - mu) (the values the
@@ -1031,14 +1072,17 @@ __global__ void mean_kernel(const double* __restrict__ sums, const double* __res
 // 64-row chunk), which keeps every FP32 chain short.  One block per (matrix,
 // 32-column strip); each of its 8 warps loads 8 consecutive rows of a chunk
 // (coalesced, independent loads).
-__global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ src, int H, int W,
-                                                     const float* __restrict__ mu, float* __restrict__ C) {
+__device__ __forceinline__ void colsum_block(const PrepSide& sd_, int b) {
+  const float* __restrict__ src = sd_.src;
+  const int H = sd_.H, W = sd_.W;
+  const float* __restrict__ mu = sd_.mu;
+  float* __restrict__ C = sd_.sat;
   __shared__ float seg[8][32];
   __shared__ float carry[32];
   const int strips = (W + 31) / 32;
-  const int m = blockIdx.x / strips;
+  const int m = b / strips;
   const int lane = threadIdx.x & 31;
-  const int x = (blockIdx.x % strips) * 32 + lane;
+  const int x = (b % strips) * 32 + lane;
   const int w = threadIdx.x >> 5;
   const float* a = src + (long long)m * H * W;
   float* c = C + (long long)m * (H + 1) * (W + 1) + 1;  // column x of C is column x + 1 of S
@@ -1074,6 +1118,14 @@ __global__ void __launch_bounds__(256) colsum_kernel(const float* __restrict__ s
     }
     __syncthreads();
   }
+}
+
+// One block per (matrix, 32-column strip) of either side.
+__global__ void __launch_bounds__(256) colsum_kernel(const PrepSide a, const PrepSide b, unsigned a_blocks) {
+  if (blockIdx.x < a_blocks)
+    colsum_block(a, (int)blockIdx.x);
+  else
+    colsum_block(b, (int)(blockIdx.x - a_blocks));
 }
 
 // Splits the centred right matrices fl32(R - mu_R) into hi/lo planes with a
@@ -1135,71 +1187,140 @@ __global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ sr
 // row, 8 rows per block) becomes its inclusive prefix sum over x, S[y][0] = 0.
 // The warp scans 32 consecutive columns at a time (coalesced), carrying the
 // running total (FP32 chains of at most W/32 + 5 terms).
-__global__ void __launch_bounds__(256) rowscan_kernel(float* __restrict__ S, long long n_rows, int W) {
+__global__ void __launch_bounds__(256) rowscan_kernel(const PrepSide a, const PrepSide b, unsigned a_blocks) {
+  const bool first = blockIdx.x < a_blocks;
+  const PrepSide& sd_ = first ? a : b;
+  float* __restrict__ S = sd_.sat;
+  const long long n_rows = sd_.sat_rows;
+  const int W = sd_.W;
   const int lane = threadIdx.x & 31;
-  const long long row = blockIdx.x * 8LL + (threadIdx.x >> 5);
+  const long long row = (first ? blockIdx.x : blockIdx.x - a_blocks) * 8LL + (threadIdx.x >> 5);
   if (row >= n_rows) return;  // warp-uniform
   float* q = S + row * (W + 1) + 1;
   if (lane == 0) q[-1] = 0.0f;
   float carry = 0.0f;
-  for (int c = 0; c < W; c += 32) {
-    float v = c + lane < W ? q[c + lane] : 0.0f;
+  for (int c0 = 0; c0 < W; c0 += 256) {
+    // eight 32-column chunks loaded together (the scan is latency-bound)
+    float v[8];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const float u = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += u;
+    for (int u = 0; u < 8; ++u) v[u] = c0 + 32 * u + lane < W ? q[c0 + 32 * u + lane] : 0.0f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const float y = __shfl_up_sync(0xffffffffu, v[u], o);
+        if (lane >= o) v[u] += y;
+      }
+      v[u] += carry;
+      if (c0 + 32 * u + lane < W) q[c0 + 32 * u + lane] = v[u];
+      carry = __shfl_sync(0xffffffffu, v[u], 31);
     }
-    v += carry;
-    if (c + lane < W) q[c + lane] = v;
-    carry = __shfl_sync(0xffffffffu, v, 31);
   }
 }
 
 // out[o][sy][sx] = mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area over the
 // overlap of shift (sy, sx), where S' are sums of the centred matrices over
-// the overlap, four summed-area-table reads each; one warp per output row
-// (8 rows per block), consecutive lanes on consecutive shifts.  FP32 (the
-// centred sums are small, and the result's rounding stays near 1e-7 of
-// max|out|).
+// the overlap, read from the summed-area tables.  A block covers 8 output
+// rows.  Along a row the overlap's rows y0..y1 are fixed, so each warp first
+// stages its row's table-row differences D_L[x] = S_L[y1][x] - S_L[y0][x]
+// and D_R likewise in shared memory (four coalesced table rows instead of
+// eight table reads per shift; 16 loads in flight per lane).  Then each
+// thread takes one shift column sx (the overlap's columns x0..x1 depend on
+// sx alone) through the block's 8 rows: S'_L = D_L[x1] - D_L[x0], S'_R =
+// D_R[x1 - dx] - D_R[x0 - dx].  The kernel writes every output once and is
+// bound by instruction issue, hence the column-wise reuse of the index
+// arithmetic.  FP32 (the centred sums are small, and the result's rounding
+// stays near 1e-7 of max|out|).
+constexpr int kCorrLeft = 516, kCorrRight = 260;  // staged widths: Wl + 1 <= 513, Wr + 1 <= 257
+constexpr int kCorrStage = kCorrLeft + kCorrRight;
 __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out, const float* __restrict__ SL,
                                                          const float* __restrict__ SR,
                                                          const float* __restrict__ mu_l,
                                                          const float* __restrict__ mu_r, int Hl, int Wl, int Hr,
                                                          int Wr, int Sy, int Sx, long long n_rows, PairMap pm) {
+  __shared__ float stage[8][kCorrStage];  // per row: D_L in [0, Wl], D_R in [Wl + 1, Wl + Wr + 1]
+  __shared__ float coef[8][4];            // per row: mu_L, mu_R, mu_L mu_R, overlap rows
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long long row = blockIdx.x * 8LL + wid;  // o * Sy + sy
-  if (row >= n_rows) return;  // warp-uniform
-  const long long o = row / Sy;
-  const int sy = (int)(row % Sy);
-  // invert o = l*o_l + k*o_k for the three pair-map forms
-  long long l, k;
-  if (pm.o_l == 0) {  // one_to_one / one_to_many: o = k
-    l = 0;
-    k = o;
-  } else if (pm.o_k == 1 && pm.o_l == pm.K) {  // n_to_m: o = l*K + k
-    l = o / pm.K;
-    k = o % pm.K;
-  } else {  // n_to_mn: o = l + k*n
-    l = o % pm.n_left;
-    k = o / pm.n_left;
+  const long long row0 = blockIdx.x * 8LL;
+  const long long row = row0 + wid;  // o * Sy + sy
+  if (row < n_rows) {                // warp-uniform
+    const long long o = row / Sy;
+    const int sy = (int)(row % Sy);
+    // invert o = l*o_l + k*o_k for the three pair-map forms
+    long long l, k;
+    if (pm.o_l == 0) {  // one_to_one / one_to_many: o = k
+      l = 0;
+      k = o;
+    } else if (pm.o_k == 1 && pm.o_l == pm.K) {  // n_to_m: o = l*K + k
+      l = o / pm.K;
+      k = o % pm.K;
+    } else {  // n_to_mn: o = l + k*n
+      l = o % pm.n_left;
+      k = o / pm.n_left;
+    }
+    const long long r = l * pm.r_l + k * pm.r_k;
+    const int dy = sy - (Hr - 1);
+    const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
+    const float* l0 = SL + (l * (Hl + 1) + y0) * (long long)(Wl + 1);
+    const float* l1 = SL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
+    const float* r0 = SR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
+    const float* r1 = SR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
+    float* st = stage[wid];
+    const int nl = Wl + 1, nt = Wl + Wr + 2;
+    for (int t0 = 0; t0 < nt; t0 += 256) {
+      float a[8], b[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int t = t0 + 32 * u + lane;
+        a[u] = 0.0f;
+        b[u] = 0.0f;
+        if (t < nl) {
+          a[u] = __ldg(l1 + t);
+          b[u] = __ldg(l0 + t);
+        } else if (t < nt) {
+          a[u] = __ldg(r1 + (t - nl));
+          b[u] = __ldg(r0 + (t - nl));
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int t = t0 + 32 * u + lane;
+        if (t < nt) st[t] = a[u] - b[u];
+      }
+    }
+    if (lane == 0) {
+      const float ml = mu_l[l], mr = mu_r[r];
+      coef[wid][0] = ml;
+      coef[wid][1] = mr;
+      coef[wid][2] = ml * mr;
+      coef[wid][3] = (float)(y1 - y0);
+    }
   }
-  const long long r = l * pm.r_l + k * pm.r_k;
-  const int dy = sy - (Hr - 1);
-  const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
-  const float* l0 = SL + (l * (Hl + 1) + y0) * (long long)(Wl + 1);
-  const float* l1 = SL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
-  const float* r0 = SR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
-  const float* r1 = SR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
-  const float ml = mu_l[l], mr = mu_r[r];
-  const float mlr = ml * mr;
-  const float rows = (float)(y1 - y0);
-  float* orow = out + row * Sx;
-  for (int sx = lane; sx < Sx; sx += 32) {
+  __syncthreads();
+  const int n_here = (int)min(8LL, n_rows - row0);
+  float cl[8], cr[8], clr[8], cy[8];
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    cl[w] = coef[w][0];
+    cr[w] = coef[w][1];
+    clr[w] = coef[w][2];
+    cy[w] = coef[w][3];
+  }
+  for (int sx = threadIdx.x; sx < Sx; sx += 256) {
     const int dx = sx - (Wr - 1);
     const int x0 = max(0, dx), x1 = min(Wl, Wr + dx);
-    const float sl = (__ldg(l1 + x1) - __ldg(l0 + x1)) - (__ldg(l1 + x0) - __ldg(l0 + x0));
-    const float sr = (__ldg(r1 + x1 - dx) - __ldg(r0 + x1 - dx)) - (__ldg(r1 + x0 - dx) - __ldg(r0 + x0 - dx));
-    orow[sx] = fmaf(mr, sl, fmaf(ml, sr, mlr * (rows * (float)(x1 - x0))));
+    const int j1 = Wl + 1 + x1 - dx, j0 = Wl + 1 + x0 - dx;
+    const float width = (float)(x1 - x0);
+    float* o = out + row0 * Sx + sx;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      if (w < n_here) {
+        const float* st = stage[w];
+        const float sl = st[x1] - st[x0];
+        const float sr = st[j1] - st[j0];
+        o[(long long)w * Sx] = fmaf(cr[w], sl, fmaf(cl[w], sr, clr[w] * (cy[w] * width)));
+      }
+    }
   }
 }
 
@@ -1255,7 +1376,7 @@ int env_int(const char* name, int def) {
 // chunk of a right row: 4 K-steps x 3 products) per accumulator.  Measured on
 // zero-mean 256x256 data: windows of 5 rows (240 MMAs) 6.0e-6 of max|out|,
 // 8 rows 8e-6, 12 rows 1.1e-5, 32 rows 3e-5 (the split alone gives ~6e-6).
-// flush_kernel widens it for data whose means dominate.  Every drain stalls
+// stats_kernel widens it for data whose means dominate.  Every drain stalls
 // the MMAs while the epilogue reads the accumulators.
 // XC_TC_FLUSH_ROWS fixes the window, XC_TC_CHUNK_ROWS the item length (studies).
 int flush_rows(int nkc) { return std::max(1, std::min(32, 240 / (12 * nkc))); }
@@ -1418,31 +1539,26 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   // 1. per-matrix means, 2. column prefix sums of the centred matrices
   {
     const long long la = (long long)g.Hl * g.Wl, ra = (long long)g.Hr * g.Wr;
-    // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
-    const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
+    // slices of at most 2048 elements (a thread adds at most 8 terms in FP32):
+    // enough blocks to fill every SM, each thread's loads all in flight
+    const int ls = (int)((la + 2047) / 2048), rs = (int)((ra + 2047) / 2048);
+    const PrepSide sl{left,  g.Hl, g.Wl, la, ls, w.sums,      w.sq,      w.mu,      w.CL, (long long)nl * (g.Hl + 1)};
+    const PrepSide sr{right, g.Hr, g.Wr, ra, rs, w.sums + nl, w.sq + nl, w.mu + nl, w.CR, (long long)nr * (g.Hr + 1)};
     XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, 2 * sizeof(double) * (nl + nr), stream));
-    sum_kernel<<<(unsigned)(nl * ls), 256, 0, stream>>>(left, la, ls, w.sums, w.sq);
-    XC_CUDA_TRY(cudaGetLastError());
-    sum_kernel<<<(unsigned)(nr * rs), 256, 0, stream>>>(right, ra, rs, w.sums + nl, w.sq + nl);
-    XC_CUDA_TRY(cudaGetLastError());
-    mean_kernel<<<(unsigned)((nl + nr + 255) / 256), 256, 0, stream>>>(w.sums, w.sq, nl, (double)la,
-                                                                        (int)(nl + nr), (double)ra, w.mu, w.sd);
+    sum_kernel<<<(unsigned)(nl * ls + nr * rs), 256, 0, stream>>>(sl, sr, (unsigned)(nl * ls));
     XC_CUDA_TRY(cudaGetLastError());
     const int npg = div_up(pm.K, t.P);
-    flush_kernel<<<(unsigned)((32LL * nl * npg + 255) / 256), 256, 0, stream>>>(
-        w.mu, w.sd, nl, pm, npg, t.P, flush_rows(t.nkc), t.chunk_rows, flush_fixed(), w.flush);
+    const unsigned mean_blocks = (unsigned)((nl + nr + 255) / 256);
+    stats_kernel<<<(unsigned)(mean_blocks + (32LL * nl * npg + 255) / 256), 256, 0, stream>>>(
+        w.sums, w.sq, nl, (double)la, (int)(nl + nr), (double)ra, w.mu, w.sd, mean_blocks, pm, npg, t.P,
+        flush_rows(t.nkc), t.chunk_rows, flush_fixed(), w.flush);
     XC_CUDA_TRY(cudaGetLastError());
-  }
-  colsum_kernel<<<(unsigned)(nl * ((g.Wl + 31) / 32)), 256, 0, stream>>>(left, g.Hl, g.Wl, w.mu, w.CL);
-  XC_CUDA_TRY(cudaGetLastError());
-  colsum_kernel<<<(unsigned)(nr * ((g.Wr + 31) / 32)), 256, 0, stream>>>(right, g.Hr, g.Wr, w.mu + nl, w.CR);
-  XC_CUDA_TRY(cudaGetLastError());
-  {
+    const unsigned lc = (unsigned)(nl * ((g.Wl + 31) / 32));
+    colsum_kernel<<<(unsigned)(lc + nr * ((g.Wr + 31) / 32)), 256, 0, stream>>>(sl, sr, lc);
+    XC_CUDA_TRY(cudaGetLastError());
     // second pass: every row of the left and of the right tables
-    const long long lrows = (long long)nl * (g.Hl + 1), rrows = nr * (g.Hr + 1);
-    rowscan_kernel<<<(unsigned)((lrows + 7) / 8), 256, 0, stream>>>(w.CL, lrows, g.Wl);
-    XC_CUDA_TRY(cudaGetLastError());
-    rowscan_kernel<<<(unsigned)((rrows + 7) / 8), 256, 0, stream>>>(w.CR, rrows, g.Wr);
+    const unsigned lb = (unsigned)((sl.sat_rows + 7) / 8);
+    rowscan_kernel<<<(unsigned)(lb + (sr.sat_rows + 7) / 8), 256, 0, stream>>>(sl, sr, lb);
     XC_CUDA_TRY(cudaGetLastError());
   }
   // 3. split of the centred right matrices
@@ -1460,6 +1576,7 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   }
   // 4. the mean terms initialise the output
   {
+    if (g.Wl + 1 > kCorrLeft || g.Wr + 1 > kCorrRight) return fail(XC_ERR_UNSUPPORTED, "correction widths");
     const long long n_rows = (long long)n_out * g.Sy;
     correction_kernel<<<(unsigned)((n_rows + 7) / 8), 256, 0, stream>>>(
         out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, n_rows, pm);
