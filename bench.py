@@ -299,6 +299,11 @@ def run_ours(args, rank, world, local_rank):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = t.item()
     e2e_err = float(np.abs(ho.numpy()[:2].astype(np.float64) - out[:2].cpu().numpy()).max())
+    # the host-buffer call may cut the work differently (output bands): the
+    # same accuracy gate as the device-resident output
+    gate_e2e, _, _ = accuracy_gate(ho.cuda(), left, right, torch, xcorr)
+    if gate_e2e > GATE:
+        raise SystemExit(f"accuracy gate failed on the host-buffer output: {gate_e2e:.3e} > {GATE}")
 
     peaks, peak_src = measured_peaks()
     flops = algorithmic_flops(left.shape, right.shape, pairs)
@@ -327,7 +332,8 @@ def run_ours(args, rank, world, local_rank):
                      "vs_cpu_oracle_2_outputs": gate_oracle, "gate": GATE},
         "e2e": {"value": pairs * world / e2e_s, "unit": "correlations/s",
                 "h2d_bytes_per_step": int(left.nbytes + right.nbytes), "d2h_bytes_per_step": int(ho.numel() * 4),
-                "api": "xc_correlate_host (pinned host buffers)", "max_abs_diff_vs_device_run": e2e_err},
+                "api": "xc_correlate_host (pinned host buffers)", "max_abs_diff_vs_device_run": e2e_err,
+                "max_rel_err_vs_fp64": gate_e2e},
         "roofline": {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
                      # a split product costs 3 tensor-core products: the split path's ceiling is peak / 3
                      "split_products": 3 if method.startswith("tc_") else None,

@@ -151,8 +151,11 @@ struct TcParams {
   int band_rank[kMaxBands];  // place of each band in the work list (a permutation of 0..n_bands-1)
   int* band_done;
   // Host-built schedule (banded launches), or null: CTA c takes entry
-  // r * gridDim.x + c in round r (-1: nothing), *n_live entries in all.
-  const int* sched;
+  // r * gridDim.x + c in round r, *n_live entries in all.  An entry is
+  // {tile key, first left row (from the tile's first), left rows, 0}, the
+  // tile key (rank * per_rank + lp) * n_halves + half as in tc_item; key -1:
+  // nothing.
+  const int4* sched;
   const int* n_live; // entries of `items` (written on the device)
   int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
   DeviceFlags* flags;
@@ -357,21 +360,18 @@ struct TcItem {
 
 // idx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_halves + half;
 // false when the item has no left rows.
-__host__ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
-  const int half = (int)(idx % p.n_halves);
-  const long long bid = idx / p.n_halves;
-  const int per_rank = p.pm.n_left * p.n_pgroups;
-  const int lp = (int)(bid % per_rank);
-  const int rank = (int)((bid / per_rank) % p.n_dytiles);
-  const int chunk = (int)(bid / ((long long)per_rank * p.n_dytiles));
+// The item of tile key (rank, lp, half) covering the tile's left rows
+// [row0, row0 + n) (clipped to the tile); false when that is empty.
+__host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int half, int lp, int rank, int row0, int n,
+                                                  TcItem* w) {
   w->l = lp / p.n_pgroups;
   w->p0 = (lp % p.n_pgroups) * p.P;
   const int t = centre_out(rank, p.n_dytiles, (p.Hr - 1) / p.DY);
   w->dy0 = -(p.Hr - 1) + t * p.DY;
   const int tile_lo = max(0, w->dy0);
   const int tile_hi = min(p.Hl, w->dy0 + p.DY - 1 + p.Hr);
-  w->a_lo = tile_lo + chunk * p.chunk_rows;
-  const int a_hi = min(tile_hi, w->a_lo + p.chunk_rows);
+  w->a_lo = tile_lo + row0;
+  const int a_hi = min(tile_hi, w->a_lo + n);
   w->n_rows = a_hi - w->a_lo;
   w->rdim2 = p.pm.r_l != 0 ? w->l : 0;
   w->s0_0 = 256 * half;
@@ -382,6 +382,24 @@ __host__ __device__ __forceinline__ bool tc_item(const TcParams& p, long long id
   while (b + 1 < p.n_bands && t >= p.band_start[b + 1]) ++b;
   w->band = b;
   return w->n_rows > 0;
+}
+
+__host__ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
+  const int half = (int)(idx % p.n_halves);
+  const long long bid = idx / p.n_halves;
+  const int per_rank = p.pm.n_left * p.n_pgroups;
+  const int lp = (int)(bid % per_rank);
+  const int rank = (int)((bid / per_rank) % p.n_dytiles);
+  const int chunk = (int)(bid / ((long long)per_rank * p.n_dytiles));
+  return tc_piece(p, half, lp, rank, chunk * p.chunk_rows, p.chunk_rows, w);
+}
+
+// An entry of the host-built schedule.
+__host__ __device__ __forceinline__ bool tc_entry(const TcParams& p, int4 e, TcItem* w) {
+  if (e.x < 0) return false;
+  const int per_rank = p.pm.n_left * p.n_pgroups;
+  const int half = e.x % p.n_halves, bid = e.x / p.n_halves;
+  return tc_piece(p, half, bid % per_rank, bid / per_rank, e.y, e.z, w);
 }
 
 // Lists the non-empty work items by output row band (in the order
@@ -439,9 +457,7 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 __device__ __forceinline__ bool round_item(const TcParams& p, long long n_live, long long round, TcItem* w) {
   if (p.sched != nullptr) {
     const long long pos = round * gridDim.x + blockIdx.x;
-    if (pos >= n_live) return false;
-    const int e = p.sched[pos];
-    return e >= 0 && tc_item(p, e, w);
+    return pos < n_live && tc_entry(p, p.sched[pos], w);
   }
   const int cs = p.paired ? 2 : 1;
   const long long G = gridDim.x / cs, c = blockIdx.x / cs;
@@ -1407,7 +1423,7 @@ struct TcWs {
   double* sums;     // n_left + n_right matrix sums
   double* sq;       // n_left + n_right sums of squares
   int* flush;       // n_left x n_pgroups accumulation windows
-  int* sched;       // banded launches: entry count + host-built schedule (n_items + 3 x SMs)
+  int* sched;       // banded launches: entry count (16 bytes), then the schedule (3 n_items + 3 x SMs int4s)
   float* CL;        // n_left x (Hl+1) x (Wl+1) summed-area tables of the centred matrices
   float* CR;        // n_right x (Hr+1) x (Wr+1)
   void* hi;         // n_right x Hr x pitch, BF16 or TF32-rounded FP32
@@ -1439,7 +1455,7 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   w.hi = take((size_t)t.es * plane);
   w.lo = take((size_t)t.es * plane);
   w.items = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items + 1)));  // list + its length
-  w.sched = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items + 3 * (size_t)sm_count() + 1)));
+  w.sched = reinterpret_cast<int*>(take(16 * (1 + 3 * (size_t)t.n_items + 3 * (size_t)sm_count())));
   w.bytes = off + 256;
   return w;
 }
@@ -1447,7 +1463,7 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
 // Pinned staging for the host-built schedule, reused once its last copy has
 // run.
 struct SchedStage {
-  int* host = nullptr;
+  int4* host = nullptr;
   size_t cap = 0;
   cudaEvent_t copied = nullptr;
   ~SchedStage() {
@@ -1462,22 +1478,64 @@ thread_local SchedStage t_stage;
 // entries are about equally long; sorted band by band, each band's short last
 // items sit beside the next band's long ones, and on 64 outputs of 511x511
 // the busiest CTA then carries 7% (two bands) to 16% (four or eight) more than
-// the mean.  Here the items, band by band and longest first, each go to the
+// the mean.  With about 8 items per CTA, even assigning each item to the CTA
+// with the least work so far leaves 6% (the last band's items are all alike,
+// with nothing small left to fill the gaps).  So each band's rows are cut
+// afresh: the band's work W (left rows over all tile keys) into about G * m
+// equal pieces, m = ceil(W / (G * chunk_rows)), a piece at least half of
+// chunk_rows and at most chunk_rows rows, every tile key's rows into near-equal
+// pieces.  Then the pieces, band by band and longest first, each go to the
 // CTA with the least work so far (cost: (left rows + 3) x active K-steps, the
-// 3 standing for an item's fixed drain), at most ceil(n / G) + 2 items per
-// CTA.  CTA c finds its r-th item at entry r * G + c (-1: none); entry 0 of
-// `region` holds the entry count, so the region needs n_items + 3 G + 1 ints.
-xc_status upload_band_schedule(const TcParams& prm, long long n_list, int G, int* region, cudaStream_t stream) {
+// 3 standing for an item's fixed drain), at most ceil(n / G) + 2 per CTA.
+// CTA c finds its r-th entry at r * G + c.  Pieces per tile key are at most
+// 2 ceil(rows / chunk_rows) + 1, so n <= 3 n_items and the entries fit in
+// 3 n_items + 3 G.  `band_items` receives the pieces per band (what the
+// epilogue counts).
+xc_status upload_band_schedule(const TcParams& prm, int G, int* region, long long* band_items,
+                               cudaStream_t stream) {
   struct Entry {
-    int rank, rows, idx, cost;
+    int rank, rows, cost;
+    int4 e;
   };
+  const int per_rank = prm.pm.n_left * prm.n_pgroups;
+  const int tc = (prm.Hr - 1) / prm.DY;
+  // left rows of each row-shift tile (by visiting rank) and each band's work
+  std::vector<int> rows_of(prm.n_dytiles), band_of(prm.n_dytiles);
+  std::vector<double> work(prm.n_bands, 0.0);
+  for (int rank = 0; rank < prm.n_dytiles; ++rank) {
+    const int t = centre_out(rank, prm.n_dytiles, tc);
+    const int dy0 = -(prm.Hr - 1) + t * prm.DY;
+    rows_of[rank] = std::max(0, std::min(prm.Hl, dy0 + prm.DY - 1 + prm.Hr) - std::max(0, dy0));
+    int b = 0;
+    while (b + 1 < prm.n_bands && t >= prm.band_start[b + 1]) ++b;
+    band_of[rank] = b;
+    work[b] += (double)rows_of[rank] * per_rank * prm.n_halves;
+  }
+  std::vector<double> target(prm.n_bands);
+  for (int b = 0; b < prm.n_bands; ++b) {
+    const double m = std::max(1.0, std::ceil(work[b] / ((double)G * prm.chunk_rows)));
+    target[b] = std::max(0.5 * prm.chunk_rows, work[b] / (G * m));
+  }
+  const int ks[2] = {__builtin_popcount(tile_mask(0, prm)) + __builtin_popcount(tile_mask(128, prm)),
+                     __builtin_popcount(tile_mask(256, prm)) + __builtin_popcount(tile_mask(384, prm))};
   std::vector<Entry> es;
-  es.reserve((size_t)n_list);
-  for (long long idx = 0; idx < n_list; ++idx) {
-    TcItem w;
-    if (!tc_item(prm, idx, &w)) continue;
-    const int ks = __builtin_popcount(w.mask0) + __builtin_popcount(w.mask1);
-    es.push_back({prm.band_rank[w.band], w.n_rows, (int)idx, (w.n_rows + 3) * ks});
+  for (int b = 0; b < prm.n_bands; ++b) band_items[b] = 0;
+  for (int rank = 0; rank < prm.n_dytiles; ++rank) {
+    const int rows = rows_of[rank], b = band_of[rank];
+    if (rows <= 0) continue;
+    const int np = std::max((rows + prm.chunk_rows - 1) / prm.chunk_rows,
+                            std::max(1, (int)std::lround(rows / target[b])));
+    for (int lp = 0; lp < per_rank; ++lp)
+      for (int half = 0; half < prm.n_halves; ++half) {
+        const int key = (rank * per_rank + lp) * prm.n_halves + half;
+        int row0 = 0;
+        for (int q = 0; q < np; ++q) {
+          const int n = rows / np + (q < rows % np ? 1 : 0);
+          es.push_back({prm.band_rank[b], n, (n + 3) * ks[half], make_int4(key, row0, n, 0)});
+          row0 += n;
+          ++band_items[b];
+        }
+      }
   }
   std::stable_sort(es.begin(), es.end(), [](const Entry& a, const Entry& b) {
     return a.rank != b.rank ? a.rank < b.rank : a.rows > b.rows;
@@ -1487,12 +1545,13 @@ xc_status upload_band_schedule(const TcParams& prm, long long n_list, int G, int
   using Slot = std::pair<long long, int>;  // (work so far, CTA): the smallest first
   std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> heap;
   for (int c = 0; c < G; ++c) heap.push({0, c});
-  std::vector<int> count(G, 0), sched((size_t)G * cap, -1);
+  std::vector<int> count(G, 0);
+  std::vector<int4> sched((size_t)G * cap, make_int4(-1, 0, 0, 0));
   int rounds = 0;
   for (const Entry& e : es) {
     const Slot s = heap.top();  // never empty: G * cap >= n + 2G
     heap.pop();
-    sched[(size_t)count[s.second] * G + s.second] = e.idx;
+    sched[(size_t)count[s.second] * G + s.second] = e.e;
     rounds = std::max(rounds, ++count[s.second]);
     if (count[s.second] < cap) heap.push({s.first + e.cost, s.second});
   }
@@ -1503,12 +1562,12 @@ xc_status upload_band_schedule(const TcParams& prm, long long n_list, int G, int
     if (t_stage.host) XC_CUDA_TRY(cudaFreeHost(t_stage.host));
     t_stage.host = nullptr;
     t_stage.cap = 0;
-    XC_CUDA_TRY(cudaMallocHost(&t_stage.host, (n_ent + 1) * sizeof(int)));
+    XC_CUDA_TRY(cudaMallocHost(&t_stage.host, (n_ent + 1) * sizeof(int4)));
     t_stage.cap = n_ent + 1;
   }
-  t_stage.host[0] = (int)n_ent;
+  t_stage.host[0] = make_int4((int)n_ent, 0, 0, 0);
   std::copy(sched.begin(), sched.begin() + n_ent, t_stage.host + 1);
-  XC_CUDA_TRY(cudaMemcpyAsync(region, t_stage.host, (n_ent + 1) * sizeof(int), cudaMemcpyHostToDevice, stream));
+  XC_CUDA_TRY(cudaMemcpyAsync(region, t_stage.host, (n_ent + 1) * sizeof(int4), cudaMemcpyHostToDevice, stream));
   XC_CUDA_TRY(cudaEventRecord(t_stage.copied, stream));
   return XC_OK;
 }
@@ -1539,9 +1598,10 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   // 1. per-matrix means, 2. column prefix sums of the centred matrices
   {
     const long long la = (long long)g.Hl * g.Wl, ra = (long long)g.Hr * g.Wr;
-    // slices of at most 2048 elements (a thread adds at most 8 terms in FP32):
-    // enough blocks to fill every SM, each thread's loads all in flight
-    const int ls = (int)((la + 2047) / 2048), rs = (int)((ra + 2047) / 2048);
+    // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
+    // (2048-element slices took 19 us instead of 10 at 64 x 256x256: the
+    // blocks' FP64 atomics on one matrix's sum serialise)
+    const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
     const PrepSide sl{left,  g.Hl, g.Wl, la, ls, w.sums,      w.sq,      w.mu,      w.CL, (long long)nl * (g.Hl + 1)};
     const PrepSide sr{right, g.Hr, g.Wr, ra, rs, w.sums + nl, w.sq + nl, w.mu + nl, w.CR, (long long)nr * (g.Hr + 1)};
     XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, 2 * sizeof(double) * (nl + nr), stream));
@@ -1725,9 +1785,12 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   if (band_done) {
     // banded: the host deals the items out to the CTAs by least work
     if (blocks > sm_count()) return fail(XC_ERR_WORKSPACE, "banded launch wider than its schedule space");
-    XC_TRY(upload_band_schedule(prm, n_list, (int)blocks, w.sched, stream));
+    long long band_items[kMaxBands];
+    XC_TRY(upload_band_schedule(prm, (int)blocks, w.sched, band_items, stream));
     prm.n_live = w.sched;
-    prm.sched = w.sched + 1;
+    prm.sched = reinterpret_cast<const int4*>(w.sched) + 1;
+    if (bands)
+      for (int k = 0; k < prm.n_bands; ++k) bands->items[k] = band_items[k];
   } else {
     // the work list: non-empty items (or pairs), most left rows first, built on the device
     prm.n_live = w.items + t.n_items;

@@ -264,7 +264,11 @@ def test_host_buffer_entry_point_banded(mode, n_l, n_r, side, bands, method, mon
     right = seeded((n_r, side - 7, side + 5), 52)
     out = xcorr.correlate_host(mode, left, right, method=method)
     ref = xcorr.correlate(mode, dev(left), dev(right), method=method).cpu().numpy()
-    # the banded work list visits the items in another order: same products,
-    # another order of the reductions into the output
-    assert rel_to_max(out, ref) <= 1e-6
-    assert rel_to_max(out, oracle.run_mode(mode, left, right, dtype="f32acc64", threads=8)) <= 1e-5
+    # a banded launch cuts each band's left rows into pieces of its own (other
+    # drain points, another order of the reductions into the output): the
+    # same products summed in another order, so the two runs agree to a few
+    # FP32 roundings of the partial sums, and each meets the 1e-5 gate
+    assert rel_to_max(out, ref) <= 4e-6
+    exact = oracle.run_mode(mode, left, right, dtype="f32acc64", threads=8)
+    assert rel_to_max(out, exact) <= 1e-5
+    assert rel_to_max(ref, exact) <= 1e-5
