@@ -82,6 +82,7 @@
 
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <mutex>
 #include <queue>
 #include <string>
@@ -89,6 +90,7 @@
 #include <vector>
 
 #include "xc_common.cuh"
+#include "tc_schedule.h"
 #include "xc_internal.h"
 
 namespace xc {
@@ -110,7 +112,6 @@ constexpr int kThreads = 32 * (2 + (kIssuers - 1) + kBuilderWarps + kEpiWarps);
 constexpr int kXLen = 520;              // staged row elements: the 511 a two-tile item reads, padded
 constexpr int kBarBytes = 256;          // 20 mbarriers at most, the abort flag, the TMEM address slot
 constexpr int kMaxChunkRows = 1024;     // left rows per work item at most
-constexpr int kMaxBands = 8;            // output row bands signalled as they complete
 
 // Per operand type: right-tile stages and the Toeplitz buffer (hi or lo part
 // of one left row): 64 core matrices of 8 BF16 or 128 of 4 FP32.
@@ -324,17 +325,6 @@ __device__ __forceinline__ bool bar_red_or(bool v, int id, int nthreads) {
       : "r"((uint32_t)v), "r"(id), "r"(nthreads)
       : "memory");
   return r != 0;
-}
-
-// dy-tile visiting order: centre (heaviest overlap) first, then alternating
-// outwards, so long tiles start early.
-__host__ __device__ __forceinline__ int centre_out(int r, int n, int tc) {
-  const int below = tc, above = n - tc - 1;
-  const int m = below < above ? below : above;
-  if (r == 0) return tc;
-  if (r <= 2 * m) return (r & 1) ? tc + (r + 1) / 2 : tc - r / 2;
-  const int extra = r - 2 * m;
-  return above > below ? tc + m + extra : tc - m - extra;
 }
 
 // Active K-steps of a 128-shift tile starting at s0: bit j is set when
@@ -1473,89 +1463,35 @@ struct SchedStage {
 };
 thread_local SchedStage t_stage;
 
-// Schedule of a banded launch.  The device work list deals its entries out in
-// a fixed snake order, which keeps the CTAs even only while neighbouring
-// entries are about equally long; sorted band by band, each band's short last
-// items sit beside the next band's long ones, and on 64 outputs of 511x511
-// the busiest CTA then carries 7% (two bands) to 16% (four or eight) more than
-// the mean.  With about 8 items per CTA, even assigning each item to the CTA
-// with the least work so far leaves 6% (the last band's items are all alike,
-// with nothing small left to fill the gaps).  So each band's rows are cut
-// afresh: the band's work W (left rows over all tile keys) into about G * m
-// equal pieces, m = ceil(W / (G * chunk_rows)), a piece at least half of
-// chunk_rows and at most chunk_rows rows, every tile key's rows into near-equal
-// pieces.  Then the pieces, band by band and longest first, each go to the
-// CTA with the least work so far (cost: (left rows + 3) x active K-steps, the
-// 3 standing for an item's fixed drain), at most ceil(n / G) + 2 per CTA.
-// CTA c finds its r-th entry at r * G + c.  Pieces per tile key are at most
-// 2 ceil(rows / chunk_rows) + 1, so n <= 3 n_items and the entries fit in
-// 3 n_items + 3 G.  `band_items` receives the pieces per band (what the
-// epilogue counts).
+// Schedule of a banded launch (plan_band_schedule), copied to `region`: its
+// entry count in the first 16 bytes, then the entries.  The device work list
+// deals its entries out in a fixed snake order, which keeps the CTAs even only
+// while neighbouring entries are about equally long; sorted band by band, each
+// band's short last items sit beside the next band's long ones, and on 64
+// outputs of 511x511 the busiest CTA then carries 7% (two bands) to 16% (four
+// or eight) more than the mean.  With about 8 items per CTA, even assigning
+// each item to the CTA with the least work so far leaves 6% (the last band's
+// items are all alike, with nothing small left to fill the gaps); hence the
+// plan's equal pieces per band.
 xc_status upload_band_schedule(const TcParams& prm, int G, int* region, long long* band_items,
                                cudaStream_t stream) {
-  struct Entry {
-    int rank, rows, cost;
-    int4 e;
-  };
-  const int per_rank = prm.pm.n_left * prm.n_pgroups;
-  const int tc = (prm.Hr - 1) / prm.DY;
-  // left rows of each row-shift tile (by visiting rank) and each band's work
-  std::vector<int> rows_of(prm.n_dytiles), band_of(prm.n_dytiles);
-  std::vector<double> work(prm.n_bands, 0.0);
-  for (int rank = 0; rank < prm.n_dytiles; ++rank) {
-    const int t = centre_out(rank, prm.n_dytiles, tc);
-    const int dy0 = -(prm.Hr - 1) + t * prm.DY;
-    rows_of[rank] = std::max(0, std::min(prm.Hl, dy0 + prm.DY - 1 + prm.Hr) - std::max(0, dy0));
-    int b = 0;
-    while (b + 1 < prm.n_bands && t >= prm.band_start[b + 1]) ++b;
-    band_of[rank] = b;
-    work[b] += (double)rows_of[rank] * per_rank * prm.n_halves;
-  }
-  std::vector<double> target(prm.n_bands);
-  for (int b = 0; b < prm.n_bands; ++b) {
-    const double m = std::max(1.0, std::ceil(work[b] / ((double)G * prm.chunk_rows)));
-    target[b] = std::max(0.5 * prm.chunk_rows, work[b] / (G * m));
-  }
-  const int ks[2] = {__builtin_popcount(tile_mask(0, prm)) + __builtin_popcount(tile_mask(128, prm)),
-                     __builtin_popcount(tile_mask(256, prm)) + __builtin_popcount(tile_mask(384, prm))};
-  std::vector<Entry> es;
-  for (int b = 0; b < prm.n_bands; ++b) band_items[b] = 0;
-  for (int rank = 0; rank < prm.n_dytiles; ++rank) {
-    const int rows = rows_of[rank], b = band_of[rank];
-    if (rows <= 0) continue;
-    const int np = std::max((rows + prm.chunk_rows - 1) / prm.chunk_rows,
-                            std::max(1, (int)std::lround(rows / target[b])));
-    for (int lp = 0; lp < per_rank; ++lp)
-      for (int half = 0; half < prm.n_halves; ++half) {
-        const int key = (rank * per_rank + lp) * prm.n_halves + half;
-        int row0 = 0;
-        for (int q = 0; q < np; ++q) {
-          const int n = rows / np + (q < rows % np ? 1 : 0);
-          es.push_back({prm.band_rank[b], n, (n + 3) * ks[half], make_int4(key, row0, n, 0)});
-          row0 += n;
-          ++band_items[b];
-        }
-      }
-  }
-  std::stable_sort(es.begin(), es.end(), [](const Entry& a, const Entry& b) {
-    return a.rank != b.rank ? a.rank < b.rank : a.rows > b.rows;
-  });
-  const long long n = (long long)es.size();
-  const int cap = (int)((n + G - 1) / G) + 2;
-  using Slot = std::pair<long long, int>;  // (work so far, CTA): the smallest first
-  std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> heap;
-  for (int c = 0; c < G; ++c) heap.push({0, c});
-  std::vector<int> count(G, 0);
-  std::vector<int4> sched((size_t)G * cap, make_int4(-1, 0, 0, 0));
-  int rounds = 0;
-  for (const Entry& e : es) {
-    const Slot s = heap.top();  // never empty: G * cap >= n + 2G
-    heap.pop();
-    sched[(size_t)count[s.second] * G + s.second] = e.e;
-    rounds = std::max(rounds, ++count[s.second]);
-    if (count[s.second] < cap) heap.push({s.first + e.cost, s.second});
-  }
-  const size_t n_ent = (size_t)rounds * G;
+  BandPlanIn in;
+  in.Hl = prm.Hl;
+  in.Hr = prm.Hr;
+  in.DY = prm.DY;
+  in.n_dytiles = prm.n_dytiles;
+  in.per_rank = prm.pm.n_left * prm.n_pgroups;
+  in.n_halves = prm.n_halves;
+  in.chunk_rows = prm.chunk_rows;
+  in.n_bands = prm.n_bands;
+  for (int b = 0; b <= prm.n_bands; ++b) in.band_start[b] = prm.band_start[b];
+  for (int b = 0; b < prm.n_bands; ++b) in.band_rank[b] = prm.band_rank[b];
+  in.ks[0] = __builtin_popcount(tile_mask(0, prm)) + __builtin_popcount(tile_mask(128, prm));
+  in.ks[1] = __builtin_popcount(tile_mask(256, prm)) + __builtin_popcount(tile_mask(384, prm));
+  std::vector<BandPiece> sched;
+  plan_band_schedule(in, G, &sched, band_items);
+  static_assert(sizeof(BandPiece) == sizeof(int4), "a schedule entry is an int4");
+  const size_t n_ent = sched.size();
   if (t_stage.copied == nullptr) XC_CUDA_TRY(cudaEventCreateWithFlags(&t_stage.copied, cudaEventDisableTiming));
   XC_CUDA_TRY(cudaEventSynchronize(t_stage.copied));  // the previous copy has read the staging buffer
   if (t_stage.cap < n_ent + 1) {
@@ -1566,7 +1502,7 @@ xc_status upload_band_schedule(const TcParams& prm, int G, int* region, long lon
     t_stage.cap = n_ent + 1;
   }
   t_stage.host[0] = make_int4((int)n_ent, 0, 0, 0);
-  std::copy(sched.begin(), sched.begin() + n_ent, t_stage.host + 1);
+  std::memcpy(t_stage.host + 1, sched.data(), n_ent * sizeof(int4));
   XC_CUDA_TRY(cudaMemcpyAsync(region, t_stage.host, (n_ent + 1) * sizeof(int4), cudaMemcpyHostToDevice, stream));
   XC_CUDA_TRY(cudaEventRecord(t_stage.copied, stream));
   return XC_OK;
@@ -1696,54 +1632,21 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   prm.paired = (t.n_halves == 2 && paired_enabled() && band_done == nullptr) ? 1 : 0;
   const long long n_list = prm.paired ? t.n_items / 2 : t.n_items;
 
-  // Output row bands: contiguous runs of row-shift tiles with about equal
-  // numbers of left rows (the work), each covering output rows
-  // [tile_lo * DY, tile_hi * DY).  The host knows each band's live item count
-  // (an item is live when its chunk of left rows is not empty).
+  // Output row bands (one unless banded); a banded launch's pieces per band
+  // come with its schedule below
   {
-    const int n_tiles_y = div_up(g.Sy, t.DY);
-    std::vector<long long> rows_of(n_tiles_y), live_of(n_tiles_y);
-    long long total = 0;
-    for (int ty = 0; ty < n_tiles_y; ++ty) {
-      const int dy0 = -(g.Hr - 1) + ty * t.DY;
-      const int lo = std::max(0, dy0), hi = std::min(g.Hl, dy0 + t.DY - 1 + g.Hr);
-      rows_of[ty] = std::max(0, hi - lo);
-      live_of[ty] = std::min<long long>(t.n_chunks, div_up(rows_of[ty], t.chunk_rows)) * t.n_halves * pm.n_left *
-                    div_up(pm.K, t.P);
-      total += rows_of[ty];
-    }
-    const int want = band_done ? std::max(1, std::min({want_bands, kMaxBands, n_tiles_y})) : 1;
-    // boundaries where the running row count passes k/want of the total; every
-    // band keeps at least one tile (and every tile has rows, so items)
-    prm.band_start[0] = 0;
-    long long acc = 0;
-    int nb = 1;
-    for (int ty = 0; ty + 1 < n_tiles_y && nb < want; ++ty) {
-      acc += rows_of[ty];
-      if (acc * want >= total * nb) prm.band_start[nb++] = ty + 1;
-    }
-    prm.band_start[nb] = n_tiles_y;
-    prm.n_bands = nb;
+    const BandLayout L = plan_bands(g.Hl, g.Hr, t.DY, g.Sy, band_done ? want_bands : 1);
+    prm.n_bands = L.n_bands;
+    for (int k = 0; k <= L.n_bands; ++k) prm.band_start[k] = L.band_start[k];
+    for (int k = 0; k < L.n_bands; ++k) prm.band_rank[k] = L.band_rank[k];
     prm.band_done = band_done;
-    // Bands with the most output rows are worked first: the copies still to
-    // run when the kernel ends are then the shortest ones.  (Equal work gives
-    // the edge bands far more rows, since the left rows per row-shift tile
-    // fall off towards both edges.)
-    int order[kMaxBands];
-    for (int k = 0; k < nb; ++k) order[k] = k;
-    const auto rows_out = [&](int k) {
-      return std::min(g.Sy, prm.band_start[k + 1] * t.DY) - std::min(g.Sy, prm.band_start[k] * t.DY);
-    };
-    std::stable_sort(order, order + nb, [&](int a, int b) { return rows_out(a) > rows_out(b); });
-    for (int r = 0; r < nb; ++r) prm.band_rank[order[r]] = r;
     if (bands) {
-      bands->n = nb;
-      for (int k = 0; k < nb; ++k) {
-        bands->order[k] = order[k];
+      bands->n = L.n_bands;
+      for (int k = 0; k < L.n_bands; ++k) {
+        bands->order[k] = L.order[k];
         bands->items[k] = 0;
-        for (int ty = prm.band_start[k]; ty < prm.band_start[k + 1]; ++ty) bands->items[k] += live_of[ty];
-        bands->row_lo[k] = std::min(g.Sy, prm.band_start[k] * t.DY);
-        bands->row_hi[k] = std::min(g.Sy, prm.band_start[k + 1] * t.DY);
+        bands->row_lo[k] = L.row_lo[k];
+        bands->row_hi[k] = L.row_hi[k];
       }
     }
   }
