@@ -129,12 +129,20 @@ xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const voi
  * device->host copy and free, i.e. the reference's whole
  * prepare/transfer/run/finalize/free sequence (src/main.cpp:123-174).
  * Synchronises `stream` before returning. Device buffers are cached per
- * thread between calls of the same size.  Problems with about 48 MiB of
- * output or more run in up to four chunks of partners (left matrices in
- * n_to_m), each chunk's copy-in, correlation and copy-out on its own stream
- * so that copies overlap the neighbouring chunks' correlations; with
- * XC_METHOD_AUTO each chunk picks its own method. Host buffers should be
- * pinned for the copies to overlap. */
+ * thread between calls of the same size.  Host buffers should be pinned for
+ * copies to overlap computation.
+ *  - The split tensor-core methods (FP32, from 16 MiB of output) copy the
+ *    output out in up to eight row bands while their one kernel runs: the
+ *    kernel counts each band's finished work in device memory and the copy
+ *    stream waits on the count.  Their pieces of work are cut per band, so
+ *    the result may differ from xc_correlate's by a few FP32 roundings of
+ *    the partial sums (both stay within 1e-5 of max|out| of the exact
+ *    result).
+ *  - Otherwise problems run in one chunk of partners (left matrices in
+ *    n_to_m) per 192 MiB of output, up to four, each chunk's copy-in,
+ *    correlation and copy-out on its own stream so that copies overlap the
+ *    neighbouring chunks' correlations; with XC_METHOD_AUTO each chunk picks
+ *    its own method. */
 xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
                             uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
                             void* stream);
