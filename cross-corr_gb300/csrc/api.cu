@@ -148,14 +148,25 @@ xc_status host_banded_tc(ThreadCache& c, xc_mode mode, bool tf32, xc_size2 left,
   XC_TRY(tc_correlate_banded((const float*)c.d_left, (const float*)c.d_right, (float*)c.d_out, g, pm, c.d_ws,
                              c.ws_bytes, s, tf32, n_bands, c.d_bands, &bands));
   const size_t row = (size_t)g.Sx * sizeof(float), mat = row * g.Sy;
+  // Once the kernel is queued, a failure to queue a band's wait or copy still
+  // lets the copies already queued finish (the release after the kernel
+  // frees every wait) before the call returns: none may write into h_out
+  // after the caller has it back.
+  const auto drain = [&](xc_status st, const char* what) {
+    cudaStreamSynchronize(c.s_out);
+    cudaStreamSynchronize(s);
+    return fail(st, what);
+  };
   for (int k = 0; k < bands.n; ++k) {
     const int b = bands.order[k];
     if (wait_value32()(reinterpret_cast<CUstream>(c.s_out), reinterpret_cast<CUdeviceptr>(c.d_bands + b),
                        (cuuint32_t)bands.items[b], CU_STREAM_WAIT_VALUE_GEQ) != CUDA_SUCCESS)
-      return fail(XC_ERR_CUDA, "stream wait on an output band failed");
+      return drain(XC_ERR_CUDA, "stream wait on an output band failed");
     const size_t off = row * bands.row_lo[b];
-    XC_CUDA_TRY(cudaMemcpy2DAsync(static_cast<char*>(h_out) + off, mat, static_cast<char*>(c.d_out) + off, mat,
-                                  row * (bands.row_hi[b] - bands.row_lo[b]), n_out, cudaMemcpyDeviceToHost, c.s_out));
+    if (cudaMemcpy2DAsync(static_cast<char*>(h_out) + off, mat, static_cast<char*>(c.d_out) + off, mat,
+                          row * (bands.row_hi[b] - bands.row_lo[b]), n_out, cudaMemcpyDeviceToHost,
+                          c.s_out) != cudaSuccess)
+      return drain(XC_ERR_CUDA, "copy of an output band failed to queue");
   }
   return XC_OK;
 }
