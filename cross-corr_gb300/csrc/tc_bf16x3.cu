@@ -121,7 +121,6 @@ struct TcCfg {
   static constexpr int kCm = TF ? 4 : 8;            // elements per 16-byte core-matrix row
   static constexpr int kQ = TF ? 128 : 64;          // core matrices in T
   static constexpr int kTBytes = kQ * 128;          // one plane of T
-  static constexpr int kEs = TF ? 4 : 2;            // element bytes
   static constexpr int kSmem = 1024 + kStages * kStageBytes + 4 * kTBytes + 4 * kXLen * 4 + kBarBytes;
 };
 
@@ -462,18 +461,10 @@ __device__ __forceinline__ long long n_rounds(const TcParams& p, long long n_liv
   return (n_live + G - 1) / G;
 }
 
-// Arrives on the mbarrier at the same shared-memory offset in every CTA of
-// `mask` once this thread's MMAs are complete.
-__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "h"(mask)
-      : "memory");
-}
-
-// mma_commit_mc when `multicast` is non-zero, else mma_commit: both forms
-// under guard predicates, so the issue loop has no branch here.
+// Arrives once this thread's MMAs are complete: on the mbarrier at the same
+// shared-memory offset in every CTA of `mask` when `multicast` is non-zero,
+// else on this CTA's barrier (mma_commit); both forms under guard
+// predicates, so the issue loop has no branch here.
 __device__ __forceinline__ void mma_commit_sel(uint64_t* bar, uint16_t mask, int multicast) {
   asm volatile(
       "{\n\t.reg .pred m;\n\t"
