@@ -139,8 +139,7 @@ struct TcParams {
   int kstep;        // columns per K-step: 16 (BF16) or 8 (TF32)
   const int* flush_tab;  // drain TMEM every this many left rows, per (left matrix, partner group)
   int chunk_rows;   // left rows per work item (a longer row range is split over items)
-  const int* items;  // non-empty work items (pairs when paired), most left rows first (tc_item encoding)
-  int paired;        // 1: clusters of two CTAs take the two halves of an item pair, sharing right tiles
+  const int* items;  // non-empty work items, most left rows first (tc_item encoding)
   // Output row bands: band b holds the items of row-shift tiles
   // [band_start[b], band_start[b+1]); the work list takes the bands one after
   // another in band_rank order, and with band_done set the
@@ -392,13 +391,10 @@ __host__ __device__ __forceinline__ bool tc_entry(const TcParams& p, int4 e, TcI
 }
 
 // Lists the non-empty work items by output row band (in the order
-// band_rank gives), then most left rows first (a counting sort): one block.  Every CTA of tc_kernel reads the same
-// list.  When
-// paired, the entries are item pairs (the two halves of the shifts, which
-// have the same rows): pair i holds items 2 i and 2 i + 1.
+// band_rank gives), then most left rows first (a counting sort): one block.
+// Every CTA of tc_kernel reads the same list.
 __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long long n_total, int* __restrict__ items,
                                                         int* __restrict__ n_live) {
-  const int step = p.paired ? 2 : 1;
   // key = rank * (chunk_rows + 1) + (chunk_rows - rows): band first, then
   // the longest items
   __shared__ int cnt[kMaxBands * (kMaxChunkRows + 1)];
@@ -407,7 +403,7 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   __syncthreads();
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
-    if (tc_item(p, idx * step, &w)) atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1);
+    if (tc_item(p, idx, &w)) atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -422,7 +418,7 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   __syncthreads();
   for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
     TcItem w;
-    if (tc_item(p, idx * step, &w))
+    if (tc_item(p, idx, &w))
       items[atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1)] = (int)idx;
   }
 }
@@ -434,57 +430,20 @@ __global__ void band_release_kernel(int* band_done, int n) {
   if ((int)threadIdx.x < n) band_done[threadIdx.x] = 0x7fffffff;
 }
 
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-
-// The item a CTA takes in `round`: list entries are dealt to the CTAs (or
-// to the clusters when paired) in snake order, round r giving position
-// r*G + c or r*G + G-1-c; in a cluster, CTA rank h takes half h of the pair.
+// The item a CTA takes in `round`: list entries are dealt to the CTAs in
+// snake order, round r giving position r*G + c or r*G + G-1-c.
 __device__ __forceinline__ bool round_item(const TcParams& p, long long n_live, long long round, TcItem* w) {
   if (p.sched != nullptr) {
     const long long pos = round * gridDim.x + blockIdx.x;
     return pos < n_live && tc_entry(p, p.sched[pos], w);
   }
-  const int cs = p.paired ? 2 : 1;
-  const long long G = gridDim.x / cs, c = blockIdx.x / cs;
+  const long long G = gridDim.x, c = blockIdx.x;
   const long long pos = round * G + ((round & 1) ? G - 1 - c : c);
   if (pos >= n_live) return false;
-  const long long idx = p.paired ? 2LL * p.items[pos] + cluster_rank() : (long long)p.items[pos];
-  return tc_item(p, idx, w);
+  return tc_item(p, (long long)p.items[pos], w);
 }
 
-__device__ __forceinline__ long long n_rounds(const TcParams& p, long long n_live) {
-  const long long G = gridDim.x / (p.paired ? 2 : 1);
-  return (n_live + G - 1) / G;
-}
-
-// Arrives once this thread's MMAs are complete: on the mbarrier at the same
-// shared-memory offset in every CTA of `mask` when `multicast` is non-zero,
-// else on this CTA's barrier (mma_commit); both forms under guard
-// predicates, so the issue loop has no branch here.
-__device__ __forceinline__ void mma_commit_sel(uint64_t* bar, uint16_t mask, int multicast) {
-  asm volatile(
-      "{\n\t.reg .pred m;\n\t"
-      "setp.ne.b32 m, %2, 0;\n\t"
-      "@m tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;\n\t"
-      "@!m tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(smem_u32(bar)),
-      "h"(mask), "r"(multicast)
-      : "memory");
-}
-
-// TMA load of a 4D box delivered to the same shared-memory offset in every
-// CTA of `mask`, each arriving (complete_tx) on its own barrier at `bar`'s offset.
-__device__ __forceinline__ void tma_load_4d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
-                                               int c2, int c3, uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster "
-      "[%0], [%1, {%3, %4, %5, %6}], [%2], %7;" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "h"(mask)
-      : "memory");
-}
+__device__ __forceinline__ long long n_rounds(long long n_live) { return (n_live + gridDim.x - 1) / gridDim.x; }
 
 // Accumulator windows of an item: tile 0 drains after every `flush` left
 // rows, tile 1 first after (flush + 1) / 2 rows and then every `flush`; both
@@ -533,17 +492,12 @@ __global__ void __launch_bounds__(kThreads, 1)
   // pipeline counters running across them, so the next item's loads and
   // MMAs overlap the previous item's final adds.
   const long long n_items = *p.n_live;
-  const long long n_round = n_rounds(p, n_items);
-  // Paired: the rank-0 CTA of the cluster loads every right tile for both
-  // CTAs (multicast), and a stage is free again once all four issuers of the
-  // cluster have consumed it.
-  const uint16_t cl_mask = p.paired ? 3 : 1;
-  const bool loader = !p.paired || cluster_rank() == 0;
+  const long long n_round = n_rounds(n_items);
   if (threadIdx.x == 0) {
     // consumed barriers take one commit from each issuer
     for (int s = 0; s < C::kStages; ++s) {
       mbar_init(&a_full[s], 1);
-      mbar_init(&a_empty[s], (p.paired ? 2 : 1) * kIssuers);
+      mbar_init(&a_empty[s], kIssuers);
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&r_full[s], kBuilderWarps);
@@ -556,12 +510,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_mbar_init();
     prefetch_tensormap(&map_hi);
     prefetch_tensormap(&map_lo);
-  }
-  // the peer's barriers must be initialised before this CTA's multicast
-  // loads and commits reach them
-  if (p.paired) {
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
@@ -593,25 +541,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 break;
               }
               mbar_arrive_expect_tx(&a_full[s], kStageBytes);
-              if (!loader) continue;  // the peer's loads arrive here too
               unsigned char* dst = b_tiles + s * kStageBytes;
               const CUtensorMap* map = pl == 0 ? &map_hi : &map_lo;
               const int x = kc * 4 * p.kstep;  // first column of the chunk
               if (p.mats_mode) {
-                for (int d = 0; d < p.DY; ++d) {
-                  if (p.paired)
-                    tma_load_4d_mc(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0, cl_mask);
-                  else
-                    tma_load_4d(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0);
-                }
+                for (int d = 0; d < p.DY; ++d)
+                  tma_load_4d(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0);
               } else {
                 const int b0 = a - w.dy0 - (p.DY - 1);
-                for (int q = 0; q < p.P; ++q) {
-                  if (p.paired)
-                    tma_load_4d_mc(dst + q * p.DY * 128, map, &a_full[s], x, b0, w.rdim2, w.p0 + q, cl_mask);
-                  else
-                    tma_load_4d(dst + q * p.DY * 128, map, &a_full[s], x, b0, w.rdim2, w.p0 + q);
-                }
+                for (int q = 0; q < p.P; ++q)
+                  tma_load_4d(dst + q * p.DY * 128, map, &a_full[s], x, b0, w.rdim2, w.p0 + q);
               }
             }
           }
@@ -713,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                   }
                 }
               }
-              mma_commit_sel(&a_empty[s], cl_mask, p.paired);
+              mma_commit(&a_empty[s]);
               // next stage, without a branch
               s = s + 1 == C::kStages ? 0 : s + 1;
               s_phase ^= s == 0 ? 1u : 0u;
@@ -915,12 +854,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   tc_fence_after();
   if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512) : "memory");
-  }
-  // neither CTA of a pair leaves while the other may still load into or
-  // arrive on its shared memory
-  if (p.paired) {
-    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
-    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
 }
 
@@ -1377,10 +1310,6 @@ int env_int(const char* name, int def) {
 // the MMAs while the epilogue reads the accumulators.
 // XC_TC_FLUSH_ROWS fixes the window, XC_TC_CHUNK_ROWS the item length (studies).
 int flush_rows(int nkc) { return std::max(1, std::min(32, 240 / (12 * nkc))); }
-bool paired_enabled() {
-  static const bool v = std::getenv("XC_TC_PAIRED") != nullptr && std::atoi(std::getenv("XC_TC_PAIRED")) != 0;
-  return v;
-}
 int flush_fixed() {
   static const int v = env_int("XC_TC_FLUSH_ROWS", 0);
   return v;
@@ -1614,14 +1543,7 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   prm.n_chunks = t.n_chunks;
   prm.flags = device_flags();
 
-  // Items come in pairs (the two halves of the shifts, Sx > 256) that read
-  // the same right tiles: with XC_TC_PAIRED=1 a cluster of two CTAs takes a
-  // pair, and one TMA load delivers each tile to both (halving the L2-to-SM
-  // traffic).  Off by default: at 256x256 x 64 the right tiles come from L2
-  // fast enough (1.62 ms unpaired, 1.65 ms paired), and the lockstep of the
-  // two CTAs costs more than the traffic it saves.
-  prm.paired = (t.n_halves == 2 && paired_enabled() && band_done == nullptr) ? 1 : 0;
-  const long long n_list = prm.paired ? t.n_items / 2 : t.n_items;
+  const long long n_list = t.n_items;
 
   // Output row bands (one unless banded); a banded launch's pieces per band
   // come with its schedule below
@@ -1647,33 +1569,7 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   // columns each), walking the list in snake order
   auto kern = tf32 ? tc_kernel<true> : tc_kernel<false>;
   XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  cfg.blockDim = dim3(kThreads);
-  cfg.dynamicSmemBytes = (size_t)t.smem_bytes;
-  cfg.stream = stream;
-  long long blocks;
-  if (prm.paired) {
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 2;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    // as many clusters as can be resident at once (a GPC with an odd number
-    // of free SMs leaves one out)
-    cfg.gridDim = dim3(2);
-    int clusters = 0;
-    XC_CUDA_TRY(cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg));
-    if (clusters < 1) return fail(XC_ERR_CUDA, "no resident cluster of two CTAs for the tensor-core kernel");
-    blocks = 2 * std::max(1LL, std::min<long long>(n_list, clusters));
-  } else {
-    int dev = 0, sms = 0;
-    XC_CUDA_TRY(cudaGetDevice(&dev));
-    XC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    blocks = std::max(1LL, std::min<long long>(n_list, sms));
-  }
-  cfg.gridDim = dim3((unsigned)blocks);
+  const long long blocks = std::max(1LL, std::min<long long>(n_list, sm_count()));
   prm.items = w.items;
   prm.sched = nullptr;
   if (band_done) {
@@ -1686,14 +1582,15 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
     if (bands)
       for (int k = 0; k < prm.n_bands; ++k) bands->items[k] = band_items[k];
   } else {
-    // the work list: non-empty items (or pairs), most left rows first, built on the device
+    // the work list: non-empty items, most left rows first, built on the device
     prm.n_live = w.items + t.n_items;
     worklist_kernel<<<1, 1024, 0, stream>>>(prm, n_list, w.items, w.items + t.n_items);
     XC_CUDA_TRY(cudaGetLastError());
   }
   const int slot = kernel_timer_begin(stream);
-  XC_CUDA_TRY(cudaLaunchKernelEx(&cfg, kern, mhi, mlo, prm));
+  kern<<<(unsigned)blocks, kThreads, (size_t)t.smem_bytes, stream>>>(mhi, mlo, prm);
   kernel_timer_end(slot, stream);
+  XC_CUDA_TRY(cudaGetLastError());
   if (band_done) {
     band_release_kernel<<<1, 32, 0, stream>>>(band_done, prm.n_bands);
     XC_CUDA_TRY(cudaGetLastError());
@@ -1722,18 +1619,24 @@ static __device__ __align__(256) unsigned char g_tc_noalloc_scratch[XC_TC_NOALLO
 namespace {
 std::mutex g_noalloc_mutex;
 void* g_noalloc_ptr[64] = {nullptr};
+unsigned long long g_noalloc_ctx[64] = {0};
 
-// Device address of the scratch array for the current device, looked up once
-// per device (with that device current) and cached.
+// Device address of the scratch array for the current device.  In host code
+// the array's name only stands in for it, so the address is looked up with
+// the device current: once per device and context (again after a context
+// reset, which gives the array a new address; on every call when the
+// context's identity is unavailable).
 xc_status noalloc_scratch(void** ptr) {
   int dev = 0;
   XC_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return fail(XC_ERR_INVALID_ARGUMENT, "device index out of range");
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_ptr[dev] == nullptr) {
+  if (g_noalloc_ptr[dev] == nullptr || ctx == 0 || g_noalloc_ctx[dev] != ctx) {
     void* p = nullptr;
     XC_CUDA_TRY(cudaGetSymbolAddress(&p, g_tc_noalloc_scratch));
     g_noalloc_ptr[dev] = p;
+    g_noalloc_ctx[dev] = ctx;
   }
   *ptr = g_noalloc_ptr[dev];
   return XC_OK;

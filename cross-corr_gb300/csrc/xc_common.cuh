@@ -53,6 +53,7 @@ struct DeviceFlags {
   unsigned int where;    // kernel-specific code of the first expiry
 };
 DeviceFlags* device_flags();  // per-device address of a __device__ variable (no allocation)
+unsigned long long current_context_id();  // unique ID of the current CUDA context, 0 if unknown
 xc_status check_device_flags(cudaStream_t stream);
 
 #if defined(__CUDACC__)

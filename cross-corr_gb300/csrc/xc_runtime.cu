@@ -77,24 +77,60 @@ bool encode_tiled(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const v
 }
 
 // ---------------------------------------------------------------------------
+// Identity of the calling thread's current CUDA context: cuCtxGetId's ID,
+// unique for the life of the process, so a context that replaced an earlier
+// one (after cudaDeviceReset) never shares it.  Taken through the runtime's
+// driver entry points (no link to libcuda); 0 when unavailable or when no
+// context is current yet.
+// ---------------------------------------------------------------------------
+namespace {
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+template <typename F>
+F driver_fn(const char* name, int version) {
+  void* ptr = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &ptr, version, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess)
+    return reinterpret_cast<F>(ptr);
+  return nullptr;
+}
+}  // namespace
+
+unsigned long long current_context_id() {
+  static const CtxGetCurrentFn get_current = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent", 12000);
+  static const CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId", 12000);
+  if (get_current == nullptr || get_id == nullptr) return 0;
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// ---------------------------------------------------------------------------
 // Device flag word: a file-scope __device__ variable (no allocation).  Its
-// device address is looked up once per device with that device current.
+// device address is looked up with the device current, once per device and
+// context (looked up again after a context reset; on every call when the
+// context's identity is unavailable).
 // ---------------------------------------------------------------------------
 __device__ DeviceFlags g_device_flags;
 
 namespace {
 std::mutex g_flag_mutex;
 DeviceFlags* g_flags[64] = {nullptr};
+unsigned long long g_flags_ctx[64] = {0};
 }  // namespace
 
 DeviceFlags* device_flags() {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lock(g_flag_mutex);
-  if (g_flags[dev] == nullptr) {
+  if (g_flags[dev] == nullptr || ctx == 0 || g_flags_ctx[dev] != ctx) {
     void* ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, g_device_flags) != cudaSuccess) return nullptr;
     g_flags[dev] = static_cast<DeviceFlags*>(ptr);
+    g_flags_ctx[dev] = ctx;
   }
   return g_flags[dev];
 }

@@ -163,8 +163,9 @@ void xc_release_thread_cache(void);
  * array of XC_TC_NOALLOC_SCRATCH_BYTES per GPU; it calls no cudaMalloc,
  * cudaFree or allocating library routine.
  *  - The first call on a device looks up that array's device address (with
- *    the device current) and caches it; make that first call before any
- *    stream capture.
+ *    the device current) and caches it for that device's context; make that
+ *    first call before any stream capture.  After cudaDeviceReset the next
+ *    call looks the address up again (the new context's array is new).
  *  - Problems whose scratch exceeds the array are rejected with
  *    XC_ERR_WORKSPACE and a message giving both sizes.  (The 256x256 x 64
  *    one_to_many problem needs about 51 MB.)

@@ -5,9 +5,12 @@ latency-critical loops where cudaMalloc/cudaFree may block or synchronise).
 It works in one fixed file-scope device array instead of a caller workspace,
 so these tests call it twice in a row through the C ABI and compare each
 result with the ordinary workspace entry point (xc_correlate with
-XC_METHOD_TC_BF16X3), within the 1e-5 relative tolerance the other parity
-tests use.  The second call uses a different shape, so stale contents of the
-shared array from the first call must not matter.
+XC_METHOD_TC_BF16X3) and with the CPU oracle (FP64 accumulation), within the
+1e-5 relative tolerance the other parity tests use.  The second call uses a
+different shape, so stale contents of the shared array from the first call
+must not matter.  A further test checks the entry point's promise itself:
+after a warm-up call, repeated calls leave the device's free memory where it
+was.
 
 This file is named to be collected last, so a run that stops at the first
 failure has already run every other test.
@@ -18,6 +21,7 @@ import numpy as np
 import pytest
 
 from helpers import rel_to_max, seeded
+from oracle import oracle
 
 import xcorr
 
@@ -51,6 +55,31 @@ def test_noalloc_matches_workspace_entry_point_twice():
         got = out.cpu().numpy()
         assert np.isfinite(got).all()
         assert rel_to_max(got, ref.cpu().numpy()) <= 1e-5, f"call {i}"
+        exact = oracle.run_mode(mode, left.cpu().numpy(), right.cpu().numpy(), dtype="f32acc64", threads=8)
+        assert rel_to_max(got, exact) <= 1e-5, f"call {i} against the oracle"
+
+
+@pytest.mark.gpu
+def test_noalloc_calls_leave_free_device_memory_unchanged():
+    """The array is part of the loaded module; no call may take device memory
+    beyond it.  The warm-up call may load the module; after it, free memory
+    (cudaMemGetInfo) must not drop over repeated calls.  The inputs and
+    outputs are allocated before the first reading."""
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    stream = torch.cuda.current_stream().cuda_stream
+    mode, n, m, ls, rs, dist = CALLS[0]
+    left = torch.as_tensor(seeded((n,) + ls, 700, dist)).cuda()
+    right = torch.as_tensor(seeded((m,) + rs, 701, dist)).cuda()
+    out = torch.empty((xcorr.output_count(mode, n, m), ls[0] + rs[0] - 1, ls[1] + rs[1] - 1), device="cuda")
+    xcorr.check(noalloc(mode, left, right, out, stream))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        xcorr.check(noalloc(mode, left, right, out, stream))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0, f"free device memory dropped by {free0 - free1} bytes"
 
 
 def test_noalloc_rejects_problems_larger_than_its_array():
