@@ -775,15 +775,30 @@ xc_status check_limit(uint32_t v, uint32_t lo, uint32_t hi, const char* what) {
   return XC_OK;
 }
 
+// The reference's distributions (src/row_distribution.cpp:7-11).  The
+// rectangle and triangle forms divide by max_rows_per_thread
+// (src/row_distribution.cuh:34-253); none ignores it.
+xc_status check_distribution(uint32_t dist, uint32_t max_rows_per_thread) {
+  if (dist > XC_DIST_TRIANGLE) return fail(XC_ERR_INVALID_ARGUMENT, "Unknown distribution " + std::to_string(dist));
+  if (dist != XC_DIST_NONE && max_rows_per_thread == 0)
+    return fail(XC_ERR_INVALID_ARGUMENT, "max_rows_per_thread must be positive for the rectangle and triangle "
+                                         "distributions");
+  return XC_OK;
+}
+
+// One launch of the plain kernel for a launcher drop-in.  `acc`: kAuto for
+// the launchers that write their output, kCaller for the work-distribution
+// launchers, which add into an output the caller zeroed
+// (src/one_to_one.hpp:276-277), as the reference's atomic kernels do.
 template <typename T>
 xc_status run_mode(xc_mode mode, const T* left, const T* right, T* out, xc_size2 ms, uint32_t nl, uint32_t nr,
-                   void* stream) {
+                   void* stream, DirectAccumulate acc = DirectAccumulate::kAuto) {
   PairMap pm;
   uint64_t n_out;
   if (!make_pair_map(mode, nl, nr, &pm, &n_out)) return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts");
   if (left == nullptr || right == nullptr || out == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL pointer");
   return direct_launch(sizeof(T) == 4 ? XC_F32 : XC_F64, left, right, out, make_geometry(ms, ms), pm,
-                       as_stream(stream), -1);
+                       as_stream(stream), -1, acc);
 }
 
 }  // namespace
@@ -833,6 +848,95 @@ extern "C" {
 
 XC_DEFINE_SHUFFLE(f32, float)
 XC_DEFINE_SHUFFLE(f64, double)
+
+// The work-distribution, multirow and multirow-multimat launchers (and the
+// local_mem:: twins of two of them).  Limits are the reference's release
+// build values (CMakeLists.txt:16-43).
+#define XC_DEFINE_SHUFFLE_MORE(SUFFIX, T)                                                                        \
+  xc_status xc_run_ccn_shuffle_work_distribution_##SUFFIX(                                                       \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t warps_per_thread_block, uint32_t max_rows_per_thread, xc_distribution distribution,               \
+      void* stream) {                                                                                            \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_distribution((uint32_t)distribution, max_rows_per_thread));                                    \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_ONE, left, right, out, matrix_size, 1, 1, stream, DirectAccumulate::kCaller);   \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_multimat_right_work_distribution_##SUFFIX(                                        \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t right_matrices_per_thread,           \
+      uint32_t max_rows_per_thread, xc_distribution distribution, void* stream) {                                \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(right_matrices_per_thread, 1, 8, "number of right matrices per thread"));                \
+    XC_TRY(check_distribution((uint32_t)distribution, max_rows_per_thread));                                    \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_MANY, left, right, out, matrix_size, 1, num_right_matrices, stream,             \
+                       DirectAccumulate::kCaller);                                                               \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_##SUFFIX(                                  \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,                  \
+      uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread, uint32_t max_rows_per_thread,       \
+      xc_distribution distribution, void* stream) {                                                              \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(left_matrices_per_thread, 1, 4, "left matrices per thread"));                             \
+    XC_TRY(check_limit(right_matrices_per_thread, 1, 4, "right matrices per thread"));                           \
+    XC_TRY(check_distribution((uint32_t)distribution, max_rows_per_thread));                                    \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_N_TO_M, left, right, out, matrix_size, num_left_matrices, num_right_matrices, stream,  \
+                       DirectAccumulate::kCaller);                                                               \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_local_mem_##SUFFIX(                        \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,                  \
+      uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread, uint32_t max_rows_per_thread,       \
+      xc_distribution distribution, void* stream) {                                                              \
+    return xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_##SUFFIX(                                   \
+        left, right, out, matrix_size, search_size, num_left_matrices, num_right_matrices, warps_per_thread_block, \
+        left_matrices_per_thread, right_matrices_per_thread, max_rows_per_thread, distribution, stream);          \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_multirow_right_##SUFFIX(const T* left, const T* right, T* out,                    \
+                                                       xc_size2 matrix_size, xc_size2 search_size,               \
+                                                       uint32_t warps_per_thread_block,                          \
+                                                       uint32_t right_rows_per_thread, void* stream) {           \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(right_rows_per_thread, 1, 8, "number of right rows per thread"));                        \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_ONE, left, right, out, matrix_size, 1, 1, stream);                              \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_multirow_both_##SUFFIX(const T* left, const T* right, T* out,                     \
+                                                      xc_size2 matrix_size, xc_size2 search_size,                \
+                                                      uint32_t warps_per_thread_block,                           \
+                                                      uint32_t max_shifts_per_thread, uint32_t max_left_rows,    \
+                                                      void* stream) {                                            \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(max_shifts_per_thread, 1, 8, "shifts per thread"));                                      \
+    XC_TRY(check_limit(max_left_rows, 1, 4, "left rows per iteration"));                                         \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_ONE, left, right, out, matrix_size, 1, 1, stream);                              \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_multirow_both_local_mem_##SUFFIX(const T* left, const T* right, T* out,           \
+                                                                xc_size2 matrix_size, xc_size2 search_size,      \
+                                                                uint32_t warps_per_thread_block,                 \
+                                                                uint32_t max_shifts_per_thread,                  \
+                                                                uint32_t max_left_rows, void* stream) {          \
+    return xc_run_ccn_shuffle_multirow_both_##SUFFIX(left, right, out, matrix_size, search_size,                 \
+                                                     warps_per_thread_block, max_shifts_per_thread,              \
+                                                     max_left_rows, stream);                                     \
+  }                                                                                                              \
+  xc_status xc_run_ccn_shuffle_multirow_right_multimat_right_##SUFFIX(                                           \
+      const T* left, const T* right, T* out, xc_size2 matrix_size, xc_size2 search_size,                         \
+      uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t right_rows_per_thread,               \
+      uint32_t right_matrices_per_thread, void* stream) {                                                        \
+    XC_TRY(check_warps(warps_per_thread_block));                                                                 \
+    XC_TRY(check_limit(right_rows_per_thread, 1, 4, "number of right rows per thread"));                        \
+    XC_TRY(check_limit(right_matrices_per_thread, 1, 4, "number of right matrices per thread"));                \
+    XC_TRY(check_search(matrix_size, search_size));                                                              \
+    return run_mode<T>(XC_ONE_TO_MANY, left, right, out, matrix_size, 1, num_right_matrices, stream);            \
+  }
+
+XC_DEFINE_SHUFFLE_MORE(f32, float)
+XC_DEFINE_SHUFFLE_MORE(f64, double)
 
 #define XC_DEFINE_FFT_GLUE(CSUF, RSUF, DT, T)                                                                     \
   xc_status xc_run_hadamard_original_##CSUF(const void* ref, void* deformed, xc_size2 subregion_size,            \

@@ -31,9 +31,19 @@
 //    (store first, then add), so no FP32 accumulation chain exceeds
 //    FLUSH_STAGES*XC products: serial FP32 sums over 256x256 overlaps would
 //    otherwise drift past 1e-5 of max|out|.
+//  * Row split (the reference's work distribution, src/naive_shuffle.cu:306-413
+//    with src/row_distribution.cuh:34-284): when a launch's tiles would not
+//    fill one wave of CTAs, each tile's right-row range is cut into slices of
+//    `rows_per_slice` rows, one CTA per slice, and every flush adds into the
+//    output with red.global.add (the output is zeroed first, or by the
+//    caller for the work-distribution launchers, as in the reference).  The
+//    reference splits the rows of one shift over warps; here a slice holds
+//    the rows of a whole tile of shifts, so the left window and right rows a
+//    stage stages in shared memory still serve all of the tile's shifts.
 //  * Bounded mbarrier waits: an expired wait records a flag and the CTA
 //    winds down (no trap, no hang).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "xc_common.cuh"
@@ -93,6 +103,9 @@ struct Uniform {
   PairMap pm;
   int tiles_sx, tiles_sy, kgroups;
   int sx_origin;  // first tile's sx (<= 0) so that every tile's left x origin is 16-byte aligned
+  int n_slices;        // CTAs per tile, each taking `rows_per_slice` of the tile's right rows
+  int rows_per_slice;
+  int accumulate;      // 1: every flush adds into the output (red.global.add), which starts zeroed
 };
 
 // Ragged batches: one tile queue over pairs of arbitrary sizes.
@@ -204,11 +217,14 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
     bool ok = true;
     for (int iter = 0; ok; ++iter) {
       TileInfo ti;
+      int slice = 0;
       if (!ragged) {
         if (iter > 0) break;
         const Uniform<T>& u = p.u;
         const int nlk = u.pm.n_left * u.kgroups;
         int bid = blockIdx.x;
+        slice = bid % u.n_slices;  // the slices of a tile are neighbouring CTAs
+        bid /= u.n_slices;
         const int lk = bid % nlk;
         bid /= nlk;
         const int tx = bid % u.tiles_sx;
@@ -253,7 +269,14 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
         ti.lmap = p.rg.lmaps + pr.left;
         ti.rmap = p.rg.rmaps + pr.right;
       }
-      const TileSpan sp = tile_span<C>(ti);
+      TileSpan sp = tile_span<C>(ti);
+      if (!ragged && p.u.n_slices > 1) {
+        // this CTA's slice of the tile's right rows (empty for the last
+        // slices of tiles with fewer rows: no stages, just the sentinel)
+        const int y0 = slice * p.u.rows_per_slice;
+        sp.ny = max(0, min(p.u.rows_per_slice, sp.ny - y0));
+        sp.y_lo += y0;
+      }
       const int nst = sp.ny * sp.nxc;
       for (int st = 0; st < nst; ++st, ++j) {
         const int slot = j % S;
@@ -350,6 +373,7 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
 
   // The empty asm keeps the compiler from hoisting the output addresses out of
   // the stage loop (they would pin many registers).
+  const bool accumulate = !ragged && p.u.accumulate;
   auto flush = [&]() {
     int sy_base = t_SY0 + row0, sx_base = t_SX0 + col0, gb = wg * TG;
     asm volatile("" : "+r"(sy_base), "+r"(sx_base), "+r"(gb));
@@ -366,7 +390,10 @@ __global__ void __launch_bounds__(C::NT, C::MINB)
           const int sx = sx_base + q;
           if (sx < 0 || sx >= t_Sx) continue;
           T* dst = o + (long long)sy * t_Sx + sx;
-          *dst = flushed ? *dst + acc[t][q][i] : acc[t][q][i];
+          if (accumulate)
+            atomicAdd(dst, acc[t][q][i]);  // result unused: a red.global.add
+          else
+            *dst = flushed ? *dst + acc[t][q][i] : acc[t][q][i];
           acc[t][q][i] = T(0);
         }
       }
@@ -459,9 +486,55 @@ using CfgF32Small = Cfg<float, 2, 1, 4, 1, 1, 128, 3, 3>;   // 32 sy x 64 sx x 1
 using CfgF64Multi = Cfg<double, 2, 2, 4, 1, 2, 64, 3, 1>;   // 32 x 64 x 4 mats
 using CfgF64Single = Cfg<double, 2, 1, 4, 1, 1, 64, 3, 2>;  // 32 x 64 x 1 mat
 
+// Right rows of the tiles in tile row ty (the y range of tile_span).
+template <typename C>
+int tile_rows(const Geometry& g, int ty) {
+  const int sy0 = ty * C::BSY;
+  const int lo = std::max(0, g.Hr - 1 - (sy0 + C::BSY - 1));
+  const int hi = std::min(g.Hr, g.Hl + g.Hr - 1 - sy0);
+  return std::max(0, hi - lo);
+}
+
+int sm_count_cached() {
+  static const int n = [] {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+      return 152;
+    return sms;
+  }();
+  return n;
+}
+
+// Rows per slice for a launch of `blocks` tiles: none (0) while the tiles
+// fill a wave of CTAs (`wave` resident at once); else the longest slices (a
+// power of two, at least 4 rows) that give two waves of non-empty slices,
+// or 4-row slices when even those give fewer.  XC_DIRECT_SLICE_ROWS fixes
+// the slice length (studies, tests).
+template <typename C>
+int pick_slice_rows(const Geometry& g, long long blocks, int tiles_sy, long long per_tile_row, int wave) {
+  static const int fixed = [] {
+    const char* e = std::getenv("XC_DIRECT_SLICE_ROWS");
+    return e ? std::max(0, std::atoi(e)) : 0;
+  }();
+  if (fixed > 0) return fixed;
+  if (blocks >= wave) return 0;
+  int max_rows = 0;
+  for (int ty = 0; ty < tiles_sy; ++ty) max_rows = std::max(max_rows, tile_rows<C>(g, ty));
+  int rows = 4;
+  while (rows < max_rows) rows *= 2;
+  for (; rows > 4; rows /= 2) {
+    long long live = 0;
+    for (int ty = 0; ty < tiles_sy; ++ty) live += (long long)div_up(tile_rows<C>(g, ty), rows) * per_tile_row;
+    if (live >= 2LL * wave) break;
+  }
+  return rows >= max_rows ? 0 : rows;
+}
+
 template <typename C>
 xc_status launch_uniform(const typename C::type* left, const typename C::type* right, typename C::type* out,
-                         const Geometry& g, const PairMap& pm, cudaStream_t stream, int force_loader) {
+                         const Geometry& g, const PairMap& pm, cudaStream_t stream, int force_loader,
+                         DirectAccumulate acc_mode) {
   using T = typename C::type;
   DirectArgs<T> p;
   std::memset(&p, 0, sizeof(p));
@@ -483,9 +556,33 @@ xc_status launch_uniform(const typename C::type* left, const typename C::type* r
   u.kgroups = div_up(pm.K, C::G);
   p.flags = device_flags();
 
-  const long long blocks = (long long)u.tiles_sx * u.tiles_sy * pm.n_left * u.kgroups;
-  if (blocks <= 0) return XC_OK;
+  const long long tiles = (long long)u.tiles_sx * u.tiles_sy * pm.n_left * u.kgroups;
+  if (tiles <= 0) return XC_OK;
+  auto kern = direct_kernel<C>;
+  int per_sm = 0;
+  XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES));
+  XC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, C::SMEM_BYTES));
+  const int slice_rows = acc_mode == DirectAccumulate::kNever
+                             ? 0
+                             : pick_slice_rows<C>(g, tiles, u.tiles_sy, (long long)u.tiles_sx * pm.n_left * u.kgroups,
+                                                  std::max(1, per_sm) * sm_count_cached());
+  u.n_slices = 1;
+  u.rows_per_slice = 1 << 30;
+  if (slice_rows > 0) {
+    int max_rows = 0;
+    for (int ty = 0; ty < u.tiles_sy; ++ty) max_rows = std::max(max_rows, tile_rows<C>(g, ty));
+    u.n_slices = std::max(1, div_up(max_rows, slice_rows));
+    u.rows_per_slice = slice_rows;
+  }
+  // the caller's output is added into (work-distribution launchers), or is
+  // zeroed here when slices of a tile add into the same outputs
+  u.accumulate = (acc_mode == DirectAccumulate::kCaller || u.n_slices > 1) ? 1 : 0;
+  const long long blocks = tiles * u.n_slices;
   if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+  if (u.accumulate && acc_mode != DirectAccumulate::kCaller) {
+    const long long n_out = (long long)(pm.n_left - 1) * pm.o_l + (long long)(pm.K - 1) * pm.o_k + 1;
+    XC_CUDA_TRY(cudaMemsetAsync(out, 0, (size_t)n_out * g.Sy * g.Sx * sizeof(T), stream));
+  }
 
   // TMA needs 16-byte aligned bases and row/matrix pitches.
   const size_t es = sizeof(T);
@@ -511,8 +608,6 @@ xc_status launch_uniform(const typename C::type* left, const typename C::type* r
   }
 
   static_assert(C::SMEM_BYTES <= 227 * 1024, "shared memory budget");
-  auto kern = direct_kernel<C>;
-  XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM_BYTES));
   const int slot = kernel_timer_begin(stream);
   kern<<<(unsigned)blocks, C::NT, C::SMEM_BYTES, stream>>>(lmap, rmap, p, use_tma);
   kernel_timer_end(slot, stream);
@@ -560,19 +655,19 @@ RaggedShape shape_of() {
 }  // namespace
 
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
-                        const PairMap& pm, cudaStream_t stream, int force_loader) {
+                        const PairMap& pm, cudaStream_t stream, int force_loader, DirectAccumulate acc) {
   if (dtype == XC_F32) {
     if (pm.K >= 4)
       return launch_uniform<CfgF32Multi>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
-                                         force_loader);
+                                         force_loader, acc);
     return launch_uniform<CfgF32Single>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
-                                        force_loader);
+                                        force_loader, acc);
   }
   if (pm.K >= 3)
     return launch_uniform<CfgF64Multi>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
-                                       force_loader);
+                                       force_loader, acc);
   return launch_uniform<CfgF64Single>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
-                                      force_loader);
+                                      force_loader, acc);
 }
 
 // Tile shapes a ragged plan may pick from (the autotuner's candidates).

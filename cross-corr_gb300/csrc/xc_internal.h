@@ -50,9 +50,17 @@ void kernel_timer_end(int slot, cudaStream_t stream);
 xc_status kernel_timing(int enable);
 xc_status kernel_timing_read(double* total_ms, uint32_t* launches);
 
-// Plain definition-based correlation (direct_simt.cu).
+// Plain definition-based correlation (direct_simt.cu).  How results reach
+// the output:
+//  kAuto   - the output is written; under-filled launches split each tile's
+//            rows over several CTAs, which zero the output first and add;
+//  kCaller - always added into the output, which the caller zeroed (the
+//            reference's work-distribution launchers, src/one_to_one.hpp:276-277);
+//  kNever  - written, never split (studies and tests of the unsplit kernel).
+enum class DirectAccumulate { kAuto = 0, kCaller = 1, kNever = 2 };
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
-                        const PairMap& pm, cudaStream_t stream, int force_loader /* -1 auto, 0 cp.async, 1 TMA */);
+                        const PairMap& pm, cudaStream_t stream, int force_loader /* -1 auto, 0 cp.async, 1 TMA */,
+                        DirectAccumulate acc = DirectAccumulate::kAuto);
 
 // Ragged batches (ragged.cu drives direct_simt.cu's persistent mode).
 struct RaggedTile {     // one tile of shifts of one pair

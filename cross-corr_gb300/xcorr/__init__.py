@@ -42,6 +42,17 @@ EXPORTED = [
     "xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f64",
     "xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f32",
     "xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f64",
+    "xc_run_ccn_shuffle_work_distribution_f32", "xc_run_ccn_shuffle_work_distribution_f64",
+    "xc_run_ccn_shuffle_multimat_right_work_distribution_f32",
+    "xc_run_ccn_shuffle_multimat_right_work_distribution_f64",
+    "xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_f32",
+    "xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_f64",
+    "xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_local_mem_f32",
+    "xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_local_mem_f64",
+    "xc_run_ccn_shuffle_multirow_right_f32", "xc_run_ccn_shuffle_multirow_right_f64",
+    "xc_run_ccn_shuffle_multirow_both_f32", "xc_run_ccn_shuffle_multirow_both_f64",
+    "xc_run_ccn_shuffle_multirow_both_local_mem_f32", "xc_run_ccn_shuffle_multirow_both_local_mem_f64",
+    "xc_run_ccn_shuffle_multirow_right_multimat_right_f32", "xc_run_ccn_shuffle_multirow_right_multimat_right_f64",
     "xc_run_hadamard_original_c64", "xc_run_hadamard_original_c128",
     "xc_run_hadamard_n_to_m_over_output_c64", "xc_run_hadamard_n_to_m_over_output_c128",
     "xc_run_scatter_f32", "xc_run_scatter_f64",
@@ -138,6 +149,18 @@ def lib():
                 vp, vp, vp, Size2, Size2, u32, u32, u32, u32, u32, vp]
             getattr(L, f"xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_{t}").argtypes = [
                 vp, vp, vp, Size2, Size2, u32, u32, u32, u32, u32, u32, u32, vp]
+            getattr(L, f"xc_run_ccn_shuffle_work_distribution_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, u32, i,
+                                                                                 vp]
+            getattr(L, f"xc_run_ccn_shuffle_multimat_right_work_distribution_{t}").argtypes = [
+                vp, vp, vp, Size2, Size2, u32, u32, u32, u32, i, vp]
+            for lm in ("", "_local_mem"):
+                getattr(L, f"xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution{lm}_{t}").argtypes = [
+                    vp, vp, vp, Size2, Size2, u32, u32, u32, u32, u32, u32, i, vp]
+                getattr(L, f"xc_run_ccn_shuffle_multirow_both{lm}_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, u32,
+                                                                                    u32, vp]
+            getattr(L, f"xc_run_ccn_shuffle_multirow_right_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, u32, vp]
+            getattr(L, f"xc_run_ccn_shuffle_multirow_right_multimat_right_{t}").argtypes = [
+                vp, vp, vp, Size2, Size2, u32, u32, u32, u32, vp]
             getattr(L, f"xc_run_scatter_{t}").argtypes = [vp, vp, Size2, u32, Size2, Size2, u32, u32, vp]
             getattr(L, f"xc_normalize_fft_results_{t}").argtypes = [vp, vp, Size2, u32, vp]
         for t in ("c64", "c128"):

@@ -293,12 +293,12 @@ xc_status xc_autotune_method(xc_mode mode, xc_dtype dtype, const void* d_left, x
 /* validated with the reference's limits and otherwise advisory: the GB300  */
 /* kernels pick their own tiling.  Nothing is allocated.                    */
 /* ------------------------------------------------------------------------ */
-/* run_ccn_shuffle (src/kernels.cuh:67-75): one_to_one, matrix_size both inputs. */
+/* run_ccn_shuffle (src/kernels.cuh:65-73): one_to_one, matrix_size both inputs. */
 xc_status xc_run_ccn_shuffle_f32(const float* left, const float* right, float* out, xc_size2 matrix_size,
                                  xc_size2 search_size, uint32_t warps_per_thread_block, void* stream);
 xc_status xc_run_ccn_shuffle_f64(const double* left, const double* right, double* out, xc_size2 matrix_size,
                                  xc_size2 search_size, uint32_t warps_per_thread_block, void* stream);
-/* run_ccn_shuffle_multimat_right (src/kernels.cuh:88-98): one left, many right. */
+/* run_ccn_shuffle_multimat_right (src/kernels.cuh:87-97): one left, many right. */
 xc_status xc_run_ccn_shuffle_multimat_right_f32(const float* left, const float* right, float* out,
                                                 xc_size2 matrix_size, xc_size2 search_size,
                                                 uint32_t num_right_matrices, uint32_t warps_per_thread_block,
@@ -307,7 +307,7 @@ xc_status xc_run_ccn_shuffle_multimat_right_f64(const double* left, const double
                                                 xc_size2 matrix_size, xc_size2 search_size,
                                                 uint32_t num_right_matrices, uint32_t warps_per_thread_block,
                                                 uint32_t right_matrices_per_thread, void* stream);
-/* run_ccn_shuffle_one_to_many_multirow_both_multimat_right (src/kernels.cuh:245-258),
+/* run_ccn_shuffle_one_to_many_multirow_both_multimat_right (src/kernels.cuh:223-236),
  * the launcher the reference's sample_app embeds (sample_app/src/main.cpp:48-59). */
 xc_status xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f32(
     const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
@@ -317,7 +317,7 @@ xc_status xc_run_ccn_shuffle_one_to_many_multirow_both_multimat_right_f64(
     const double* left, const double* right, double* out, xc_size2 matrix_size, xc_size2 search_size,
     uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t shifts_per_thread_right_matrix,
     uint32_t right_matrices_per_thread, uint32_t left_rows_per_iteration, void* stream);
-/* run_ccn_n_to_m_shuffle_multirow_both_multimat_both (src/kernels.cuh:260-273):
+/* run_ccn_n_to_m_shuffle_multirow_both_multimat_both (src/kernels.cuh:238-252):
  * output index l*num_right + r. */
 xc_status xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f32(
     const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
@@ -329,6 +329,95 @@ xc_status xc_run_ccn_n_to_m_shuffle_multirow_both_multimat_both_f64(
     uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,
     uint32_t shifts_per_thread_right_matrix, uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread,
     uint32_t left_rows_per_iteration, void* stream);
+
+/* Work distribution (src/row_distribution.cuh:9-13, the DIST template
+ * argument of the *_work_distribution launchers): how the reference splits
+ * the rows of a shift over workers.  Validated (rectangle and triangle need
+ * max_rows_per_thread > 0) and otherwise advisory: the GB300 kernel splits
+ * the right rows of a whole tile of shifts over CTAs when its tiles would
+ * not fill the GPU. */
+typedef enum xc_distribution { XC_DIST_NONE = 0, XC_DIST_RECTANGLE = 1, XC_DIST_TRIANGLE = 2 } xc_distribution;
+/* The work-distribution launchers ADD their results into `out`, which the
+ * caller zeroes first, like the reference's atomic kernels
+ * (src/one_to_one.hpp:276-277 zeroes before run_ccn_shuffle_work_distribution). */
+/* run_ccn_shuffle_work_distribution (src/kernels.cuh:75-85): one_to_one. */
+xc_status xc_run_ccn_shuffle_work_distribution_f32(const float* left, const float* right, float* out,
+                                                   xc_size2 matrix_size, xc_size2 search_size,
+                                                   uint32_t warps_per_thread_block, uint32_t max_rows_per_thread,
+                                                   xc_distribution distribution, void* stream);
+xc_status xc_run_ccn_shuffle_work_distribution_f64(const double* left, const double* right, double* out,
+                                                   xc_size2 matrix_size, xc_size2 search_size,
+                                                   uint32_t warps_per_thread_block, uint32_t max_rows_per_thread,
+                                                   xc_distribution distribution, void* stream);
+/* run_ccn_shuffle_multimat_right_work_distribution (src/kernels.cuh:130-142): one left, many right. */
+xc_status xc_run_ccn_shuffle_multimat_right_work_distribution_f32(
+    const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t right_matrices_per_thread,
+    uint32_t max_rows_per_thread, xc_distribution distribution, void* stream);
+xc_status xc_run_ccn_shuffle_multimat_right_work_distribution_f64(
+    const double* left, const double* right, double* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t right_matrices_per_thread,
+    uint32_t max_rows_per_thread, xc_distribution distribution, void* stream);
+/* run_ccn_shuffle_n_to_m_multimat_both_work_distribution (src/kernels.cuh:161-174)
+ * and its local_mem:: twin (src/kernels.cuh:256-269): output l*num_right + r. */
+xc_status xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_f32(
+    const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+    uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread, uint32_t max_rows_per_thread,
+    xc_distribution distribution, void* stream);
+xc_status xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_f64(
+    const double* left, const double* right, double* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+    uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread, uint32_t max_rows_per_thread,
+    xc_distribution distribution, void* stream);
+xc_status xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_local_mem_f32(
+    const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+    uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread, uint32_t max_rows_per_thread,
+    xc_distribution distribution, void* stream);
+xc_status xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_local_mem_f64(
+    const double* left, const double* right, double* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_left_matrices, uint32_t num_right_matrices, uint32_t warps_per_thread_block,
+    uint32_t left_matrices_per_thread, uint32_t right_matrices_per_thread, uint32_t max_rows_per_thread,
+    xc_distribution distribution, void* stream);
+/* run_ccn_shuffle_multirow_right (src/kernels.cuh:176-185): one_to_one. */
+xc_status xc_run_ccn_shuffle_multirow_right_f32(const float* left, const float* right, float* out,
+                                                xc_size2 matrix_size, xc_size2 search_size,
+                                                uint32_t warps_per_thread_block, uint32_t right_rows_per_thread,
+                                                void* stream);
+xc_status xc_run_ccn_shuffle_multirow_right_f64(const double* left, const double* right, double* out,
+                                                xc_size2 matrix_size, xc_size2 search_size,
+                                                uint32_t warps_per_thread_block, uint32_t right_rows_per_thread,
+                                                void* stream);
+/* run_ccn_shuffle_multirow_both (src/kernels.cuh:187-197) and its local_mem::
+ * twin (src/kernels.cuh:271-281): one_to_one. */
+xc_status xc_run_ccn_shuffle_multirow_both_f32(const float* left, const float* right, float* out,
+                                               xc_size2 matrix_size, xc_size2 search_size,
+                                               uint32_t warps_per_thread_block, uint32_t max_shifts_per_thread,
+                                               uint32_t max_left_rows, void* stream);
+xc_status xc_run_ccn_shuffle_multirow_both_f64(const double* left, const double* right, double* out,
+                                               xc_size2 matrix_size, xc_size2 search_size,
+                                               uint32_t warps_per_thread_block, uint32_t max_shifts_per_thread,
+                                               uint32_t max_left_rows, void* stream);
+xc_status xc_run_ccn_shuffle_multirow_both_local_mem_f32(const float* left, const float* right, float* out,
+                                                         xc_size2 matrix_size, xc_size2 search_size,
+                                                         uint32_t warps_per_thread_block,
+                                                         uint32_t max_shifts_per_thread, uint32_t max_left_rows,
+                                                         void* stream);
+xc_status xc_run_ccn_shuffle_multirow_both_local_mem_f64(const double* left, const double* right, double* out,
+                                                         xc_size2 matrix_size, xc_size2 search_size,
+                                                         uint32_t warps_per_thread_block,
+                                                         uint32_t max_shifts_per_thread, uint32_t max_left_rows,
+                                                         void* stream);
+/* run_ccn_shuffle_multirow_right_multimat_right (src/kernels.cuh:209-221): one left, many right. */
+xc_status xc_run_ccn_shuffle_multirow_right_multimat_right_f32(
+    const float* left, const float* right, float* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t right_rows_per_thread,
+    uint32_t right_matrices_per_thread, void* stream);
+xc_status xc_run_ccn_shuffle_multirow_right_multimat_right_f64(
+    const double* left, const double* right, double* out, xc_size2 matrix_size, xc_size2 search_size,
+    uint32_t num_right_matrices, uint32_t warps_per_thread_block, uint32_t right_rows_per_thread,
+    uint32_t right_matrices_per_thread, void* stream);
 
 /* run_hadamard_original (src/kernels.cuh:7-15, src/hadamard.cu:33-58,176-192):
  * in place, deformed[i] = ref[i mod (area*subregions)] * conj(deformed[i]);

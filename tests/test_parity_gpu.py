@@ -178,6 +178,74 @@ def test_reference_launchers():
     assert rel_to_max(o2.cpu().numpy(), ref2) <= 1e-5
 
 
+# (launcher, mode, n_left, n_right, extra arguments after search_size, adds into out)
+# Extra arguments follow src/kernels.cuh: counts, warps per block, tile
+# arguments, then max_rows_per_thread and the distribution for the
+# work-distribution launchers (1 = rectangle, 2 = triangle, 0 = none).
+MORE_LAUNCHERS = [
+    ("xc_run_ccn_shuffle_work_distribution", "one_to_one", 1, 1, (8, 5, 2), True),
+    ("xc_run_ccn_shuffle_work_distribution", "one_to_one", 1, 1, (4, 0, 0), True),
+    ("xc_run_ccn_shuffle_multimat_right_work_distribution", "one_to_many", 1, 5, (5, 8, 4, 7, 1), True),
+    ("xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution", "n_to_m", 3, 4, (3, 4, 8, 2, 2, 6, 2), True),
+    ("xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_local_mem", "n_to_m", 2, 3, (2, 3, 8, 4, 4, 3, 1),
+     True),
+    ("xc_run_ccn_shuffle_multirow_right", "one_to_one", 1, 1, (8, 4), False),
+    ("xc_run_ccn_shuffle_multirow_both", "one_to_one", 1, 1, (8, 4, 2), False),
+    ("xc_run_ccn_shuffle_multirow_both_local_mem", "one_to_one", 1, 1, (8, 8, 4), False),
+    ("xc_run_ccn_shuffle_multirow_right_multimat_right", "one_to_many", 1, 6, (6, 8, 2, 3), False),
+]
+
+
+@pytest.mark.parametrize("side", [23, 96])
+@pytest.mark.parametrize("suffix", ["f32", "f64"])
+@pytest.mark.parametrize("case", MORE_LAUNCHERS, ids=lambda c: c[0][len("xc_run_ccn_shuffle_"):] + "_" + c[1])
+def test_reference_launchers_work_distribution_and_multirow(case, suffix, side):
+    """The work-distribution, multirow and multirow-multimat drop-ins
+    (src/kernels.cuh:75-281) against the oracle.  The work-distribution ones
+    add into `out`, as the reference's atomic kernels do: the output starts at
+    1.0 here and must end at 1.0 plus the correlation.  At 23x23 the plain
+    kernel's tiles leave the GPU nearly empty, so its rows are split over
+    CTAs (red.global.add); at 96x96 with 5-6 partners too."""
+    name, mode, n, m, extra, adds = case
+    dt = torch.float32 if suffix == "f32" else torch.float64
+    npdt = np.float32 if suffix == "f32" else np.float64
+    L = xcorr.lib()
+    left = seeded((n, side, side), 60 + side, dtype=npdt)
+    right = seeded((m, side, side), 61 + side, dtype=npdt)
+    n_out = xcorr.output_count(mode, n, m)
+    base = 1.0 if adds else float("nan")
+    out = torch.full((n_out, 2 * side - 1, 2 * side - 1), base, dtype=dt, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    ms, ss = xcorr.size2(side, side), xcorr.size2(2 * side - 1, 2 * side - 1)
+    fn = getattr(L, f"{name}_{suffix}")
+    d_left, d_right = dev(left, dt), dev(right, dt)  # held until the kernel has run
+    xcorr.check(fn(d_left.data_ptr(), d_right.data_ptr(), out.data_ptr(), ms, ss, *extra, st))
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().astype(np.float64) - (1.0 if adds else 0.0)
+    ref = oracle.run_mode(mode, left, right, dtype="f32acc64" if suffix == "f32" else "f64", threads=8)
+    assert rel_to_max(got, ref) <= (1e-5 if suffix == "f32" else 1e-12)
+
+
+def test_reference_launcher_limits():
+    """The reference's argument checks (src/naive_shuffle*.cu launchers;
+    release limits, CMakeLists.txt:16-43) return XC_ERR_INVALID_ARGUMENT."""
+    L = xcorr.lib()
+    p = 16  # never dereferenced: every call below is rejected first
+    ms, ss = xcorr.size2(8, 8), xcorr.size2(15, 15)
+    assert L.xc_run_ccn_shuffle_work_distribution_f32(p, p, p, ms, ss, 33, 4, 1, None) == 1  # warps > 32
+    assert L.xc_run_ccn_shuffle_work_distribution_f32(p, p, p, ms, ss, 8, 0, 2, None) == 1  # triangle, 0 rows
+    assert L.xc_run_ccn_shuffle_work_distribution_f32(p, p, p, ms, ss, 8, 4, 3, None) == 1  # unknown distribution
+    assert L.xc_run_ccn_shuffle_multimat_right_work_distribution_f32(p, p, p, ms, ss, 4, 8, 9, 4, 1, None) == 1
+    assert L.xc_run_ccn_shuffle_n_to_m_multimat_both_work_distribution_f64(p, p, p, ms, ss, 2, 2, 8, 5, 1, 4, 1,
+                                                                            None) == 1
+    assert L.xc_run_ccn_shuffle_multirow_right_f32(p, p, p, ms, ss, 8, 9, None) == 1
+    assert L.xc_run_ccn_shuffle_multirow_both_f32(p, p, p, ms, ss, 8, 4, 5, None) == 1
+    assert L.xc_run_ccn_shuffle_multirow_both_local_mem_f64(p, p, p, ms, ss, 8, 9, 2, None) == 1
+    assert L.xc_run_ccn_shuffle_multirow_right_multimat_right_f32(p, p, p, ms, ss, 3, 8, 5, 2, None) == 1
+    assert L.xc_run_ccn_shuffle_multirow_right_multimat_right_f32(p, p, p, ms, ss, 3, 8, 2, 0, None) == 1
+    assert L.xc_run_ccn_shuffle_multirow_right_f32(p, p, p, ms, xcorr.size2(16, 15), 8, 2, None) == 1  # search size
+
+
 def test_fft_glue_launchers():
     """hadamard_original / hadamard_n_to_m_over_output / scatter / normalize drop-ins."""
     L = xcorr.lib()
