@@ -357,6 +357,7 @@ def run_ours(args, rank, world, local_rank):
         line["ragged_n_to_m"] = ragged_study(torch, xcorr)
     if rank == 0 and not args.no_configs:
         line["configs"] = config_studies(torch, xcorr)
+        line["large_fft"] = large_fft_study(torch, xcorr)
     if rank == 0 and not args.no_cpu_baseline:
         rate, dt = cpu_reference_rate(left, right, 16, os.cpu_count() or 1)
         # the reference's cpu_* are single-threaded by construction: one core too
@@ -370,10 +371,78 @@ def run_ours(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def sampled_fp64(left, right, outs, ref_scale, rng, n_shifts):
+    """Max |out - exact| / scale over `n_shifts` shifts per output, each
+    summed in FP64 on the CPU (numpy) straight from the definition
+    out[sy + Hr-1][sx + Wr-1] = sum L[y+sy][x+sx] R[y][x]; every output also
+    gets its centre shift (the longest sum).  left (Hl, Wl), right (m, Hr,
+    Wr), outs (m, Sy, Sx) for one_to_many; scale[k] = max|exact| of output k."""
+    hl, wl = left.shape
+    _, hr, wr = right.shape
+    L = left.astype(np.float64)
+    worst = 0.0
+    for k in range(right.shape[0]):
+        R = right[k].astype(np.float64)
+        sys_ = np.concatenate([[hr - 1], rng.integers(0, hl + hr - 1, n_shifts - 1)])
+        sxs = np.concatenate([[wr - 1], rng.integers(0, wl + wr - 1, n_shifts - 1)])
+        for oy, ox in zip(sys_, sxs):
+            dy, dx = int(oy) - (hr - 1), int(ox) - (wr - 1)
+            y0, y1 = max(0, -dy), min(hr, hl - dy)
+            x0, x1 = max(0, -dx), min(wr, wl - dx)
+            exact = float(np.sum(L[y0 + dy:y1 + dy, x0 + dx:x1 + dx] * R[y0:y1, x0:x1]))
+            worst = max(worst, abs(float(outs[k][oy, ox]) - exact) / ref_scale[k])
+    return worst
+
+
+def large_fft_study(torch, xcorr, reps=5):
+    """one_to_many FP32 FFT, left 2048x2048 and 16 right 2048x2048 (U[0,1),
+    seed 5): 16 outputs of 4095x4095 from 4096x4096 transforms, where the
+    normalisation scales in FP64.  Error against the library's FP64 FFT
+    (all 16 outputs, full) and against FP64 sums on the CPU at 64 sampled
+    shifts per output (centre shift included)."""
+    rng = np.random.default_rng(5)
+    left = rng.random((1, 2048, 2048)).astype(np.float32)
+    right = rng.random((16, 2048, 2048)).astype(np.float32)
+    dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+    ws_bytes = xcorr.workspace_size("one_to_many", "f32", "fft", (2048, 2048), 1, (2048, 2048), 16)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    o = xcorr.correlate("one_to_many", dl, dr, method="fft", workspace=ws)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        xcorr.correlate("one_to_many", dl, dr, method="fft", out=o, workspace=ws)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    del ws
+    # the FP64 FFT of the same inputs, output by output (one right at a time
+    # keeps the FP64 workspace near 1 GB)
+    errs_fft, scales = [], []
+    dl64 = dl.double()
+    for k in range(16):
+        ref = xcorr.correlate("one_to_many", dl64, dr[k:k + 1].double(), method="fft")[0]
+        scale = float(ref.abs().max())
+        errs_fft.append(float((o[k].double() - ref).abs().max()) / scale)
+        scales.append(scale)
+        del ref
+    host = o.cpu().numpy()
+    err_cpu = sampled_fp64(left[0], right, host, scales, np.random.default_rng(55), 64)
+    del o, dl, dr, dl64
+    torch.cuda.empty_cache()
+    return {"config": "one_to_many 2048x2048 x 16 right U[0,1) seed 5", "dtype": "f32", "method": "fft",
+            "transform": [4096, 4096], "outputs": 16, "output_shape": [4095, 4095],
+            "correlations_per_s": 16 / (ms / 1000.0), "ms": ms,
+            "max_rel_err_vs_gpu_fp64_fft_all_outputs": max(errs_fft),
+            "max_rel_err_vs_cpu_fp64_64_sampled_shifts_per_output": err_cpu}
+
+
 def ragged_study(torch, xcorr, reps=5):
     """Ragged n_to_m batch (512 pairs, every side drawn from U{16..512}, values
     U[-1,1), seed 4): the persistent, graph-captured plan with its autotuned
-    tile shape against one plain-kernel launch per pair."""
+    tile shape against one plain-kernel launch per pair.  The CPU oracle
+    checks the 24 smallest and the 8 largest pairs (about 270 GMAC, run in a
+    background thread while the GPU timings run)."""
     import tempfile
 
     from oracle import oracle
@@ -386,6 +455,18 @@ def ragged_study(torch, xcorr, reps=5):
         lefts.append(rng.uniform(-1, 1, (hl, wl)).astype(np.float32))
         rights.append(rng.uniform(-1, 1, (hr, wr)).astype(np.float32))
     pairs = [(i, i) for i in range(512)]
+    by_work = sorted(range(512), key=lambda i: lefts[i].size * rights[i].size)
+    small, large = by_work[:24], by_work[-8:]
+    checked = small + large
+    refs = {}
+
+    def run_oracle():
+        res = oracle.run_pairs([lefts[i] for i in checked], [rights[i] for i in checked],
+                               threads=os.cpu_count() or 1)
+        refs.update(zip(checked, res))
+
+    worker = threading.Thread(target=run_oracle)
+    worker.start()
     plan = xcorr.RaggedPlan(lefts, rights, pairs)
     shape, tune_ms = plan.autotune()
     base = torch.zeros_like(plan.out)
@@ -405,16 +486,21 @@ def ragged_study(torch, xcorr, reps=5):
     ms_pairs = timed(lambda: plan.per_pair(base))
     outs, outs_b = plan.outputs(), plan.outputs(base)
     diff = max(oracle.max_rel_to_max(a, b) for a, b in zip(outs, outs_b))
-    small = sorted(range(512), key=lambda i: lefts[i].size * rights[i].size)[:24]
-    refs = oracle.run_pairs([lefts[i] for i in small], [rights[i] for i in small], threads=os.cpu_count() or 1)
-    err = max(oracle.max_rel_to_max(outs[i], r) for i, r in zip(small, refs))
+    worker.join()
+    err = max(oracle.max_rel_to_max(outs[i], refs[i]) for i in small)
+    err_large = max(oracle.max_rel_to_max(outs[i], refs[i]) for i in large)
+    err_large_pp = max(oracle.max_rel_to_max(outs_b[i], refs[i]) for i in large)
     flops = sum(2.0 * l.size * r.size for l, r in zip(lefts, rights))
     plan.close()
     return {"pairs": 512, "sides": "U{16..512} each of Hl, Wl, Hr, Wr", "values": "U[-1,1)", "seed": 4,
             "persistent_graph_ms": ms_graph, "per_pair_launches_ms": ms_pairs, "speedup": ms_pairs / ms_graph,
             "autotuned_tile_shape": shape, "autotune_ms": tune_ms,
             "correlations_per_s": 512 / (ms_graph / 1000.0), "tflops": flops / (ms_graph / 1000.0) / 1e12,
-            "max_rel_err_vs_oracle_24_smallest_pairs": err, "max_rel_diff_graph_vs_per_pair": diff}
+            "max_rel_err_vs_oracle_24_smallest_pairs": err,
+            "max_rel_err_vs_oracle_8_largest_pairs": err_large,
+            "largest_pairs_sides": [list(lefts[i].shape) + list(rights[i].shape) for i in large],
+            "per_pair_launches_max_rel_err_vs_oracle_8_largest_pairs": err_large_pp,
+            "max_rel_diff_graph_vs_per_pair": diff}
 
 
 def profiled_traffic(kernel):

@@ -246,6 +246,46 @@ def test_reference_launcher_limits():
     assert L.xc_run_ccn_shuffle_multirow_right_f32(p, p, p, ms, xcorr.size2(16, 15), 8, 2, None) == 1  # search size
 
 
+@pytest.mark.parametrize("dtype", ["f32", "f64"])
+def test_fft_transform_side_1024_or_more_small_right(dtype):
+    """Transform sides of 1024 or more normalise in FP64: a 1000x1000 left
+    with 40x40 rights (1039-point sides padded to a smooth size) against the
+    oracle, in FP32 and FP64."""
+    npdt = np.float32 if dtype == "f32" else np.float64
+    tdt = torch.float32 if dtype == "f32" else torch.float64
+    left = seeded((1, 1000, 1000), 71, dtype=npdt)
+    right = seeded((3, 40, 40), 72, "signed", dtype=npdt)
+    got = run("one_to_many", left, right, "fft", tdt)
+    ref = oracle.run_mode("one_to_many", left, right, dtype="f32acc64" if dtype == "f32" else "f64", threads=8)
+    assert rel_to_max(got, ref) <= (1e-5 if dtype == "f32" else 1e-10)
+
+
+def test_fft_equal_sides_1024_against_fp64():
+    """1024x1024 left and two 1024x1024 rights (2048x2048 transforms), FP32
+    FFT: every output against the library's FP64 FFT of the same inputs, and
+    against FP64 sums on the CPU at 48 sampled shifts per output (the centre
+    shift, the longest sum, included)."""
+    left = seeded((1, 1024, 1024), 73)
+    right = seeded((2, 1024, 1024), 74)
+    got = run("one_to_many", left, right, "fft")
+    ref = run("one_to_many", left.astype(np.float64), right.astype(np.float64), "fft", torch.float64)
+    assert rel_to_max(got, ref) <= 1e-5
+    rng = np.random.default_rng(75)
+    L = left[0].astype(np.float64)
+    for k in range(2):
+        R = right[k].astype(np.float64)
+        scale = np.abs(ref[k]).max()
+        oys = np.concatenate([[1023], rng.integers(0, 2047, 47)])
+        oxs = np.concatenate([[1023], rng.integers(0, 2047, 47)])
+        for oy, ox in zip(oys, oxs):
+            dy, dx = int(oy) - 1023, int(ox) - 1023
+            y0, y1 = max(0, -dy), min(1024, 1024 - dy)
+            x0, x1 = max(0, -dx), min(1024, 1024 - dx)
+            exact = np.sum(L[y0 + dy:y1 + dy, x0 + dx:x1 + dx] * R[y0:y1, x0:x1])
+            assert abs(got[k][oy, ox] - exact) / scale <= 1e-5
+            assert abs(ref[k][oy, ox] - exact) / scale <= 1e-10
+
+
 def test_fft_glue_launchers():
     """hadamard_original / hadamard_n_to_m_over_output / scatter / normalize drop-ins."""
     L = xcorr.lib()

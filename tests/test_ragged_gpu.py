@@ -97,3 +97,24 @@ def test_ragged_shared_matrices_n_to_m_style():
     torch.cuda.synchronize()
     check_outputs(plan.outputs(), lefts, rights, pairs)
     plan.close()
+
+
+def test_ragged_largest_pairs_match_oracle():
+    """Pairs with every side near the top of the U{16..512} range of the
+    512-pair batch, where FP32 chains are longest (the batch's checks in the
+    bench cover its 8 largest pairs the same way)."""
+    rng = np.random.default_rng(44)
+    lefts = [rng.uniform(-1, 1, (512, 497)).astype(np.float32), rng.uniform(-1, 1, (479, 512)).astype(np.float32)]
+    rights = [rng.uniform(-1, 1, (505, 488)).astype(np.float32), rng.uniform(-1, 1, (512, 509)).astype(np.float32)]
+    pairs = [(0, 0), (1, 1)]
+    plan = xcorr.RaggedPlan(lefts, rights, pairs)
+    plan.execute()
+    base = torch.zeros_like(plan.out)
+    plan.per_pair(base)
+    torch.cuda.synchronize()
+    # one pair at a time, its rows over all host threads
+    refs = [oracle.run_mode("one_to_one", a, b, threads=os.cpu_count() or 1)[0] for a, b in zip(lefts, rights)]
+    for got, got_pp, ref in zip(plan.outputs(), plan.outputs(base), refs):
+        assert rel_to_max(got, ref) <= 1e-5
+        assert rel_to_max(got_pp, ref) <= 1e-5
+    plan.close()
