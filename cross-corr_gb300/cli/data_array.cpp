@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cerrno>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -33,28 +34,75 @@ void split_csv(const std::string& line, std::vector<std::string>& out) {
   }
 }
 
+// Worker threads for CSV parsing and formatting: the host's cores, at most
+// 16, and at most one per 256 rows.
+int csv_threads(size_t rows) {
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  return (int)std::max<size_t>(1, std::min<size_t>({(size_t)std::min(hw, 16u), rows / 256 + 1}));
+}
+
+// Runs fn(lo, hi) over [0, n) split into `threads` contiguous ranges.
+template <typename F>
+void parallel_rows(size_t n, int threads, F fn) {
+  if (threads <= 1) {
+    fn((size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const size_t per = (n + threads - 1) / threads;
+  for (int t = 1; t < threads; ++t) {
+    const size_t lo = std::min(n, per * t), hi = std::min(n, lo + per);
+    pool.emplace_back([=, &fn] { fn(lo, hi); });
+  }
+  fn((size_t)0, std::min(n, per));
+  for (auto& th : pool) th.join();
+}
+
+// One value of a data line: leading and trailing blanks and a leading '+'
+// allowed, as strtod accepts them; correctly rounded to T.
 template <typename T>
-T parse_value(const std::string& s, size_t row) {
-  const char* b = s.c_str();
-  while (*b == ' ' || *b == '\t') ++b;
-  char* end = nullptr;
-  errno = 0;
-  double v = std::strtod(b, &end);
-  if (end == b) throw std::runtime_error("Invalid value \"" + s + "\" on data line " + std::to_string(row));
-  while (*end == ' ' || *end == '\t' || *end == '\r') ++end;
-  if (*end != '\0') throw std::runtime_error("Invalid value \"" + s + "\" on data line " + std::to_string(row));
-  return static_cast<T>(v);
+bool parse_token(const char* b, const char* e, T* v) {
+  while (b < e && (*b == ' ' || *b == '\t')) ++b;
+  while (e > b && (e[-1] == ' ' || e[-1] == '\t' || e[-1] == '\r')) --e;
+  if (b < e && *b == '+' && e - b > 1 && b[1] != '-') ++b;
+  if (b == e) return false;
+  const auto r = std::from_chars(b, e, *v);
+  return r.ec == std::errc() && r.ptr == e;
 }
 
 }  // namespace
 
-// read_header / read_data (src/matrix.hpp:94-159).
+// read_header / read_data (src/matrix.hpp:94-159): the same header rules and
+// messages.  The file is read whole; its data lines are found with one memchr
+// pass and parsed by several threads (std::from_chars), each over a range of
+// lines.  A malformed line reports the same message the reference gives; the
+// first such line in file order wins.
 template <typename T>
 data_array<T> load_csv(const std::string& path) {
-  std::ifstream in(path);
-  if (!in) throw std::runtime_error("Could not open file " + path);
-  std::string line;
-  if (!std::getline(in, line)) throw std::runtime_error("Could not read file header");
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (f == nullptr) throw std::runtime_error("Could not open file " + path);
+  std::string buf;
+  {
+    char chunk[1 << 16];
+    size_t n;
+    while ((n = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.append(chunk, n);
+    std::fclose(f);
+  }
+  const char* base = buf.data();
+  const size_t size = buf.size();
+  size_t pos = 0;
+  auto next_line = [&](size_t* b, size_t* e) {  // getline: false at end of input
+    if (pos >= size) return false;
+    const void* nl = std::memchr(base + pos, '\n', size - pos);
+    *b = pos;
+    *e = nl ? (size_t)((const char*)nl - base) : size;
+    pos = *e + 1;
+    return true;
+  };
+  size_t hb, he;
+  if (!next_line(&hb, &he)) throw std::runtime_error("Could not read file header");
+  std::string line(base + hb, he - hb);
+  if (!line.empty() && line.back() == '\r') line.pop_back();
   if (line.compare(0, 2, "# ") != 0) throw std::runtime_error("Invalid file header format");
   std::vector<std::string> tok;
   split_csv(line.substr(2), tok);
@@ -69,49 +117,95 @@ data_array<T> load_csv(const std::string& path) {
   const uint32_t rows = to_u32(tok[0]), cols = to_u32(tok[1]);
   const uint32_t count = tok.size() == 3 ? to_u32(tok[2]) : 1;
   data_array<T> a(rows, cols, count);
-  size_t total_rows = (size_t)rows * count;
-  T* dst = a.data.data();
-  for (size_t y = 0; y < total_rows; ++y) {
-    if (!std::getline(in, line))
+  const size_t total_rows = (size_t)rows * count;
+  std::vector<size_t> lb(total_rows), le(total_rows);
+  for (size_t y = 0; y < total_rows; ++y)
+    if (!next_line(&lb[y], &le[y]))
       throw std::runtime_error("Failed to read line " + std::to_string(y % rows) + " from csv file");
-    if (!line.empty() && line.back() == '\r') line.pop_back();
-    split_csv(line, tok);
-    if (tok.size() > cols)
-      throw std::runtime_error("Line " + std::to_string(y % rows) + " is too long, expected " + std::to_string(cols) +
-                               "values");
-    if (tok.size() < cols)
-      throw std::runtime_error("Line" + std::to_string(y % rows) + " is too short, expected " + std::to_string(cols) +
-                               ", got " + std::to_string(tok.size()) + " values");
-    for (uint32_t x = 0; x < cols; ++x) dst[x] = parse_value<T>(tok[x], y);
-    dst += cols;
-  }
+  // per thread: the first bad line of its range and its message
+  const int threads = csv_threads(total_rows);
+  std::vector<size_t> bad_row(threads, (size_t)-1);
+  std::vector<std::string> bad_msg(threads);
+  T* out = a.data.data();
+  const size_t per = (total_rows + threads - 1) / std::max(1, threads);
+  parallel_rows(total_rows, threads, [&](size_t lo, size_t hi) {
+    const int t = (int)(lo / std::max<size_t>(1, per));
+    for (size_t y = lo; y < hi; ++y) {
+      const char* b = base + lb[y];
+      const char* e = base + le[y];
+      if (e > b && e[-1] == '\r') --e;
+      size_t n_tok = 1;
+      for (const char* q = b; q < e; ++q) n_tok += *q == ',';
+      std::string msg;
+      if (n_tok > cols) {
+        msg = "Line " + std::to_string(y % rows) + " is too long, expected " + std::to_string(cols) + "values";
+      } else if (n_tok < cols) {
+        msg = "Line" + std::to_string(y % rows) + " is too short, expected " + std::to_string(cols) + ", got " +
+              std::to_string(n_tok) + " values";
+      } else {
+        T* dst = out + y * cols;
+        const char* q = b;
+        for (uint32_t x = 0; x < cols; ++x) {
+          const char* c = x + 1 < cols ? static_cast<const char*>(std::memchr(q, ',', (size_t)(e - q))) : e;
+          if (!parse_token<T>(q, c, dst + x)) {
+            msg = "Invalid value \"" + std::string(q, c) + "\" on data line " + std::to_string(y);
+            break;
+          }
+          q = c + 1;
+        }
+      }
+      if (!msg.empty()) {
+        bad_row[t] = y;
+        bad_msg[t] = msg;
+        return;
+      }
+    }
+  });
+  for (int t = 0; t < threads; ++t)
+    if (bad_row[t] != (size_t)-1) throw std::runtime_error(bad_msg[t]);
   return a;
 }
 
 // write_header / write_data (src/matrix.hpp:161-185), with the row stride
 // fixed (the reference strides rows by matrix_size.y, src/matrix.hpp:180) and
-// round-trip precision instead of 6 fixed decimals.
+// the shortest round-trip representation (std::to_chars) instead of 6 fixed
+// decimals.  Ranges of rows are formatted by several threads and written in
+// order.
 template <typename T>
 void store_csv(const std::string& path, const data_array<T>& a) {
-  FILE* f = std::fopen(path.c_str(), "w");
+  FILE* f = std::fopen(path.c_str(), "wb");
   if (f == nullptr) throw std::runtime_error("Could not open output file " + path);
   std::fprintf(f, "# %u,%u,%u\n", a.rows, a.cols, a.count);
-  const char* fmt = sizeof(T) == 4 ? "%.9g" : "%.17g";
-  std::string buf;
-  char num[64];
   const size_t total_rows = (size_t)a.rows * a.count;
-  for (size_t y = 0; y < total_rows; ++y) {
-    buf.clear();
-    const T* row = a.data.data() + y * a.cols;
-    for (uint32_t x = 0; x < a.cols; ++x) {
-      if (x) buf.push_back(',');
-      int n = std::snprintf(num, sizeof(num), fmt, (double)row[x]);
-      buf.append(num, (size_t)n);
-    }
-    buf.push_back('\n');
-    std::fwrite(buf.data(), 1, buf.size(), f);
+  const int threads = csv_threads(total_rows);
+  // blocks of rows: each formatted into its own buffer, written in order
+  const size_t block = 4096;
+  const size_t n_blocks = (total_rows + block - 1) / block;
+  bool ok = true;
+  for (size_t g0 = 0; g0 < n_blocks && ok; g0 += (size_t)threads) {
+    const size_t g1 = std::min(n_blocks, g0 + (size_t)threads);
+    std::vector<std::string> bufs(g1 - g0);
+    parallel_rows(g1 - g0, (int)(g1 - g0), [&](size_t lo, size_t hi) {
+      char num[64];
+      for (size_t g = lo; g < hi; ++g) {
+        std::string& out = bufs[g];
+        const size_t y0 = (g0 + g) * block, y1 = std::min(total_rows, y0 + block);
+        out.reserve((y1 - y0) * a.cols * 12);
+        for (size_t y = y0; y < y1; ++y) {
+          const T* row = a.data.data() + y * a.cols;
+          for (uint32_t x = 0; x < a.cols; ++x) {
+            if (x) out.push_back(',');
+            const auto r = std::to_chars(num, num + sizeof(num), row[x]);
+            out.append(num, (size_t)(r.ptr - num));
+          }
+          out.push_back('\n');
+        }
+      }
+    });
+    for (const auto& b : bufs)
+      if (std::fwrite(b.data(), 1, b.size(), f) != b.size()) ok = false;
   }
-  if (std::fclose(f) != 0) throw std::runtime_error("Failed to write " + path);
+  if (std::fclose(f) != 0 || !ok) throw std::runtime_error("Failed to write " + path);
 }
 
 template <typename T>

@@ -126,3 +126,45 @@ def test_measurement_csv_for_cpu_algorithm(tmp_path):
     assert rows[0] == ("Load,Load_iterations,Prepare,Prepare_iterations,Transfer,Transfer_iterations,Run,"
                        "Run_iterations,Finalize,Finalize_iterations,Free,Free_iterations,Store,Store_iterations")
     assert len(rows) == 3 and all(len(x.split(",")) == 14 for x in rows[1:])
+
+
+def test_csv_reader_edge_cases_and_round_trip(tmp_path):
+    """The CSV reader (read_header / read_data, src/matrix.hpp:94-159): CRLF
+    line ends, blanks and a leading '+', malformed lines reported with the
+    reference's messages (the first bad line in file order), and a round
+    trip of a multi-threaded store and load through the cpu_* path."""
+    good = tmp_path / "good.csv"
+    good.write_bytes(b"# 2,3,1\r\n1, +2.5 ,3e-1\r\n-4,5.0,6\r\n")
+    out = tmp_path / "out.csv"
+    r = cross("run", "-p", "-o", str(out), "cpu_one_to_one", str(good), str(good))
+    assert r.returncode == 0, r.stderr
+    m = np.array([[1, 2.5, 0.3], [-4, 5, 6]])
+    exp = oracle.run_mode("one_to_one", m[None], m[None], dtype="f64")[0]
+    np.testing.assert_allclose(oracle.read_csv(str(out))[0], exp, rtol=1e-6)
+    cases = [(b"# 2,3\n1,2,3\n4,5,6,7\n", "Line 1 is too long"),
+             (b"# 2,3\n1,2\n4,5,6\n", "Line0 is too short, expected 3, got 2 values"),
+             (b"# 2,3\n1,2,3\n4,x,6\n", 'Invalid value "x"'),
+             (b"# 3,3\n1,2,3\n4,5,6\n", "Failed to read line 2 from csv file"),
+             (b"# 2,3\n1,2,3\n4,5\n1,2\n", "Line1 is too short"),
+             (b"2,3\n1,2,3\n", "Invalid file header format")]
+    for k, (text, msg) in enumerate(cases):
+        bad = tmp_path / f"bad{k}.csv"
+        bad.write_bytes(text)
+        r = cross("run", "-p", "cpu_one_to_one", str(bad), str(good))
+        assert r.returncode == 3 and msg in r.stderr, (text, r.stderr)
+    # a larger file: rows spread over the parser's threads; one_to_many output
+    # (9 matrices) written by the formatter's threads and read back exactly
+    rng = np.random.default_rng(9)
+    left = rng.standard_normal((1, 40, 37)).astype(np.float32)
+    right = rng.standard_normal((9, 40, 37)).astype(np.float32)
+    lp, rp, op = tmp_path / "l.csv", tmp_path / "r.csv", tmp_path / "o.csv"
+    for path, a in ((lp, left), (rp, right)):
+        with open(path, "w") as f:
+            f.write(f"# {a.shape[1]},{a.shape[2]},{a.shape[0]}\n")
+            for row in a.reshape(-1, a.shape[2]):
+                f.write(",".join(repr(float(v)) for v in row) + "\n")
+    r = cross("run", "-p", "-o", str(op), "cpu_one_to_many", str(lp), str(rp))
+    assert r.returncode == 0, r.stderr
+    got = oracle.read_csv(str(op))
+    ref = oracle.run_mode("one_to_many", left, right, dtype="f32")
+    np.testing.assert_array_equal(got.astype(np.float32), ref.astype(np.float32))
