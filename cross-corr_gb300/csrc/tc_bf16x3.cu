@@ -11,45 +11,51 @@
 // Formulation (implicit GEMM).  For a left row a and a right row b the
 // contribution to output row sy = a - b + Hr - 1 is a 1D correlation, a
 // Toeplitz matrix-vector product.  One tcgen05.mma computes
-//     D[m][n] += sum_k A[m][k] * B[n][k]        (M=128, N=256, K=16, BF16)
+//     D[m][n] += sum_k A[m][k] * B[n][k]        (M=128, N<=256, K=16, BF16)
 // with
-//   m -> column shift sx = s0 + m of a 128-shift tile:
-//        A[m][k] = Lp_a[s0 + m + k0 + k], Lp_a[j] = L[a][j - (Wr-1)] (zero
-//        outside the row).
-//   n -> (partner matrix p, row shift dy): B[n][k] = R_p[a - dy][k0 + k]
-//        (right rows, staged by TMA with 128-byte swizzle, K-major).
+//   m -> (partner matrix p, row shift dy): A[m][k] = R_p[a - dy][k0 + k]
+//        (right rows, staged by TMA with 128-byte swizzle, K-major);
+//   n -> column shift sx = w0 + n: B[n][k] = Lp_a[w0 + n + k0 + k],
+//        Lp_a[j] = L[a][j - (Wr-1)] (zero outside the row).
+// The shifts lie along N, i.e. along tensor-memory columns: the accumulator
+// of a shift half is 128 lanes x 256 columns, and each K-step's MMA covers
+// only the shifts whose overlap with the K-step's 16 right columns is not
+// empty -- a window that slides along the diagonal of the (shift, column)
+// plane, placed by the MMA's tensor-memory column offset and N.  A fixed
+// 128-shift tile along M would multiply zeros over the triangles where that
+// diagonal crosses it (half of every crossed tile: 1.5x the algorithmic work
+// at Wl = Wr = 256); the windows waste only their rounding to 16 shifts.
+// The first MMA of an accumulation window covers the whole half, which also
+// starts every column of the accumulator afresh.
 //
-// The Toeplitz operand A is read from shared memory through an ordinary
+// The Toeplitz operand B is read from shared memory through an ordinary
 // matrix descriptor.  In the K-major layout without swizzle an 8-row x
 // 16-byte core matrix (r, t) sits at start + 16 r + e t (e = element bytes)
-// and core matrices are LBO apart along K and SBO apart along M.  Element
-// (m, k) lands at 128 (m/8 + k/8) + 16 (m%8) + 2 (k%8) for BF16 with
-// LBO = SBO = 128 bytes, and its value Lp[c + m + k] depends only on
-// 8 (m/8 + k/8) + m%8 + k%8, so one buffer T[q][r][t] = X[8 q + r + t] of
-// 8-element core matrices serves every shift tile and K-step as an offset of
-// the start address: builder warps write T once per left row (16 KB for the
-// hi and lo parts) instead of a Toeplitz matrix per K-step.  TF32 (4-element
-// core-matrix rows): T[q][r][t] = X[4 q + r + t], LBO = 128, SBO = 256.
-// N = 256: a 128x256x16 MMA reads 4 KB of A and 8 KB of B in 128 cycles,
-// 96 bytes per clock of the 128 shared memory delivers; at N = 128 the same
-// operands would need all of it.  Measured on GB300, this operand form runs
-// at 4095 MAC/clk/SM (the tensor pipe's peak).  The shift axis lies along M,
-// so K-steps whose 128 shifts see only zeros are skipped (a quarter of them
-// at Wl = Wr).
+// and core matrices are LBO apart along K and SBO apart along N.  Element
+// (n, k) lands at 128 (n/8 + k/8) + 16 (n%8) + 2 (k%8) for BF16 with
+// LBO = SBO = 128 bytes, and its value Lp[c + n + k] depends only on
+// 8 (n/8 + k/8) + n%8 + k%8, so one buffer T[q][r][t] = X[8 q + r + t] of
+// 8-element core matrices serves every window and K-step as an offset of
+// the start address: builder warps write T once per left row instead of a
+// Toeplitz matrix per K-step.  TF32 (4-element core-matrix rows):
+// T[q][r][t] = X[4 q + r + t], LBO = 128, SBO = 256.
 //
-// A work item is two shift tiles (256 shifts) of one (partner group,
-// row-shift group, chunk of left rows); a second item covers the other two
-// when Sx > 256.  The kernel is persistent (one CTA per SM) and walks a
-// device-built list of the items.  Tensor memory holds the two 128x256 FP32
-// accumulators (all 512 columns).  Every few left rows (the window, chosen
-// per left matrix and partner group from the data's statistics) the epilogue
-// warps read the accumulators and add them to the output with coalesced
-// red.global.add (consecutive lanes are consecutive shifts).
+// A work item is every shift of one (partner group, row-shift group, chunk
+// of left rows); two issuer threads each issue one shift half's MMAs (one
+// thread alone cannot issue the small windows fast enough: measured, about
+// 79 cycles per MMA from one thread, at the pipe's rate from two).  The
+// kernel is persistent (one CTA per SM) and walks a device-built list of the
+// items.  Tensor memory holds the two halves' FP32 accumulators (all 512
+// columns).  Every few left rows (the window, chosen per left matrix and
+// partner group from the data's statistics) the epilogue warps read the
+// accumulators and add them to the output with red.global.add, through a
+// small shared-memory transpose so that each reduction instruction covers
+// consecutive shifts.
 //
 // Right tiles come in stages of one plane (hi or lo) of one 128-byte column
-// chunk (256 rows x 128 bytes).  Per chunk the MMAs that read the hi plane
-// (A_hi B_hi and A_lo B_hi) run first, then those that read the lo plane
-// (A_hi B_lo), so each stage is released as soon as its own MMAs finish.
+// chunk (128 rows x 128 bytes).  Per chunk the MMAs that read the hi plane
+// (R_hi L_hi and R_hi L_lo) run first, then those that read the lo plane
+// (R_lo L_hi), so each stage is released as soon as its own MMAs finish.
 //
 // Accuracy.  Tensor-core FP32 accumulation drops low bits on every MMA with a
 // consistent sign, so the error of a long chain grows linearly with its
@@ -64,18 +70,15 @@
 //
 // Warp roles (736 threads, one CTA per SM):
 //   warp 0      TMA producer of the right-row tiles
-//   warp 1      TMEM allocation; one thread issues the MMAs of shift tile 0
-//   warp 22     one thread issues the MMAs of shift tile 1
-//               (with XC_TC_ISSUERS=1, 704 threads: warp 1 issues both)
+//   warp 1      TMEM allocation; one thread issues the MMAs of shift half 0
+//   warp 22     one thread issues the MMAs of shift half 1
 //   warps 2-5   builders of the Toeplitz core-matrix buffer (two row buffers)
-//   warps 6-21  epilogue: 4 per TMEM lane quadrant, 128 accumulator columns each
-// Each tile's accumulator is drained on its own schedule, the two offset by
-// half a window: while the epilogue drains one tile, the other tile's issuer
+//   warps 6-21  epilogue: eight per half, two per TMEM lane quadrant
+// Each half's accumulator is drained on its own schedule, the two offset by
+// half a window: while the epilogue drains one half, the other half's issuer
 // keeps the tensor pipe busy (as far as the shared right-tile stages allow).
-// The issue loops are on the critical path (a lone thread barely keeps up
-// with 128x256x16 MMAs): a stage's MMAs are one straight block under guard
-// predicates, and the next stage's barrier is looked at before the current
-// stage's MMAs are issued.
+// A stage's MMAs are one straight block under guard predicates, and the next
+// stage's barrier is looked at before the current stage's MMAs are issued.
 // All waits are bounded: an expired wait records a flag, the CTA winds down,
 // waits (bounded) for its own copies and MMAs, frees TMEM and returns.
 #include <cuda_bf16.h>
@@ -97,31 +100,35 @@ namespace xc {
 
 namespace {
 
-constexpr int kN = 256;                 // B rows per MMA: P partners x DY row shifts
-constexpr int kStageBytes = kN * 128;   // one plane of one 128-byte column chunk
+constexpr int kLanes = 128;                // A rows per MMA: P partners x DY row shifts
+constexpr int kStageBytes = kLanes * 128;  // one plane of one 128-byte column chunk
+constexpr int kHalfCols = 256;             // tensor-memory columns per shift half
 constexpr int kBuilderWarps = 4;
-constexpr int kEpiWarps = 16;           // four per TMEM lane quadrant
-// MMA issuer threads: 2 (one per shift tile, warps 1 and 22) or 1 (warp 1
-// issues both tiles)
-#ifndef XC_TC_ISSUERS
-#define XC_TC_ISSUERS 2
-#endif
-constexpr int kIssuers = XC_TC_ISSUERS;
-// warp 0 producer, warps 1 (and 22) MMA issuers, 2-5 builders, 6-21 epilogue
-constexpr int kThreads = 32 * (2 + (kIssuers - 1) + kBuilderWarps + kEpiWarps);
-constexpr int kXLen = 520;              // staged row elements: the 511 a two-tile item reads, padded
-constexpr int kBarBytes = 256;          // 20 mbarriers at most, the abort flag, the TMEM address slot
-constexpr int kMaxChunkRows = 1024;     // left rows per work item at most
+constexpr int kEpiWarps = 16;              // eight per shift half, two per TMEM lane quadrant
+// warp 0 producer, warps 1 and 22 MMA issuers (one per shift half), 2-5
+// builders, 6-21 epilogue
+constexpr int kThreads = 32 * (3 + kBuilderWarps + kEpiWarps);
+constexpr int kIssuer1Warp = 2 + kBuilderWarps + kEpiWarps;
+constexpr int kXLen = 792;                 // staged row elements: every shift plus a right row, padded
+constexpr int kBarBytes = 256;             // 20 mbarriers at most, the abort flag, the TMEM address slot
+constexpr int kMaxChunkRows = 1024;        // left rows per work item at most
+constexpr int kMaxKSteps = 32;             // K-steps of a 256-column right row (16 BF16 or 32 TF32)
+constexpr int kTrans = 17;                 // padded row of an epilogue warp's 32 x 16 transpose tile
 
 // Per operand type: right-tile stages and the Toeplitz buffer (hi or lo part
-// of one left row): 64 core matrices of 8 BF16 or 128 of 4 FP32.
+// of one left row): core matrices of 8 BF16 or 4 FP32 per 16-byte row,
+// covering X[0, 776) (every shift of both halves plus a right row).
 template <bool TF>
 struct TcCfg {
-  static constexpr int kStages = TF ? 4 : 5;
+  static constexpr int kStages = TF ? 4 : 7;
   static constexpr int kCm = TF ? 4 : 8;            // elements per 16-byte core-matrix row
-  static constexpr int kQ = TF ? 128 : 64;          // core matrices in T
+  static constexpr int kQ = TF ? 194 : 98;          // core matrices in T
   static constexpr int kTBytes = kQ * 128;          // one plane of T
-  static constexpr int kSmem = 1024 + kStages * kStageBytes + 4 * kTBytes + 4 * kXLen * 4 + kBarBytes;
+  static constexpr int kTransBytes = kEpiWarps * 32 * kTrans * 4;
+  static constexpr int kOffBytes = kEpiWarps * 32 * 8;
+  static constexpr int kSmem = 1024 + kStages * kStageBytes + 4 * kTBytes + 4 * kXLen * 4 + kTransBytes +
+                               kOffBytes + kBarBytes;
+  static_assert(kCm * (kQ - 1) + 7 + kCm - 1 < kXLen, "T reads inside the staged row");
 };
 
 struct TcParams {
@@ -130,13 +137,21 @@ struct TcParams {
   float* out;
   int Hl, Wl, Hr, Wr, Sy, Sx;
   PairMap pm;
-  int P, DY;        // partners x row shifts per B tile, P*DY = 256
+  int P, DY;        // partners x row shifts per A tile, P*DY = 128
   int mats_mode;    // 1: one TMA box per row shift spans P partners; 0: one box per partner spans DY rows
   int n_pgroups;    // ceil(K / P)
   int n_dytiles;    // ceil(Sy / DY)
-  int n_halves;     // work items across the shifts (two 128-shift tiles each)
+  int n_halves;     // 1: a work item covers every shift (both tensor-memory halves)
+  int half_w;       // shifts per half (a multiple of 16, at most 256): half h covers [h half_w, (h+1) half_w)
   int nkc;          // 128-byte column chunks of a right row (64 BF16 or 32 TF32 columns)
   int kstep;        // columns per K-step: 16 (BF16) or 8 (TF32)
+  // The MMA window of each (half, K-step): the shifts whose overlap with the
+  // K-step's right columns is not empty, rounded out to 16.  Packed: TMEM
+  // column (bits 0-8), N / 16 (9-13), active (14), Toeplitz core-matrix
+  // offset (16-23).  kreset: the whole half (the first MMA of a window,
+  // which also zeroes the accumulator).
+  uint32_t ktab[2][kMaxKSteps];
+  uint32_t kreset[2];
   const int* flush_tab;  // drain TMEM every this many left rows, per (left matrix, partner group)
   int chunk_rows;   // left rows per work item (a longer row range is split over items)
   const int* items;  // non-empty work items, most left rows first (tc_item encoding)
@@ -152,8 +167,7 @@ struct TcParams {
   // Host-built schedule (banded launches), or null: CTA c takes entry
   // r * gridDim.x + c in round r, *n_live entries in all.  An entry is
   // {tile key, first left row (from the tile's first), left rows, 0}, the
-  // tile key (rank * per_rank + lp) * n_halves + half as in tc_item; key -1:
-  // nothing.
+  // tile key rank * per_rank + lp as in tc_item; key -1: nothing.
   const int4* sched;
   const int* n_live; // entries of `items` (written on the device)
   int n_chunks;     // chunks per (dy tile): ceil(max rows / chunk_rows)
@@ -178,8 +192,11 @@ __host__ __device__ constexpr uint32_t idesc_tf32_f32(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// The same, issued only when `exec` is non-zero (a guard predicate instead
-// of a branch keeps a stage's MMAs one straight block of code).
+// D[tmem] (+)= A[smem] * B[smem]^T, both operands through descriptors, issued
+// only when `exec` is non-zero (a guard predicate instead of a branch keeps a
+// stage's MMAs one straight block of code).  No memory clobber: the MMA reads
+// shared memory asynchronously, and volatile keeps it in order with the
+// barrier waits and commits around it.
 template <bool TF>
 __device__ __forceinline__ void mma_ss_if(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate, uint32_t exec) {
@@ -204,26 +221,6 @@ __device__ __forceinline__ float tf32_round(float x) {
   uint32_t r;
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return __uint_as_float(r);
-}
-
-// D[tmem] (+)= A[smem] * B[smem]^T, both operands through descriptors.  No
-// memory clobber: the MMA reads shared memory asynchronously, and volatile
-// keeps it in order with the barrier waits and commits around it.
-template <bool TF>
-__device__ __forceinline__ void mma_ss(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                       uint32_t accumulate) {
-  if constexpr (TF)
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-  else
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ uint64_t make_desc(uint32_t lo, uint32_t hi) {
@@ -255,12 +252,9 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ void red_add(float* addr, float v) {
-  asm volatile("red.global.add.f32 [%0], %1;" ::"l"(addr), "f"(v) : "memory");
-}
-
-// The same under a predicate (no branch: a drain's 32 adds stay one straight
-// block the compiler can schedule; the address of a false one is not used).
+// red.global.add under a predicate (no branch: a drain's adds stay one
+// straight block the compiler can schedule; the address of a false one is
+// not used).
 __device__ __forceinline__ void red_add_if(float* addr, float v, uint32_t pred) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
@@ -325,33 +319,44 @@ __device__ __forceinline__ bool bar_red_or(bool v, int id, int nthreads) {
   return r != 0;
 }
 
-// Active K-steps of a 128-shift tile starting at s0: bit j is set when
-// A's K-step j (right columns kstep*j .. kstep*j + kstep - 1) meets a left
-// column.
-__host__ __device__ __forceinline__ uint32_t tile_mask(int s0, const TcParams& p) {
-  uint32_t m = 0;
-  if (s0 >= p.Sx) return 0;
-  for (int j = 0; j < 4 * p.nkc; ++j) {
-    const int k0 = p.kstep * j;
-    if (k0 < p.Wr && s0 + k0 + 127 + p.kstep - 1 >= p.Wr - 1 && s0 + k0 <= p.Wr + p.Wl - 2) m |= 1u << j;
-  }
-  return m;
+// The window of half h and K-step j (right columns kstep*j ..): shifts sx
+// whose left columns sx + k - (Wr-1) meet the row for some column k of the
+// K-step, clipped to the half and rounded out to 16; packed as in ktab.  The
+// MMA's B operand starts at X[w0 + kstep*j] (X[i] = centred left row at
+// column i - (Wr-1)), core matrix (w0 + kstep*j) / kCm.
+inline uint32_t pack_window(int dcol, int n, bool active, int bq) {
+  return (uint32_t)dcol | ((uint32_t)(n / 16) << 9) | ((active ? 1u : 0u) << 14) | ((uint32_t)bq << 16);
 }
 
-// One work item: two 128-shift tiles (one CTA half) of one (left matrix,
-// partner group, row-shift group, chunk of left rows).
+inline void kstep_windows(int Wl, int Wr, int Sx, int half_w, int kstep, int cm, int nks, uint32_t ktab[2][kMaxKSteps],
+                          uint32_t kreset[2]) {
+  for (int h = 0; h < 2; ++h) {
+    const int H0 = h * half_w, H1 = std::min(Sx, H0 + half_w);
+    kreset[h] = pack_window(h * kHalfCols, half_w, true, H0 / cm);
+    for (int j = 0; j < kMaxKSteps; ++j) {
+      ktab[h][j] = 0;
+      const int k0 = j * kstep;
+      if (j >= nks || k0 >= Wr || H0 >= H1) continue;
+      const int k_hi = std::min(k0 + kstep, Wr) - 1;
+      const int lo = std::max(H0, Wr - 1 - k_hi), hi = std::min(H1, Wr - 1 + Wl - k0);
+      if (lo >= hi) continue;
+      const int w0 = H0 + (lo - H0) / 16 * 16;
+      const int n = (hi - w0 + 15) / 16 * 16;
+      ktab[h][j] = pack_window(h * kHalfCols + (w0 - H0), n, true, (w0 + k0) / cm);
+    }
+  }
+}
+
+// One work item: every shift of one (left matrix, partner group, row-shift
+// group, chunk of left rows).
 struct TcItem {
-  int l, p0, dy0, a_lo, n_rows, rdim2, s0_0, s0_1;
-  uint32_t mask0, mask1;
+  int l, p0, dy0, a_lo, n_rows, rdim2;
   int band;  // output row band of the item's row-shift tile
 };
 
-// idx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_halves + half;
-// false when the item has no left rows.
-// The item of tile key (rank, lp, half) covering the tile's left rows
+// The item of tile key (rank, lp) covering the tile's left rows
 // [row0, row0 + n) (clipped to the tile); false when that is empty.
-__host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int half, int lp, int rank, int row0, int n,
-                                                  TcItem* w) {
+__host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int lp, int rank, int row0, int n, TcItem* w) {
   w->l = lp / p.n_pgroups;
   w->p0 = (lp % p.n_pgroups) * p.P;
   const int t = centre_out(rank, p.n_dytiles, (p.Hr - 1) / p.DY);
@@ -362,32 +367,27 @@ __host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int half, i
   const int a_hi = min(tile_hi, w->a_lo + n);
   w->n_rows = a_hi - w->a_lo;
   w->rdim2 = p.pm.r_l != 0 ? w->l : 0;
-  w->s0_0 = 256 * half;
-  w->s0_1 = w->s0_0 + 128;
-  w->mask0 = tile_mask(w->s0_0, p);
-  w->mask1 = tile_mask(w->s0_1, p);
   int b = 0;
   while (b + 1 < p.n_bands && t >= p.band_start[b + 1]) ++b;
   w->band = b;
   return w->n_rows > 0;
 }
 
+// idx = (chunk * n_dytiles + rank) * per_rank + lp; false when the item has
+// no left rows.
 __host__ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
-  const int half = (int)(idx % p.n_halves);
-  const long long bid = idx / p.n_halves;
   const int per_rank = p.pm.n_left * p.n_pgroups;
-  const int lp = (int)(bid % per_rank);
-  const int rank = (int)((bid / per_rank) % p.n_dytiles);
-  const int chunk = (int)(bid / ((long long)per_rank * p.n_dytiles));
-  return tc_piece(p, half, lp, rank, chunk * p.chunk_rows, p.chunk_rows, w);
+  const int lp = (int)(idx % per_rank);
+  const int rank = (int)((idx / per_rank) % p.n_dytiles);
+  const int chunk = (int)(idx / ((long long)per_rank * p.n_dytiles));
+  return tc_piece(p, lp, rank, chunk * p.chunk_rows, p.chunk_rows, w);
 }
 
 // An entry of the host-built schedule.
 __host__ __device__ __forceinline__ bool tc_entry(const TcParams& p, int4 e, TcItem* w) {
   if (e.x < 0) return false;
   const int per_rank = p.pm.n_left * p.n_pgroups;
-  const int half = e.x % p.n_halves, bid = e.x / p.n_halves;
-  return tc_piece(p, half, bid % per_rank, bid / per_rank, e.y, e.z, w);
+  return tc_piece(p, e.x % per_rank, e.x / per_rank, e.y, e.z, w);
 }
 
 // Lists the non-empty work items by output row band (in the order
@@ -445,19 +445,18 @@ __device__ __forceinline__ bool round_item(const TcParams& p, long long n_live, 
 
 __device__ __forceinline__ long long n_rounds(long long n_live) { return (n_live + gridDim.x - 1) / gridDim.x; }
 
-// Accumulator windows of an item: tile 0 drains after every `flush` left
-// rows, tile 1 first after (flush + 1) / 2 rows and then every `flush`; both
+// Accumulator windows of an item: half 0 drains after every `flush` left
+// rows, half 1 first after (flush + 1) / 2 rows and then every `flush`; both
 // drain after the item's last row.  True when row ai (0-based) ends a window.
-__device__ __forceinline__ bool window_end(int tt, int ai, int n_rows, int flush) {
+__device__ __forceinline__ bool window_end(int h, int ai, int n_rows, int flush) {
   if (ai == n_rows - 1) return true;
-  // one issuer drains both tiles together
-  const int off = (tt == 0 || kIssuers == 1) ? 0 : flush - (flush + 1) / 2;
+  const int off = h == 0 ? 0 : flush - (flush + 1) / 2;
   return (ai + 1 + off) % flush == 0;
 }
 
-__device__ __forceinline__ int window_count(int tt, int n_rows, int flush) {
+__device__ __forceinline__ int window_count(int h, int n_rows, int flush) {
   int n = 0;
-  for (int ai = 0; ai < n_rows; ++ai) n += window_end(tt, ai, n_rows, flush) ? 1 : 0;
+  for (int ai = 0; ai < n_rows; ++ai) n += window_end(h, ai, n_rows, flush) ? 1 : 0;
   return n;
 }
 
@@ -466,21 +465,23 @@ __device__ __forceinline__ int window_count(int tt, int n_rows, int flush) {
 template <bool TF>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_kernel(const __grid_constant__ CUtensorMap map_hi, const __grid_constant__ CUtensorMap map_lo,
-              const TcParams p) {
+              const __grid_constant__ TcParams p) {
   using C = TcCfg<TF>;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  unsigned char* b_tiles = smem;                                       // kStages x (256 rows x 128 B)
-  unsigned char* t_buf = b_tiles + C::kStages * kStageBytes;           // [row buffer][hi, lo] Toeplitz core matrices
+  unsigned char* a_tiles = smem;                                       // kStages x (128 rows x 128 B)
+  unsigned char* t_buf = a_tiles + C::kStages * kStageBytes;           // [row buffer][hi, lo] Toeplitz core matrices
   float* xs = reinterpret_cast<float*>(t_buf + 4 * C::kTBytes);        // [row buffer][hi, lo] x kXLen staged row
-  uint64_t* bars = reinterpret_cast<uint64_t*>(xs + 4 * kXLen);
+  float* trans = xs + 4 * kXLen;                                       // [epilogue warp] 32 x kTrans transpose tile
+  long long* offs = reinterpret_cast<long long*>(trans + kEpiWarps * 32 * kTrans);  // [epilogue warp][lane row]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(offs + kEpiWarps * 32);
   uint64_t* a_full = bars;                   // [kStages] right-row tile landed
   uint64_t* a_empty = bars + C::kStages;     // [kStages] tile consumed
   uint64_t* r_full = bars + 2 * C::kStages;  // [2] Toeplitz row buffer written
   uint64_t* r_empty = r_full + 2;            // [2] row buffer consumed
-  uint64_t* t_full = r_empty + 2;            // [2] a tile's accumulator ready to drain
-  uint64_t* t_empty = t_full + 2;            // [2] a tile's accumulator drained
+  uint64_t* t_full = r_empty + 2;            // [2] a half's accumulator ready to drain
+  uint64_t* t_empty = t_full + 2;            // [2] a half's accumulator drained
   uint64_t* mma_done = t_empty + 2;          // [2] one per issuer
   volatile int* abort_flag = reinterpret_cast<volatile int*>(mma_done + 2);
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mma_done + 3);
@@ -497,11 +498,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     // consumed barriers take one commit from each issuer
     for (int s = 0; s < C::kStages; ++s) {
       mbar_init(&a_full[s], 1);
-      mbar_init(&a_empty[s], kIssuers);
+      mbar_init(&a_empty[s], 2);
     }
     for (int s = 0; s < 2; ++s) {
       mbar_init(&r_full[s], kBuilderWarps);
-      mbar_init(&r_empty[s], kIssuers);
+      mbar_init(&r_empty[s], 2);
       mbar_init(&t_full[s], 1);
       mbar_init(&t_empty[s], kEpiWarps / 2);
       mbar_init(&mma_done[s], 1);
@@ -541,7 +542,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 break;
               }
               mbar_arrive_expect_tx(&a_full[s], kStageBytes);
-              unsigned char* dst = b_tiles + s * kStageBytes;
+              unsigned char* dst = a_tiles + s * kStageBytes;
               const CUtensorMap* map = pl == 0 ? &map_hi : &map_lo;
               const int x = kc * 4 * p.kstep;  // first column of the chunk
               if (p.mats_mode) {
@@ -561,23 +562,23 @@ __global__ void __launch_bounds__(kThreads, 1)
           mbar_wait_bounded(&a_full[q % C::kStages], (q / C::kStages) & 1, 1u << 16);
       }
     }
-  } else if (warp == 1 || (kIssuers == 2 && warp == 2 + kBuilderWarps + kEpiWarps)) {
+  } else if (warp == 1 || warp == kIssuer1Warp) {
     // ------------------------------------------------------------ MMA issuers
-    // With two issuers, both walk the same items, rows and stages; each
-    // issues its own tile's MMAs and commits to the shared consumed barriers.
-    // With one, it issues both tiles' MMAs.
-    constexpr int kT = 3 - kIssuers;          // tiles per issuer
-    const int t_first = warp == 1 ? 0 : 1;    // first tile of this issuer
+    // Both walk the same items, rows and stages; issuer h issues the MMAs of
+    // shift half h (its own accumulator, tensor-memory columns
+    // [256 h, 256 h + 256)) and commits to the shared consumed barriers.
+    const int h = warp == 1 ? 0 : 1;
     if (lane == 0) {
-      // B: SBO 1024 B (8 rows x 128 B), 128-byte swizzle.  A (Toeplitz
-      // buffer): no swizzle, LBO 128 B along K, SBO 128 B (BF16) or 256 B
-      // (TF32) along M.
-      constexpr uint32_t kBHi = (1024u >> 4) | (1u << 14) | (2u << 29);
-      constexpr uint32_t kAHi = ((TF ? 256u : 128u) >> 4) | (1u << 14);
-      const uint32_t idesc = TF ? idesc_tf32_f32(128, kN) : idesc_bf16_f32(128, kN);
-      const uint32_t b_word = ((smem_u32(b_tiles) >> 4) & 0x3FFFu) | (1u << 16);
+      // A (right-row tile): SBO 1024 B (8 rows x 128 B), 128-byte swizzle.  B
+      // (Toeplitz buffer): no swizzle, LBO 128 B along K, SBO 128 B (BF16) or
+      // 256 B (TF32) along N.
+      constexpr uint32_t kAHi = (1024u >> 4) | (1u << 14) | (2u << 29);
+      constexpr uint32_t kBHi = ((TF ? 256u : 128u) >> 4) | (1u << 14);
+      const uint32_t idesc0 = TF ? idesc_tf32_f32(128, 0) : idesc_bf16_f32(128, 0);
+      const uint32_t a_word = ((smem_u32(a_tiles) >> 4) & 0x3FFFu) | (1u << 16);
       const uint32_t t_word = ((smem_u32(t_buf) >> 4) & 0x3FFFu) | ((128u >> 4) << 16);
-      constexpr uint32_t kTileQ = 128 / C::kCm;   // core matrices between the two shift tiles
+      const uint32_t* ktab = p.ktab[h];
+      const uint32_t kres = p.kreset[h];
       int s = 0, rb = 0;                      // stage, Toeplitz row buffer
       uint32_t s_phase = 0, r_phase = 0, t_phase = 1;
       bool s_ready = false;                   // stage s seen landed ahead of time
@@ -585,23 +586,16 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long round = 0; round < n_round && ok; ++round) {
         TcItem w;
         if (!round_item(p, n_items, round, &w)) continue;
-        uint32_t mm[kT];
-        int first[kT];
-#pragma unroll
-        for (int t = 0; t < kT; ++t) {
-          mm[t] = t_first + t == 0 ? w.mask0 : w.mask1;
-          first[t] = mm[t] ? __ffs(mm[t]) - 1 : -1;
-        }
         const int n_rows = w.n_rows;
         const int flush = p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P];
         int rows_in = 0;
         for (int ai = 0; ai < n_rows && ok; ++ai) {
           if (rows_in == 0) {
             // the epilogue must have drained the previous window
-#pragma unroll
-            for (int t = 0; t < kT; ++t)
-              if (!wait_or_abort(&t_empty[t_first + t], t_phase, abort_flag, p.flags, 14)) ok = false;
-            if (!ok) break;
+            if (!wait_or_abort(&t_empty[h], t_phase, abort_flag, p.flags, 14)) {
+              ok = false;
+              break;
+            }
             t_phase ^= 1u;
           }
           if (!wait_or_abort(&r_full[rb], r_phase, abort_flag, p.flags, 12)) {
@@ -612,13 +606,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t th = t_word + (uint32_t)rb * (2 * C::kTBytes >> 4);
           const uint32_t tl = th + (C::kTBytes >> 4);
           for (int kc = 0; kc < p.nkc && ok; ++kc) {
-            uint32_t pat[kT];
-            int rk[kT];
-#pragma unroll
-            for (int t = 0; t < kT; ++t) {
-              pat[t] = (mm[t] >> (4 * kc)) & 0xFu;
-              rk[t] = (rows_in == 0 && (first[t] >> 2) == kc) ? (first[t] & 3) : -1;  // K-step that resets
-            }
+            // the window's first MMA covers the whole half and starts the
+            // accumulator afresh
+            const uint32_t reset = (rows_in == 0 && kc == 0) ? 1u : 0u;
 #pragma unroll
             for (int pl = 0; pl < 2; ++pl) {
               if (!s_ready && !wait_or_abort(&a_full[s], s_phase, abort_flag, p.flags, 13)) {
@@ -631,25 +621,25 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int s2 = s + 1 == C::kStages ? 0 : s + 1;
                 s_ready = mbar_test_wait(&a_full[s2], s2 == 0 ? s_phase ^ 1u : s_phase);
               }
-              const uint32_t bw = b_word + (uint32_t)s * (kStageBytes >> 4);
+              const uint32_t aw = a_word + (uint32_t)s * (kStageBytes >> 4);
 #pragma unroll
               for (int ks = 0; ks < 4; ++ks) {
-                const uint64_t bd = make_desc(bw + ks * 2, kBHi);
-#pragma unroll
-                for (int t = 0; t < kT; ++t) {
-                  const int tt = t_first + t;
-                  // K-steps whose shifts meet only zeros are skipped (guard predicate)
-                  const uint32_t on = (pat[t] >> ks) & 1u;
-                  const uint32_t d = tmem_base + (uint32_t)tt * kN;
-                  // A for (tile, K-step j) starts 2 j + 128/kCm tt core matrices in
-                  const uint32_t qa = (uint32_t)(2 * (4 * kc + ks)) + (uint32_t)tt * kTileQ;
-                  const uint64_t ahi = make_desc(th + qa * (128u >> 4), kAHi);
-                  if (pl == 0) {
-                    mma_ss_if<TF>(d, ahi, bd, idesc, ks == rk[t] ? 0u : 1u, on);
-                    mma_ss_if<TF>(d, make_desc(tl + qa * (128u >> 4), kAHi), bd, idesc, 1u, on);
-                  } else {
-                    mma_ss_if<TF>(d, ahi, bd, idesc, 1u, on);
-                  }
+                const uint64_t ad = make_desc(aw + ks * 2, kAHi);
+                const uint32_t e = ktab[4 * kc + ks];
+                const uint32_t on = (e >> 14) & 1u;
+                const uint32_t d = tmem_base + (e & 511u);
+                const uint32_t id = idesc0 | ((((e >> 9) & 31u) * 2u) << 17);
+                const uint32_t bq = (e >> 16) * (128u >> 4);  // core matrices -> 16-byte units
+                if (pl == 0) {
+                  // R_hi L_hi (the window's first one over the whole half), R_hi L_lo
+                  const uint32_t r0 = (ks == 0) ? reset : 0u;
+                  const uint32_t e0 = r0 ? kres : e;
+                  mma_ss_if<TF>(tmem_base + (e0 & 511u), ad, make_desc(th + (e0 >> 16) * (128u >> 4), kBHi),
+                                idesc0 | ((((e0 >> 9) & 31u) * 2u) << 17), r0 ? 0u : 1u, r0 | on);
+                  mma_ss_if<TF>(d, ad, make_desc(tl + bq, kBHi), id, 1u, on);
+                } else {
+                  // R_lo L_hi
+                  mma_ss_if<TF>(d, ad, make_desc(th + bq, kBHi), id, 1u, on);
                 }
               }
               mma_commit(&a_empty[s]);
@@ -663,22 +653,22 @@ __global__ void __launch_bounds__(kThreads, 1)
           rb ^= 1;
           if (rb == 0) r_phase ^= 1u;
           ++rows_in;
-          if (window_end(t_first, ai, n_rows, flush)) {
-#pragma unroll
-            for (int t = 0; t < kT; ++t) mma_commit(&t_full[t_first + t]);
+          if (window_end(h, ai, n_rows, flush)) {
+            mma_commit(&t_full[h]);
             rows_in = 0;
           }
         }
       }
       // All MMAs issued by this thread must finish before TMEM is released.
-      mma_commit(&mma_done[t_first]);
-      mbar_wait_bounded(&mma_done[t_first], 0, 1u << 22);
+      mma_commit(&mma_done[h]);
+      mbar_wait_bounded(&mma_done[h], 0, 1u << 22);
     }
   } else if (warp < 2 + kBuilderWarps) {
     // ------------------------------------------------------------ Toeplitz builders
-    // Per left row: stage the centred, split row X[i] = Lp[s0 + i] (hi and lo
-    // parts), then write the core-matrix buffer T[q][r][t] = X[kCm q + r + t]
-    // of both parts into the free row buffer.
+    // Per left row: stage the centred, split row X[i] = Lp[i] (hi and lo
+    // parts; Lp[i] = L[a][i - (Wr-1)], zero outside the row), then write the
+    // core-matrix buffer T[q][r][t] = X[kCm q + r + t] of both parts into the
+    // free row buffer.
     const int bt = threadIdx.x - 64;  // 0..127
     constexpr int kChunks = 2 * C::kQ * 8;  // 16-byte rows of T, both parts
     int rows_done = 0;
@@ -688,7 +678,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!round_item(p, n_items, round, &w)) continue;
       const float* lrow_base = p.left + (long long)w.l * p.Hl * p.Wl;
       const float mu = __ldg(p.mu_left + w.l);
-      const int x_off = w.s0_0 - (p.Wr - 1);  // left column of X[0]
+      const int x_off = -(p.Wr - 1);  // left column of X[0]
       int ai = 0;
       for (; ai < w.n_rows; ++ai, ++rows_done) {
         const int rbuf = rows_done & 1;
@@ -698,16 +688,16 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int i = bt; i < kXLen; i += 32 * kBuilderWarps) {
           const int x = x_off + i;
           const float v = (x >= 0 && x < p.Wl) ? __ldg(src + x) - mu : 0.0f;
-          float h, l;
+          float hv, lv;
           if constexpr (TF) {
-            h = tf32_round(v);
-            l = tf32_round(v - h);
+            hv = tf32_round(v);
+            lv = tf32_round(v - hv);
           } else {
-            h = __bfloat162float(__float2bfloat16_rn(v));
-            l = v - h;
+            hv = __bfloat162float(__float2bfloat16_rn(v));
+            lv = v - hv;
           }
-          xh[i] = h;
-          xl[i] = l;
+          xh[i] = hv;
+          xl[i] = lv;
         }
         // the staged row is complete; the builder threads also leave together here
         if (bar_red_or(!ok, 1, 32 * kBuilderWarps)) {
@@ -749,89 +739,85 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp < 2 + kBuilderWarps + kEpiWarps) {
     // ------------------------------------------------------------ epilogue
-    // Warp w (index ew = w - 6): lane quadrant q = w % 4, accumulator
-    // columns [128 * (ew / 4), +128): tile tt = ew / 8, B rows nb.. of it.
-    constexpr int kCols = 128;
+    // Warp w (index ew = w - 6): half h = ew / 8, TMEM lane quadrant
+    // q = w % 4 (lane rows 32 q ..: A rows, i.e. (partner, row shift)),
+    // columns [128 cb, 128 cb + 128) of the half, cb = (ew / 4) % 2.  A
+    // 32-column load gives each thread one lane row's 32 shifts; a 32 x 16
+    // piece goes through shared memory so that each reduction instruction
+    // covers 16 consecutive shifts of two output rows.
     const int ew = warp - (2 + kBuilderWarps);
     const int q = warp & 3;
-    const int tt = ew >> 3;
-    const int nb = ((ew >> 2) & 1) * kCols;
+    const int h = ew >> 3;
+    const int cb = (ew >> 2) & 1;
+    float* tb = trans + ew * (32 * kTrans);
+    long long* my_off = offs + ew * 32;
+    const int lgP = __ffs(p.P) - 1, lgDY = __ffs(p.DY) - 1;
     int d_all = 0;
     bool ok = true;
     for (long long round = 0; round < n_round && ok; ++round) {
       TcItem w;
       if (!round_item(p, n_items, round, &w)) continue;
-      // Output offset of B row n: ((l*o_l + k*o_k)*Sy + sy)*Sx with k = p0 + pp,
-      // sy = dy + Hr - 1.  Rows are partner-major inside a row shift (P >= 8:
-      // n = d*P + pp, dy = dy0 + d) or row-shift-major inside a partner
-      // (P < 8: n = pp*DY + d, dy = dy0 + DY-1 - d).  Computed per 32-row
-      // batch (no table lookups: shared memory is busy serving the MMAs).
-      const long long row_l = (long long)w.l * p.pm.o_l;
-      const long long kstride = (long long)p.pm.o_k * p.Sy * p.Sx;
-      const int lgP = __ffs(p.P) - 1, lgDY = __ffs(p.DY) - 1;
-      const bool live = (tt == 0 ? w.mask0 : w.mask1) != 0u;
-      const int sx = (tt == 0 ? w.s0_0 : w.s0_1) + 32 * q + lane;
-      const int n_drains = window_count(tt, w.n_rows, p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P]);
+      {
+        // output offset of this thread's lane row m (or -1): partner-major
+        // inside a row shift (P >= 8: m = d*P + pp, dy = dy0 + d) or
+        // row-shift-major inside a partner (P < 8: m = pp*DY + d,
+        // dy = dy0 + DY-1 - d)
+        const int m = 32 * q + lane;
+        int k, dy;
+        if (p.mats_mode) {
+          k = w.p0 + (m & (p.P - 1));
+          dy = w.dy0 + (m >> lgP);
+        } else {
+          k = w.p0 + (m >> lgDY);
+          dy = w.dy0 + (p.DY - 1) - (m & (p.DY - 1));
+        }
+        const int sy = dy + p.Hr - 1;
+        long long o = -1;
+        if (k < p.pm.K && sy >= 0 && sy < p.Sy)
+          o = (((long long)w.l * p.pm.o_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx;
+        __syncwarp();  // the previous item's readers are done with the table
+        my_off[lane] = o;
+        __syncwarp();
+      }
+      const int sx_base = h * p.half_w + 128 * cb;
+      const int n_drains = window_count(h, w.n_rows, p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P]);
       for (int d = 0; d < n_drains; ++d, ++d_all) {
-        bool wt = wait_or_abort_sleep(&t_full[tt], d_all & 1, abort_flag, p.flags, 16);
+        bool wt = wait_or_abort_sleep(&t_full[h], d_all & 1, abort_flag, p.flags, 16);
         wt = __all_sync(0xffffffffu, wt);  // tcgen05.ld below must stay warp-uniform
         if (!wt) {
           ok = false;
           break;
         }
         tc_fence_after();
-        if (live) {
-          const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(tt * kN + nb);
-          for (int j = 0; j < kCols; j += 32) {
+        if (sx_base < min(p.Sx, (h + 1) * p.half_w)) {
+          const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kHalfCols + 128 * cb);
+          for (int j = 0; j < 128; j += 32) {
             float v[32];
             tmem_ld32(col0 + (uint32_t)j, v);
             tmem_wait_ld();
-            if (sx >= p.Sx) continue;
-            const int n0 = nb + j;
-            if (p.P >= 32 || !p.mats_mode) {
-              // the batch lies inside one row shift (P >= 32) or one partner
-              // (DY >= 64): offsets o0 + i * stride for i in [i_lo, i_hi)
-              long long o0, stride;
-              int i_lo = 0, i_hi = 32;
-              if (p.mats_mode) {
-                const int k0 = w.p0 + (n0 & (p.P - 1));
-                const int sy = w.dy0 + (n0 >> lgP) + p.Hr - 1;
-                if (sy < 0 || sy >= p.Sy) continue;
-                i_hi = min(32, p.pm.K - k0);
-                o0 = ((row_l + (long long)k0 * p.pm.o_k) * p.Sy + sy) * p.Sx;
-                stride = kstride;
-              } else {
-                const int k = w.p0 + (n0 >> lgDY);
-                if (k >= p.pm.K) continue;
-                const int sy0 = w.dy0 + (p.DY - 1) - (n0 & (p.DY - 1)) + p.Hr - 1;
-                i_lo = max(0, sy0 - (p.Sy - 1));
-                i_hi = min(32, sy0 + 1);
-                o0 = ((row_l + (long long)k * p.pm.o_k) * p.Sy + sy0) * p.Sx;
-                stride = -(long long)p.Sx;
-              }
-              float* o = p.out + o0 + sx;
-              // rows i_lo <= i < i_hi of the batch are inside the output
-              const uint32_t below_hi = i_hi >= 32 ? 0xffffffffu : (i_hi <= 0 ? 0u : (1u << i_hi) - 1u);
-              const uint32_t from_lo = i_lo <= 0 ? 0xffffffffu : (i_lo >= 32 ? 0u : ~((1u << i_lo) - 1u));
-              const uint32_t valid = below_hi & from_lo;
 #pragma unroll
-              for (int i = 0; i < 32; ++i) red_add_if(o + i * stride, v[i], (valid >> i) & 1u);
-            } else {
-              // P = 8 or 16: several row shifts per batch
+            for (int u = 0; u < 2; ++u) {
+              // lane row `lane`, shifts 16 u ..: into the tile's row `lane`
 #pragma unroll
-              for (int i = 0; i < 32; ++i) {
-                const int n = n0 + i;
-                const int k = w.p0 + (n & (p.P - 1));
-                const int sy = w.dy0 + (n >> lgP) + p.Hr - 1;
-                if (k < p.pm.K && sy >= 0 && sy < p.Sy)
-                  red_add(p.out + ((row_l + (long long)k * p.pm.o_k) * p.Sy + sy) * p.Sx + sx, v[i]);
+              for (int c = 0; c < 16; ++c) tb[lane * kTrans + c] = v[16 * u + c];
+              __syncwarp();
+              // shift column cc, lane rows (lane / 16) + 2 i
+              const int cc = lane & 15;
+              const int sx = sx_base + j + 16 * u + cc;
+              const uint32_t in_x = (sx < p.Sx && sx < (h + 1) * p.half_w) ? 1u : 0u;
+#pragma unroll
+              for (int i = 0; i < 16; ++i) {
+                const int r = (lane >> 4) + 2 * i;
+                const long long o = my_off[r];
+                red_add_if(p.out + (o < 0 ? 0 : o) + sx, tb[r * kTrans + cc], in_x & (o >= 0 ? 1u : 0u));
               }
+              __syncwarp();
             }
           }
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&t_empty[tt]);  // one arrival per warp
+        if (lane == 0) mbar_arrive(&t_empty[h]);  // one arrival per warp
       }
       if (p.band_done != nullptr) {
         // this thread's reductions become visible before the band count moves
@@ -1255,7 +1241,7 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, n_tiles, n_halves, nkc, kstep, es, pitch, n_chunks, chunk_rows;
+  int P, DY, mats_mode, half_w, nkc, kstep, es, pitch, n_chunks, chunk_rows;
   long long n_items;
   int smem_bytes;
 };
@@ -1264,14 +1250,13 @@ int chunk_rows_fixed();
 int sm_count();
 
 bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
-  if (g.Sx > 512 || g.Wr > 256) return false;  // four 128-shift tiles, 16 K-steps
+  if (g.Sx > 512 || g.Wr > 256) return false;  // two 256-shift halves, 256 right columns
   int P = 1;
-  while (P < kN && P < pm.K) P *= 2;
+  while (P < kLanes && P < pm.K) P *= 2;
   t->P = P;
-  t->DY = kN / P;
+  t->DY = kLanes / P;
   t->mats_mode = P >= 8 ? 1 : 0;
-  t->n_tiles = (g.Sx + 127) / 128;
-  t->n_halves = (t->n_tiles + 1) / 2;
+  t->half_w = ((g.Sx + 1) / 2 + 15) / 16 * 16;
   t->es = tf32 ? 4 : 2;                 // bytes per operand element
   t->kstep = tf32 ? 8 : 16;             // columns per MMA K-step (32 bytes)
   const int chunk = 128 / t->es;        // columns per 128-byte TMA box row
@@ -1280,12 +1265,12 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   // left rows per item: at most 32, fewer when that leaves fewer than two
   // items per SM (small problems), at least 4
   const long long span = t->DY - 1 + std::min(g.Hl, g.Hr);
-  const long long rows_all = span * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, P) * t->n_halves;
+  const long long rows_all = span * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, P);
   t->chunk_rows = chunk_rows_fixed() > 0
                       ? chunk_rows_fixed()
                       : (int)std::max(4LL, std::min(32LL, rows_all / (2LL * sm_count())));
   t->n_chunks = (int)div_up(span, (long long)t->chunk_rows);
-  t->n_items = (long long)t->n_halves * t->n_chunks * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
+  t->n_items = (long long)t->n_chunks * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
   t->smem_bytes = tf32 ? TcCfg<true>::kSmem : TcCfg<false>::kSmem;
   return t->smem_bytes <= 227 * 1024;
 }
@@ -1401,13 +1386,17 @@ xc_status upload_band_schedule(const TcParams& prm, int G, int* region, long lon
   in.DY = prm.DY;
   in.n_dytiles = prm.n_dytiles;
   in.per_rank = prm.pm.n_left * prm.n_pgroups;
-  in.n_halves = prm.n_halves;
+  in.n_halves = 1;
   in.chunk_rows = prm.chunk_rows;
   in.n_bands = prm.n_bands;
   for (int b = 0; b <= prm.n_bands; ++b) in.band_start[b] = prm.band_start[b];
   for (int b = 0; b < prm.n_bands; ++b) in.band_rank[b] = prm.band_rank[b];
-  in.ks[0] = __builtin_popcount(tile_mask(0, prm)) + __builtin_popcount(tile_mask(128, prm));
-  in.ks[1] = __builtin_popcount(tile_mask(256, prm)) + __builtin_popcount(tile_mask(384, prm));
+  // cost of a left row: the MMA windows of both halves, in 16-shift units
+  int units = 0;
+  for (int h = 0; h < 2; ++h)
+    for (int j = 0; j < kMaxKSteps; ++j)
+      if ((prm.ktab[h][j] >> 14) & 1u) units += (int)((prm.ktab[h][j] >> 9) & 31u);
+  in.ks[0] = in.ks[1] = std::max(1, units);
   std::vector<BandPiece> sched;
   plan_band_schedule(in, G, &sched, band_items);
   static_assert(sizeof(BandPiece) == sizeof(int4), "a schedule entry is an int4");
@@ -1535,9 +1524,11 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   prm.mats_mode = t.mats_mode;
   prm.n_pgroups = div_up(pm.K, t.P);
   prm.n_dytiles = div_up(g.Sy, t.DY);
-  prm.n_halves = t.n_halves;
+  prm.n_halves = 1;
+  prm.half_w = t.half_w;
   prm.nkc = t.nkc;
   prm.kstep = t.kstep;
+  kstep_windows(g.Wl, g.Wr, g.Sx, t.half_w, t.kstep, tf32 ? 4 : 8, 4 * t.nkc, prm.ktab, prm.kreset);
   prm.flush_tab = w.flush;
   prm.chunk_rows = t.chunk_rows;
   prm.n_chunks = t.n_chunks;

@@ -37,11 +37,11 @@ def run(exe, cases):
 
 
 def dy_of(k):
-    """Row shifts per tile for k partners (partners per group: the next power of two, at most 256)."""
+    """Row shifts per tile for k partners (partners per group: the next power of two, at most 128)."""
     p = 1
-    while p < 256 and p < k:
+    while p < 128 and p < k:
         p *= 2
-    return 256 // p
+    return 128 // p
 
 
 def cases():
@@ -63,8 +63,10 @@ def cases():
     ]
     for hl, hr, k, nl, nh, cr, want, g in shapes:
         dy = dy_of(k)
-        per_rank = nl * ((k + (256 // dy) - 1) // (256 // dy))
+        per_rank = nl * ((k + (128 // dy) - 1) // (128 // dy))
         out.append((hl, hr, dy, hl + hr - 1, per_rank, nh, cr, want, g, 16, 16 if nh == 2 else 0))
+        # the kernel's own form: one item per tile key covers every shift
+        out.append((hl, hr, dy, hl + hr - 1, per_rank, 1, cr, want, g, 34, 34))
     return out
 
 
@@ -77,10 +79,12 @@ def test_band_schedule_invariants(checker):
 
 
 def test_band_schedule_balance_at_the_bench_shape(checker):
-    """1 x 64 right 256x256 in eight bands on 152 CTAs: the busiest CTA's
-    modelled work within 1% of the mean (least-work assignment of the fixed
-    32-row chunks left 6%, the snake order 16%)."""
-    (r,) = run(checker, [(256, 256, 4, 511, 1, 2, 32, 8, 152, 16, 16)])
+    """1 x 64 right 256x256 in eight bands on 152 CTAs (64 partners x 2 row
+    shifts per item, one item per tile key): the busiest CTA's modelled work
+    within 3% of the mean.  (Cutting the bands into pieces of a quarter chunk
+    would bring the ratio under 1% but raise the busiest CTA's work by 7%,
+    every piece adding a drain.)"""
+    (r,) = run(checker, [(256, 256, 2, 511, 1, 1, 32, 8, 152, 34, 34)])
     assert r[0] == "ok"
     max_load, mean = float(r[3]), float(r[4])
-    assert max_load / mean <= 1.01, (max_load, mean)
+    assert max_load / mean <= 1.03, (max_load, mean)
