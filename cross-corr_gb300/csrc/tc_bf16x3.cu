@@ -73,7 +73,7 @@
 //   warp 1      TMEM allocation; one thread issues the MMAs of shift half 0
 //   warp 22     one thread issues the MMAs of shift half 1
 //   warps 2-5   builders of the Toeplitz core-matrix buffer (two row buffers)
-//   warps 6-21  epilogue: eight per half, two per TMEM lane quadrant
+//   warps 6-21  epilogue: four per TMEM lane quadrant, all draining each half
 // Each half's accumulator is drained on its own schedule, the two offset by
 // half a window: while the epilogue drains one half, the other half's issuer
 // keeps the tensor pipe busy (as far as the shared right-tile stages allow).
@@ -104,7 +104,7 @@ constexpr int kLanes = 128;                // A rows per MMA: P partners x DY ro
 constexpr int kStageBytes = kLanes * 128;  // one plane of one 128-byte column chunk
 constexpr int kHalfCols = 256;             // tensor-memory columns per shift half
 constexpr int kBuilderWarps = 4;
-constexpr int kEpiWarps = 16;              // eight per shift half, two per TMEM lane quadrant
+constexpr int kEpiWarps = 16;              // four per TMEM lane quadrant, all draining each half
 // warp 0 producer, warps 1 and 22 MMA issuers (one per shift half), 2-5
 // builders, 6-21 epilogue
 constexpr int kThreads = 32 * (3 + kBuilderWarps + kEpiWarps);
@@ -113,18 +113,22 @@ constexpr int kXLen = 792;                 // staged row elements: every shift p
 constexpr int kBarBytes = 256;             // 20 mbarriers at most, the abort flag, the TMEM address slot
 constexpr int kMaxChunkRows = 1024;        // left rows per work item at most
 constexpr int kMaxKSteps = 32;             // K-steps of a 256-column right row (16 BF16 or 32 TF32)
-constexpr int kTrans = 17;                 // padded row of an epilogue warp's 32 x 16 transpose tile
 
 // Per operand type: right-tile stages and the Toeplitz buffer (hi or lo part
 // of one left row): core matrices of 8 BF16 or 4 FP32 per 16-byte row,
 // covering X[0, 776) (every shift of both halves plus a right row).
+// An epilogue warp transposes 32 lane rows x kTransW shifts at a time
+// through shared memory (rows padded by one float): 32 for BF16, so that one
+// reduction instruction covers one output row's 32 shifts (a 128-byte line);
+// 16 for TF32, whose larger Toeplitz buffer leaves less room.
 template <bool TF>
 struct TcCfg {
-  static constexpr int kStages = TF ? 4 : 7;
+  static constexpr int kStages = TF ? 4 : 5;
   static constexpr int kCm = TF ? 4 : 8;            // elements per 16-byte core-matrix row
   static constexpr int kQ = TF ? 194 : 98;          // core matrices in T
   static constexpr int kTBytes = kQ * 128;          // one plane of T
-  static constexpr int kTransBytes = kEpiWarps * 32 * kTrans * 4;
+  static constexpr int kTransW = TF ? 16 : 32;
+  static constexpr int kTransBytes = kEpiWarps * 32 * (kTransW + 1) * 4;
   static constexpr int kOffBytes = kEpiWarps * 32 * 8;
   static constexpr int kSmem = 1024 + kStages * kStageBytes + 4 * kTBytes + 4 * kXLen * 4 + kTransBytes +
                                kOffBytes + kBarBytes;
@@ -454,11 +458,6 @@ __device__ __forceinline__ bool window_end(int h, int ai, int n_rows, int flush)
   return (ai + 1 + off) % flush == 0;
 }
 
-__device__ __forceinline__ int window_count(int h, int n_rows, int flush) {
-  int n = 0;
-  for (int ai = 0; ai < n_rows; ++ai) n += window_end(h, ai, n_rows, flush) ? 1 : 0;
-  return n;
-}
 
 // 23 warps: at most 6 on one SM sub-partition, whose 16K registers cap a
 // thread at 80.  TF: TF32 operands (K = 8 per MMA) instead of BF16 (K = 16).
@@ -473,8 +472,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char* a_tiles = smem;                                       // kStages x (128 rows x 128 B)
   unsigned char* t_buf = a_tiles + C::kStages * kStageBytes;           // [row buffer][hi, lo] Toeplitz core matrices
   float* xs = reinterpret_cast<float*>(t_buf + 4 * C::kTBytes);        // [row buffer][hi, lo] x kXLen staged row
-  float* trans = xs + 4 * kXLen;                                       // [epilogue warp] 32 x kTrans transpose tile
-  long long* offs = reinterpret_cast<long long*>(trans + kEpiWarps * 32 * kTrans);  // [epilogue warp][lane row]
+  float* trans = xs + 4 * kXLen;                                       // [epilogue warp] transpose tile
+  long long* offs = reinterpret_cast<long long*>(trans + kEpiWarps * 32 * (C::kTransW + 1));  // [warp][lane row]
   uint64_t* bars = reinterpret_cast<uint64_t*>(offs + kEpiWarps * 32);
   uint64_t* a_full = bars;                   // [kStages] right-row tile landed
   uint64_t* a_empty = bars + C::kStages;     // [kStages] tile consumed
@@ -504,7 +503,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&r_full[s], kBuilderWarps);
       mbar_init(&r_empty[s], 2);
       mbar_init(&t_full[s], 1);
-      mbar_init(&t_empty[s], kEpiWarps / 2);
+      mbar_init(&t_empty[s], kEpiWarps);
       mbar_init(&mma_done[s], 1);
     }
     *abort_flag = 0;
@@ -739,20 +738,21 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp < 2 + kBuilderWarps + kEpiWarps) {
     // ------------------------------------------------------------ epilogue
-    // Warp w (index ew = w - 6): half h = ew / 8, TMEM lane quadrant
-    // q = w % 4 (lane rows 32 q ..: A rows, i.e. (partner, row shift)),
-    // columns [128 cb, 128 cb + 128) of the half, cb = (ew / 4) % 2.  A
-    // 32-column load gives each thread one lane row's 32 shifts; a 32 x 16
-    // piece goes through shared memory so that each reduction instruction
-    // covers 16 consecutive shifts of two output rows.
+    // Every epilogue warp takes part in every drain, in the order the
+    // windows end (by left row; half 0 first at the item's last row): warp w
+    // (index ew = w - 6) reads TMEM lane quadrant q = w % 4 (lane rows 32 q ..:
+    // A rows, i.e. (partner, row shift)) and columns [64 cq, 64 cq + 64) of the
+    // half, cq = ew / 4.  A 32-column load gives each thread one lane row's
+    // 32 shifts; it goes through shared memory so that each reduction
+    // instruction covers consecutive shifts of one output row.
+    constexpr int TW = C::kTransW;
     const int ew = warp - (2 + kBuilderWarps);
     const int q = warp & 3;
-    const int h = ew >> 3;
-    const int cb = (ew >> 2) & 1;
-    float* tb = trans + ew * (32 * kTrans);
+    const int cq = ew >> 2;
+    float* tb = trans + ew * (32 * (TW + 1));
     long long* my_off = offs + ew * 32;
     const int lgP = __ffs(p.P) - 1, lgDY = __ffs(p.DY) - 1;
-    int d_all = 0;
+    int drained0 = 0, drained1 = 0;  // drains of each half so far
     bool ok = true;
     for (long long round = 0; round < n_round && ok; ++round) {
       TcItem w;
@@ -779,45 +779,50 @@ __global__ void __launch_bounds__(kThreads, 1)
         my_off[lane] = o;
         __syncwarp();
       }
-      const int sx_base = h * p.half_w + 128 * cb;
-      const int n_drains = window_count(h, w.n_rows, p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P]);
-      for (int d = 0; d < n_drains; ++d, ++d_all) {
-        bool wt = wait_or_abort_sleep(&t_full[h], d_all & 1, abort_flag, p.flags, 16);
-        wt = __all_sync(0xffffffffu, wt);  // tcgen05.ld below must stay warp-uniform
-        if (!wt) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        if (sx_base < min(p.Sx, (h + 1) * p.half_w)) {
-          const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kHalfCols + 128 * cb);
-          for (int j = 0; j < 128; j += 32) {
-            float v[32];
-            tmem_ld32(col0 + (uint32_t)j, v);
-            tmem_wait_ld();
+      const int flush = p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P];
+      for (int ai = 0; ai < w.n_rows && ok; ++ai) {
+        for (int h = 0; h < 2; ++h) {
+          if (!window_end(h, ai, w.n_rows, flush)) continue;
+          bool wt = wait_or_abort_sleep(&t_full[h], (h ? drained1 : drained0) & 1, abort_flag, p.flags, 16);
+          if (h) ++drained1;
+          else ++drained0;
+          wt = __all_sync(0xffffffffu, wt);  // tcgen05.ld below must stay warp-uniform
+          if (!wt) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const int sx_base = h * p.half_w + 64 * cq;
+          if (sx_base < min(p.Sx, (h + 1) * p.half_w)) {
+            const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kHalfCols + 64 * cq);
+            for (int j = 0; j < 64; j += 32) {
+              float v[32];
+              tmem_ld32(col0 + (uint32_t)j, v);
+              tmem_wait_ld();
 #pragma unroll
-            for (int u = 0; u < 2; ++u) {
-              // lane row `lane`, shifts 16 u ..: into the tile's row `lane`
+              for (int u = 0; u < 32 / TW; ++u) {
+                // lane row `lane`, shifts TW u ..: into the tile's row `lane`
 #pragma unroll
-              for (int c = 0; c < 16; ++c) tb[lane * kTrans + c] = v[16 * u + c];
-              __syncwarp();
-              // shift column cc, lane rows (lane / 16) + 2 i
-              const int cc = lane & 15;
-              const int sx = sx_base + j + 16 * u + cc;
-              const uint32_t in_x = (sx < p.Sx && sx < (h + 1) * p.half_w) ? 1u : 0u;
+                for (int c = 0; c < TW; ++c) tb[lane * (TW + 1) + c] = v[TW * u + c];
+                __syncwarp();
+                // shift column cc, lane rows (lane / TW) + (32 / TW) i
+                const int cc = lane & (TW - 1);
+                const int sx = sx_base + j + TW * u + cc;
+                const uint32_t in_x = (sx < p.Sx && sx < (h + 1) * p.half_w) ? 1u : 0u;
 #pragma unroll
-              for (int i = 0; i < 16; ++i) {
-                const int r = (lane >> 4) + 2 * i;
-                const long long o = my_off[r];
-                red_add_if(p.out + (o < 0 ? 0 : o) + sx, tb[r * kTrans + cc], in_x & (o >= 0 ? 1u : 0u));
+                for (int i = 0; i < TW; ++i) {
+                  const int r = (lane / TW) + (32 / TW) * i;
+                  const long long o = my_off[r];
+                  red_add_if(p.out + (o < 0 ? 0 : o) + sx, tb[r * (TW + 1) + cc], in_x & (o >= 0 ? 1u : 0u));
+                }
+                __syncwarp();
               }
-              __syncwarp();
             }
           }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&t_empty[h]);  // one arrival per warp
         }
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&t_empty[h]);  // one arrival per warp
       }
       if (p.band_done != nullptr) {
         // this thread's reductions become visible before the band count moves
