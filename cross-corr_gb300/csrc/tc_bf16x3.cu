@@ -258,14 +258,16 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 
 // red.global.add under a predicate (no branch: a drain's adds stay one
 // straight block the compiler can schedule; the address of a false one is
-// not used).
+// not used).  No memory clobber: nothing in this thread reads the output, so
+// the shared-memory loads that feed the adds may be scheduled ahead of
+// earlier adds; the drain's closing fence and barrier arrival order the adds
+// before the accumulator is released and before a band count moves.
 __device__ __forceinline__ void red_add_if(float* addr, float v, uint32_t pred) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %2, 0;\n\t"
       "@p red.global.add.f32 [%0], %1;\n\t}" ::"l"(addr),
-      "f"(v), "r"(pred)
-      : "memory");
+      "f"(v), "r"(pred));
 }
 
 // Non-blocking look at a phase: the MMA issuers ask for the next stage
