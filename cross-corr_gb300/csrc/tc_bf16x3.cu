@@ -741,7 +741,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else if (warp < 2 + kBuilderWarps + kEpiWarps) {
     // ------------------------------------------------------------ epilogue
     // Every epilogue warp takes part in every drain, in the order the
-    // windows end (by left row; half 0 first at the item's last row): warp w
+    // windows end (by left row; half 0 first at the item's last row), and
+    // releases the accumulator as soon as its columns are in registers: warp w
     // (index ew = w - 6) reads TMEM lane quadrant q = w % 4 (lane rows 32 q ..:
     // A rows, i.e. (partner, row shift)) and columns [64 cq, 64 cq + 64) of the
     // half, cq = ew / 4.  A 32-column load gives each thread one lane row's
@@ -795,35 +796,66 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           tc_fence_after();
           const int sx_base = h * p.half_w + 64 * cq;
-          if (sx_base < min(p.Sx, (h + 1) * p.half_w)) {
-            const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kHalfCols + 64 * cq);
-            for (int j = 0; j < 64; j += 32) {
-              float v[32];
-              tmem_ld32(col0 + (uint32_t)j, v);
+          const bool live = sx_base < min(p.Sx, (h + 1) * p.half_w);
+          const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kHalfCols + 64 * cq);
+          // reductions of lane rows x TW shifts from the transpose tile: shift
+          // column cc, lane rows (lane / TW) + (32 / TW) i
+          auto reduce_tile = [&](int sx0) {
+            const int cc = lane & (TW - 1);
+            const int sx = sx0 + cc;
+            const uint32_t in_x = (sx < p.Sx && sx < (h + 1) * p.half_w) ? 1u : 0u;
+#pragma unroll
+            for (int i = 0; i < TW; ++i) {
+              const int r = (lane / TW) + (32 / TW) * i;
+              const long long o = my_off[r];
+              red_add_if(p.out + (o < 0 ? 0 : o) + sx, tb[r * (TW + 1) + cc], in_x & (o >= 0 ? 1u : 0u));
+            }
+          };
+          float v[32];
+          if constexpr (TW == 32) {
+            // The first 32 columns go into the transpose tile and the next 32
+            // into registers; then the accumulator is released, and the
+            // issuer restarts the half while the adds below are issued.
+            if (live) {
+              tmem_ld32(col0, v);
               tmem_wait_ld();
 #pragma unroll
-              for (int u = 0; u < 32 / TW; ++u) {
-                // lane row `lane`, shifts TW u ..: into the tile's row `lane`
+              for (int c = 0; c < 32; ++c) tb[lane * (TW + 1) + c] = v[c];
+              tmem_ld32(col0 + 32u, v);
+              tmem_wait_ld();
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&t_empty[h]);  // one arrival per warp
+            if (live) {
+              reduce_tile(sx_base);
+              __syncwarp();
 #pragma unroll
-                for (int c = 0; c < TW; ++c) tb[lane * (TW + 1) + c] = v[TW * u + c];
-                __syncwarp();
-                // shift column cc, lane rows (lane / TW) + (32 / TW) i
-                const int cc = lane & (TW - 1);
-                const int sx = sx_base + j + TW * u + cc;
-                const uint32_t in_x = (sx < p.Sx && sx < (h + 1) * p.half_w) ? 1u : 0u;
+              for (int c = 0; c < 32; ++c) tb[lane * (TW + 1) + c] = v[c];
+              __syncwarp();
+              reduce_tile(sx_base + 32);
+              __syncwarp();
+            }
+          } else {
+            // 16-wide tiles: the adds come first, then the release
+            if (live) {
+              for (int j = 0; j < 64; j += 32) {
+                tmem_ld32(col0 + (uint32_t)j, v);
+                tmem_wait_ld();
 #pragma unroll
-                for (int i = 0; i < TW; ++i) {
-                  const int r = (lane / TW) + (32 / TW) * i;
-                  const long long o = my_off[r];
-                  red_add_if(p.out + (o < 0 ? 0 : o) + sx, tb[r * (TW + 1) + cc], in_x & (o >= 0 ? 1u : 0u));
+                for (int u = 0; u < 2; ++u) {
+#pragma unroll
+                  for (int c = 0; c < TW; ++c) tb[lane * (TW + 1) + c] = v[TW * u + c];
+                  __syncwarp();
+                  reduce_tile(sx_base + j + TW * u);
+                  __syncwarp();
                 }
-                __syncwarp();
               }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&t_empty[h]);  // one arrival per warp
           }
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&t_empty[h]);  // one arrival per warp
         }
       }
       if (p.band_done != nullptr) {
