@@ -1282,13 +1282,14 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 struct TcPlan {
   int P, DY, mats_mode, half_w, nkc, kstep, es, pitch, n_chunks, chunk_rows;
   long long n_items;
+  long long n_items_ws;  // items at 32-row chunks: the work list and schedule space of either form of launch
   int smem_bytes;
 };
 
 int chunk_rows_fixed();
 int sm_count();
 
-bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
+bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool banded = false) {
   if (g.Sx > 512 || g.Wr > 256) return false;  // two 256-shift halves, 256 right columns
   int P = 1;
   while (P < kLanes && P < pm.K) P *= 2;
@@ -1301,15 +1302,21 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t) {
   const int chunk = 128 / t->es;        // columns per 128-byte TMA box row
   t->nkc = (g.Wr + chunk - 1) / chunk;
   t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
-  // left rows per item: at most 32, fewer when that leaves fewer than two
-  // items per SM (small problems), at least 4
+  // left rows per item: at most 64, fewer when that leaves fewer than two
+  // items per SM (small problems), at least 4.  Longer items end fewer
+  // accumulator windows early (at one_to_many 256x256 x 64: 1.071 ms with
+  // 32-row items, 1.039 ms with 64).  A banded launch keeps at most 32: its
+  // host plan cuts each band into pieces of half to one item, and 152 CTAs
+  // need that many pieces per band.
   const long long span = t->DY - 1 + std::min(g.Hl, g.Hr);
   const long long rows_all = span * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, P);
-  t->chunk_rows = chunk_rows_fixed() > 0
-                      ? chunk_rows_fixed()
-                      : (int)std::max(4LL, std::min(32LL, rows_all / (2LL * sm_count())));
+  const long long per_tile_key = (long long)div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
+  const long long fair = rows_all / (2LL * sm_count());
+  const int chunk32 = chunk_rows_fixed() > 0 ? chunk_rows_fixed() : (int)std::max(4LL, std::min(32LL, fair));
+  t->chunk_rows = chunk_rows_fixed() > 0 || banded ? chunk32 : (int)std::max(4LL, std::min(64LL, fair));
   t->n_chunks = (int)div_up(span, (long long)t->chunk_rows);
-  t->n_items = (long long)t->n_chunks * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
+  t->n_items = (long long)t->n_chunks * per_tile_key;
+  t->n_items_ws = std::max(t->n_items, div_up(span, (long long)chunk32) * per_tile_key);
   t->smem_bytes = tf32 ? TcCfg<true>::kSmem : TcCfg<false>::kSmem;
   return t->smem_bytes <= 227 * 1024;
 }
@@ -1388,8 +1395,8 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
   w.CR = reinterpret_cast<float*>(take(sizeof(float) * (size_t)nr * (g.Hr + 1) * (g.Wr + 1)));
   w.hi = take((size_t)t.es * plane);
   w.lo = take((size_t)t.es * plane);
-  w.items = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items + 1)));  // list + its length
-  w.sched = reinterpret_cast<int*>(take(16 * (1 + 3 * (size_t)t.n_items + 3 * (size_t)sm_count())));
+  w.items = reinterpret_cast<int*>(take(sizeof(int) * ((size_t)t.n_items_ws + 1)));  // list + its length
+  w.sched = reinterpret_cast<int*>(take(16 * (1 + 3 * (size_t)t.n_items_ws + 3 * (size_t)sm_count())));
   w.bytes = off + 256;
   return w;
 }
@@ -1468,7 +1475,7 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
                               const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
                               int want_bands, int* band_done, TcBands* bands) {
   TcPlan t;
-  if (!tc_plan(g, pm, tf32, &t))
+  if (!tc_plan(g, pm, tf32, &t, band_done != nullptr))
     return fail(XC_ERR_UNSUPPORTED,
                 "split tensor-core paths support outputs up to 512 columns and right widths up to 256");
   const size_t need = ws_layout(nullptr, g, pm, t).bytes;
