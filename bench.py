@@ -358,6 +358,8 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and not args.no_configs:
         line["configs"] = config_studies(torch, xcorr)
         line["large_fft"] = large_fft_study(torch, xcorr)
+    if rank == 0 and not args.no_reference_gpu:
+        line["reference_gpu"] = reference_gpu_study(torch, xcorr, line)
     if rank == 0 and not args.no_cpu_baseline:
         rate, dt = cpu_reference_rate(left, right, 16, os.cpu_count() or 1)
         # the reference's cpu_* are single-threaded by construction: one core too
@@ -565,6 +567,138 @@ def config_studies(torch, xcorr, reps=20):
     return out
 
 
+def reference_gpu_study(torch, xcorr, line, reps=10):
+    """Baseline leg: the reference's own nai_shuffle GPU kernels on this GPU
+    (compiled unchanged from its sources into oracle/_ref/ by
+    oracle/build_ref_gpu.py, launched by oracle/ref_gpu.py with its launchers'
+    grid), on the same inputs as the plain kernel: one_to_one 128x128
+    (seed 1), the headline one_to_many 256x256 x 64 (seed 2), and 8 + 32 x
+    64x64 N(0,1) (seed 3) as n_to_mn and n_to_m, FP32.  Each kernel is timed
+    over a small sweep of the reference's own launch arguments
+    (benchmarking/args_test/args_test.yml ranges); the fastest is reported
+    with its error against FP64.  The n_to_mn / n_to_m forms launch per left
+    matrix on 8 streams, as the reference's drivers do (src/n_to_mn.hpp:553-572,
+    src/n_to_m.hpp:198-212).  Plain-kernel ("direct") times on the same
+    inputs, from this run, stand beside them."""
+    from oracle import oracle, ref_gpu
+
+    if not ref_gpu.available():
+        return {"unavailable": "reference cubins not built (run oracle/build_ref_gpu.py where the reference is)"}
+    R = ref_gpu.RefKernels()
+    streams = [torch.cuda.Stream() for _ in range(8)]
+    main = torch.cuda.current_stream()
+
+    def time_call(fn, zero=None):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            if zero is not None:
+                zero.zero_()
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def per_left(launch, n_left):
+        # one launch per left matrix, dealt to 8 streams after the main stream's work
+        ev = torch.cuda.Event()
+        ev.record(main)
+        for i in range(n_left):
+            s = streams[i % len(streams)]
+            s.wait_event(ev)
+            launch(i, s.cuda_stream)
+        for s in streams[:n_left]:
+            main.wait_stream(s)
+
+    def case(name, mode, left, right, variants, direct_ms):
+        n, H, W = left.shape
+        m = right.shape[0]
+        ref = oracle.run_mode(mode, left, right, dtype="f32acc64", threads=os.cpu_count() or 1)
+        if mode == "n_to_mn":  # rights of left l together (the reference's host de-interleave)
+            right = np.ascontiguousarray(right.reshape(m // n, n, H, W).transpose(1, 0, 2, 3).reshape(m, H, W))
+        dl, dr = torch.from_numpy(left).cuda(), torch.from_numpy(right).cuda()
+        n_out = ref.shape[0]
+        out = torch.zeros((n_out, 2 * H - 1, 2 * W - 1), device="cuda")
+        rows = []
+        for vname, launch, atomic in variants:
+            if mode in ("n_to_mn", "n_to_m"):
+                # rights of left l: n_to_mn takes rights l, l+n, ... (the reference de-interleaves them first,
+                # src/n_to_mn.hpp:165-171; the kernel work is the same on contiguous blocks), n_to_m all M
+                k = m // n if mode == "n_to_mn" else m
+                osz = (2 * H - 1) * (2 * W - 1)
+                fn = lambda launch=launch, k=k: per_left(
+                    lambda i, st: launch(dl.data_ptr() + i * H * W * 4,
+                                         dr.data_ptr() + (i * k * H * W * 4 if mode == "n_to_mn" else 0),
+                                         out.data_ptr() + i * k * osz * 4, k, st), n)
+            else:
+                fn = lambda launch=launch: launch(dl.data_ptr(), dr.data_ptr(), out.data_ptr(), m,
+                                                  main.cuda_stream)
+            ms = time_call(fn, out if atomic else None)
+            if atomic:
+                out.zero_()
+                fn()
+            torch.cuda.synchronize()
+            got = out.cpu().numpy().astype(np.float64)
+            if mode == "n_to_mn":  # blocks of left l's rights back to the reference order (output i: left i mod n)
+                got = got.reshape(n, m // n, *got.shape[1:]).transpose(1, 0, 2, 3).reshape(got.shape)
+            err = max(oracle.max_rel_to_max(got[q], ref[q]) for q in range(n_out))
+            rows.append({"kernel": vname, "ms": ms, "correlations_per_s": n_out / (ms / 1000.0),
+                         "max_rel_err_vs_fp64": err})
+        best = min(rows, key=lambda r: r["ms"])
+        return {"config": name, "dtype": "f32", "outputs": int(n_out), "best": best,
+                "direct_ms": direct_ms, "direct_speedup_over_best": (best["ms"] / direct_ms) if direct_ms else None,
+                "variants": rows}
+
+    def o2m_variants(H, W):
+        v = []
+        for S in (2, 4):
+            for M in (2, 4):
+                for Rr in (2, 4):
+                    for warps in (4, 8):
+                        v.append((f"ccn_shuffle_one_to_many_multirow_both_multimat_right<{S},{M},{Rr}> warps={warps}",
+                                  lambda l, r, o, k, st, S=S, M=M, Rr=Rr, warps=warps:
+                                  R.one_to_many_multirow_both_multimat_right(l, r, o, H, W, k, warps=warps, shifts=S,
+                                                                             mats=M, rows=Rr, stream=st), False))
+        return v
+
+    def wd_variants(H, W, mats_list):
+        v = []
+        for M in mats_list:
+            for max_rows in (8, 32):
+                v.append((f"ccn_shuffle_multimat_right_work_distribution<{M}, rectangle> warps=8 max_rows={max_rows}",
+                          lambda l, r, o, k, st, M=M, max_rows=max_rows:
+                          R.multimat_right_work_distribution(l, r, o, H, W, k, warps=8, mats=M, max_rows=max_rows,
+                                                             stream=st), True))
+        return v
+
+    def direct_ms_of(config, dtype="f32"):
+        for row in line.get("configs", []):
+            if row["config"] == config and row["dtype"] == dtype:
+                return row["direct"]["ms"]
+        return None
+
+    out = []
+    rng = np.random.default_rng(1)
+    a, b = rng.random((1, 128, 128)).astype(np.float32), rng.random((1, 128, 128)).astype(np.float32)
+    c1 = [(f"ccn_shuffle warps={w}", lambda l, r, o, k, st, w=w: R.ccn_shuffle(l, r, o, 128, 128, warps=w, stream=st),
+           False) for w in (4, 8, 16)]
+    c1 += wd_variants(128, 128, (1,))
+    out.append(case("one_to_one 128x128 U[0,1) seed 1", "one_to_one", a, b, c1,
+                    direct_ms_of("one_to_one 128x128 U[0,1) seed 1")))
+    left, right = make_inputs()
+    plain = line.get("plain_fp32", {}).get("ms_per_step")
+    out.append(case("one_to_many 256x256 x 64 U[0,1) seed 2 (the headline workload)", "one_to_many", left, right,
+                    o2m_variants(256, 256) + wd_variants(256, 256, (4, 8)), plain))
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((8, 64, 64)).astype(np.float32)
+    b = rng.standard_normal((32, 64, 64)).astype(np.float32)
+    for mode, cname in (("n_to_mn", "n_to_mn 8+32 x 64x64 N(0,1) seed 3"), ("n_to_m", "n_to_m 8+32 x 64x64 N(0,1) seed 3")):
+        out.append(case(cname, mode, a, b, o2m_variants(64, 64) + wd_variants(64, 64, (4,)), direct_ms_of(cname)))
+    return out
+
+
 def gpu_launches(method, steps):
     # kernels per xc_correlate call: direct 1; fft 2 pads + multiply + normalise
     # (+ cuFFT's own); tc: sums, means and accumulation windows, column sums,
@@ -583,6 +717,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged n_to_m side study")
     ap.add_argument("--no-configs", action="store_true", help="skip the other fixed configurations")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the baseline leg that times the reference's own GPU kernels")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -15,6 +15,8 @@
 //                        (src/fft_helpers.hpp:193-261): quadrant swap, division
 //                        by the transform size and crop in one coalesced pass.
 #include <algorithm>
+#include <cstring>
+#include <type_traits>
 
 #include "xc_common.cuh"
 #include "xc_internal.h"
@@ -49,10 +51,20 @@ constexpr int kGlueRows = 8;  // rows per block in the row-walking glue kernels
 // dst rows have pitch `dst_pitch` elements (>= pad_cols; the tail of a row
 // beyond pad_cols is left untouched).  A block walks `rows_per_block`
 // consecutive (matrix, row) pairs, so the row indices cost one division per
-// block; each thread writes 4 consecutive elements per step along the row.
+// block.  Each row is written as a scalar head up to its first 16-byte
+// boundary (rows of the in-place R2C layout, pitch 2 (px/2 + 1), start only
+// 8-byte aligned every other row), a body of 16-byte stores and a scalar
+// tail; rows outside the source are zeros and read nothing.
+template <typename T>
+__device__ __forceinline__ T pad_value(const T* srow, bool row_in, int sx, int cols) {
+  return (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
+}
+
 template <typename T>
 __global__ void pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int rows, int cols, int count, int pad_rows,
                            int pad_cols, int dst_pitch, int dst_y, int dst_x, int rows_per_block) {
+  constexpr int V = 16 / (int)sizeof(T);  // elements per 16-byte store
+  using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
   const long long n_rows = (long long)count * pad_rows;
   const long long r0 = (long long)blockIdx.x * rows_per_block;
   long long m = r0 / pad_rows;
@@ -60,50 +72,32 @@ __global__ void pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int r
   for (int i = 0; i < rows_per_block && r0 + i < n_rows; ++i) {
     const int sy = y - dst_y;
     const bool row_in = sy >= 0 && sy < rows;
-    const T* srow = src + (m * rows + sy) * (long long)cols;
+    const T* srow = src + (m * rows + (row_in ? sy : 0)) * (long long)cols;
     T* drow = dst + (r0 + i) * (long long)dst_pitch;
-    for (int x0 = threadIdx.x * 4; x0 < pad_cols; x0 += blockDim.x * 4) {
-      T v[4];
+    const int lead = min(pad_cols, (int)(((16u - ((uint32_t)(uintptr_t)drow & 15u)) & 15u) / sizeof(T)));
+    const int n_body = (pad_cols - lead) / V;
+    const int tail0 = lead + n_body * V;
+    if ((int)threadIdx.x < lead) drow[threadIdx.x] = pad_value(srow, row_in, (int)threadIdx.x - dst_x, cols);
+    if ((int)threadIdx.x < pad_cols - tail0)
+      drow[tail0 + threadIdx.x] = pad_value(srow, row_in, tail0 + (int)threadIdx.x - dst_x, cols);
+    Vec* body = reinterpret_cast<Vec*>(drow + lead);
+    for (int k = threadIdx.x; k < n_body; k += blockDim.x) {
+      const int x0 = lead + k * V;
       const int sx0 = x0 - dst_x;
-      if constexpr (sizeof(T) == 4) {
-        // one 16-byte load when the 4 source elements are in the row and aligned
-        if (row_in && sx0 >= 0 && sx0 + 4 <= cols && (((uintptr_t)(srow + sx0)) & 15) == 0) {
-          const float4 f = __ldg(reinterpret_cast<const float4*>(srow + sx0));
-          v[0] = f.x;
-          v[1] = f.y;
-          v[2] = f.z;
-          v[3] = f.w;
-        } else {
+      T v[V];
+      if (!row_in || sx0 >= cols || sx0 + V <= 0) {
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int sx = sx0 + e;
-            v[e] = (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
-          }
-        }
+        for (int e = 0; e < V; ++e) v[e] = T(0);
+      } else if (sx0 >= 0 && sx0 + V <= cols && (((uintptr_t)(srow + sx0)) & 15) == 0) {
+        const Vec f = __ldg(reinterpret_cast<const Vec*>(srow + sx0));
+        memcpy(v, &f, sizeof(f));
       } else {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int sx = sx0 + e;
-          v[e] = (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
-        }
+        for (int e = 0; e < V; ++e) v[e] = pad_value(srow, true, sx0 + e, cols);
       }
-      bool done = false;
-      if constexpr (sizeof(T) == 4) {
-        if (x0 + 4 <= pad_cols && (((uintptr_t)(drow + x0)) & 15) == 0) {
-          *reinterpret_cast<float4*>(drow + x0) = make_float4(v[0], v[1], v[2], v[3]);
-          done = true;
-        } else if (x0 + 4 <= pad_cols && (((uintptr_t)(drow + x0)) & 7) == 0) {
-          // rows of the in-place R2C layout (even pitch) start 8-byte aligned
-          *reinterpret_cast<float2*>(drow + x0) = make_float2(v[0], v[1]);
-          *reinterpret_cast<float2*>(drow + x0 + 2) = make_float2(v[2], v[3]);
-          done = true;
-        }
-      }
-      if (!done) {
-#pragma unroll
-        for (int e = 0; e < 4; ++e)
-          if (x0 + e < pad_cols) drow[x0 + e] = v[e];
-      }
+      Vec o;
+      memcpy(&o, v, sizeof(o));
+      body[k] = o;
     }
     if (++y == pad_rows) {
       y = 0;
