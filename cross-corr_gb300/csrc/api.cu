@@ -227,7 +227,8 @@ std::map<SelKey, xc_method> g_tuned;
 
 bool method_supported(xc_method m, xc_dtype dtype, xc_size2 left, xc_size2 right) {
   if (m == XC_METHOD_TC_BF16X3 || m == XC_METHOD_TC_TF32X3)
-    return dtype == XC_F32 && left.x + right.x - 1 <= 512 && right.x <= 256;
+    // FP32 only; the mean-correction kernel stages Wl + Wr + 2 floats per output row (8 rows, <= 200 KB)
+    return dtype == XC_F32 && (uint64_t)left.x + right.x + 2 <= 6400;
   return m == XC_METHOD_DIRECT || m == XC_METHOD_FFT;
 }
 

@@ -130,8 +130,9 @@ struct TcCfg {
   static constexpr int kTransW = TF ? 16 : 32;
   static constexpr int kTransBytes = kEpiWarps * 32 * (kTransW + 1) * 4;
   static constexpr int kOffBytes = kEpiWarps * 32 * 8;
+  static constexpr int kTabBytes = 2 * (kMaxKSteps + 1) * 4 + 8;  // the issuers' K-step windows
   static constexpr int kSmem = 1024 + kStages * kStageBytes + 4 * kTBytes + 4 * kXLen * 4 + kTransBytes +
-                               kOffBytes + kBarBytes;
+                               kOffBytes + kTabBytes + kBarBytes;
   static_assert(kCm * (kQ - 1) + 7 + kCm - 1 < kXLen, "T reads inside the staged row");
 };
 
@@ -145,17 +146,15 @@ struct TcParams {
   int mats_mode;    // 1: one TMA box per row shift spans P partners; 0: one box per partner spans DY rows
   int n_pgroups;    // ceil(K / P)
   int n_dytiles;    // ceil(Sy / DY)
-  int n_halves;     // 1: a work item covers every shift (both tensor-memory halves)
-  int half_w;       // shifts per half (a multiple of 16, at most 256): half h covers [h half_w, (h+1) half_w)
-  int nkc;          // 128-byte column chunks of a right row (64 BF16 or 32 TF32 columns)
+  // A work item covers one x-part (shifts [512 xp, 512 xp + 512), in two
+  // halves) and one k-part (right columns [256 kp, 256 kp + 256)) of its
+  // rows; parts of the same outputs add into them like row chunks do.
+  int n_parts;      // work items per tile key: n_xparts * n_kparts
+  int n_kparts;
+  int half_w;       // shifts per half (a multiple of 16, at most 256): half h of x-part xp
+                    // covers [512 xp + h half_w, 512 xp + (h+1) half_w)
+  int nkc;          // 128-byte column chunks of a whole k-part (64 BF16 or 32 TF32 columns each)
   int kstep;        // columns per K-step: 16 (BF16) or 8 (TF32)
-  // The MMA window of each (half, K-step): the shifts whose overlap with the
-  // K-step's right columns is not empty, rounded out to 16.  Packed: TMEM
-  // column (bits 0-8), N / 16 (9-13), active (14), Toeplitz core-matrix
-  // offset (16-23).  kreset: the whole half (the first MMA of a window,
-  // which also zeroes the accumulator).
-  uint32_t ktab[2][kMaxKSteps];
-  uint32_t kreset[2];
   const int* flush_tab;  // drain TMEM every this many left rows, per (left matrix, partner group)
   int chunk_rows;   // left rows per work item (a longer row range is split over items)
   const int* items;  // non-empty work items, most left rows first (tc_item encoding)
@@ -325,44 +324,51 @@ __device__ __forceinline__ bool bar_red_or(bool v, int id, int nthreads) {
   return r != 0;
 }
 
-// The window of half h and K-step j (right columns kstep*j ..): shifts sx
-// whose left columns sx + k - (Wr-1) meet the row for some column k of the
-// K-step, clipped to the half and rounded out to 16; packed as in ktab.  The
-// MMA's B operand starts at X[w0 + kstep*j] (X[i] = centred left row at
-// column i - (Wr-1)), core matrix (w0 + kstep*j) / kCm.
-inline uint32_t pack_window(int dcol, int n, bool active, int bq) {
+// The MMA window of half h and the K-step whose first right column is k0,
+// in the x-part starting at shift s0 and the k-part starting at column
+// kbase: the shifts sx whose left columns sx + k - (Wr-1) meet the row for
+// some column k of the K-step, clipped to the half and rounded out to 16.
+// Packed: TMEM column (bits 0-8), N / 16 (9-13), active (14), and the core
+// matrix of the Toeplitz buffer the MMA's B operand starts at (16-23): the
+// item's staged row is X[i] = Lp[s0 + kbase + i], so B[n][k] = Lp[w0 + n +
+// k0 + k] starts at X[w0 - s0 + k0 - kbase].  kreset = true: the whole half
+// from the part's first column (the first MMA of a window, which also
+// starts every accumulator column afresh).
+__host__ __device__ __forceinline__ uint32_t pack_window(int dcol, int n, bool active, int bq) {
   return (uint32_t)dcol | ((uint32_t)(n / 16) << 9) | ((active ? 1u : 0u) << 14) | ((uint32_t)bq << 16);
 }
 
-inline void kstep_windows(int Wl, int Wr, int Sx, int half_w, int kstep, int cm, int nks, uint32_t ktab[2][kMaxKSteps],
-                          uint32_t kreset[2]) {
-  for (int h = 0; h < 2; ++h) {
-    const int H0 = h * half_w, H1 = std::min(Sx, H0 + half_w);
-    kreset[h] = pack_window(h * kHalfCols, half_w, true, H0 / cm);
-    for (int j = 0; j < kMaxKSteps; ++j) {
-      ktab[h][j] = 0;
-      const int k0 = j * kstep;
-      if (j >= nks || k0 >= Wr || H0 >= H1) continue;
-      const int k_hi = std::min(k0 + kstep, Wr) - 1;
-      const int lo = std::max(H0, Wr - 1 - k_hi), hi = std::min(H1, Wr - 1 + Wl - k0);
-      if (lo >= hi) continue;
-      const int w0 = H0 + (lo - H0) / 16 * 16;
-      const int n = (hi - w0 + 15) / 16 * 16;
-      ktab[h][j] = pack_window(h * kHalfCols + (w0 - H0), n, true, (w0 + k0) / cm);
-    }
-  }
+__host__ __device__ __forceinline__ uint32_t kstep_window(const TcParams& p, int s0, int kbase, int h, int k0,
+                                                          bool reset) {
+  const int cm = p.kstep == 16 ? 8 : 4;
+  const int H0 = s0 + h * p.half_w, H1 = min(p.Sx, H0 + p.half_w);
+  if (reset) return pack_window(h * kHalfCols, p.half_w, true, (H0 - s0) / cm);
+  if (k0 >= p.Wr || H0 >= H1) return 0;
+  const int k_hi = min(k0 + p.kstep, p.Wr) - 1;
+  const int lo = max(H0, p.Wr - 1 - k_hi), hi = min(H1, p.Wr - 1 + p.Wl - k0);
+  if (lo >= hi) return 0;
+  const int w0 = H0 + (lo - H0) / 16 * 16;
+  const int n = (hi - w0 + 15) / 16 * 16;
+  return pack_window(h * kHalfCols + (w0 - H0), n, true, (w0 - s0 + k0 - kbase) / cm);
 }
 
 // One work item: every shift of one (left matrix, partner group, row-shift
 // group, chunk of left rows).
 struct TcItem {
   int l, p0, dy0, a_lo, n_rows, rdim2;
+  int s0, kbase, nkc;  // x-part's first shift, k-part's first right column, its 128-byte chunks
   int band;  // output row band of the item's row-shift tile
 };
 
-// The item of tile key (rank, lp) covering the tile's left rows
+// The item of tile key (rank, lp, part) covering the tile's left rows
 // [row0, row0 + n) (clipped to the tile); false when that is empty.
-__host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int lp, int rank, int row0, int n, TcItem* w) {
+__host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int part, int lp, int rank, int row0, int n,
+                                                  TcItem* w) {
+  const int xp = part / p.n_kparts, kp = part % p.n_kparts;
+  w->s0 = 512 * xp;
+  w->kbase = 256 * kp;
+  const int chunk_cols = 4 * p.kstep;
+  w->nkc = min(p.nkc, (p.Wr - w->kbase + chunk_cols - 1) / chunk_cols);
   w->l = lp / p.n_pgroups;
   w->p0 = (lp % p.n_pgroups) * p.P;
   const int t = centre_out(rank, p.n_dytiles, (p.Hr - 1) / p.DY);
@@ -379,21 +385,25 @@ __host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int lp, int
   return w->n_rows > 0;
 }
 
-// idx = (chunk * n_dytiles + rank) * per_rank + lp; false when the item has
-// no left rows.
+// idx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_parts + part; false
+// when the item has no left rows.
 __host__ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
   const int per_rank = p.pm.n_left * p.n_pgroups;
-  const int lp = (int)(idx % per_rank);
-  const int rank = (int)((idx / per_rank) % p.n_dytiles);
-  const int chunk = (int)(idx / ((long long)per_rank * p.n_dytiles));
-  return tc_piece(p, lp, rank, chunk * p.chunk_rows, p.chunk_rows, w);
+  const int part = (int)(idx % p.n_parts);
+  const long long key = idx / p.n_parts;
+  const int lp = (int)(key % per_rank);
+  const int rank = (int)((key / per_rank) % p.n_dytiles);
+  const int chunk = (int)(key / ((long long)per_rank * p.n_dytiles));
+  return tc_piece(p, part, lp, rank, chunk * p.chunk_rows, p.chunk_rows, w);
 }
 
-// An entry of the host-built schedule.
+// An entry of the host-built schedule: tile key (rank * per_rank + lp) *
+// n_parts + part.
 __host__ __device__ __forceinline__ bool tc_entry(const TcParams& p, int4 e, TcItem* w) {
   if (e.x < 0) return false;
   const int per_rank = p.pm.n_left * p.n_pgroups;
-  return tc_piece(p, e.x % per_rank, e.x / per_rank, e.y, e.z, w);
+  const int part = e.x % p.n_parts, key = e.x / p.n_parts;
+  return tc_piece(p, part, key % per_rank, key / per_rank, e.y, e.z, w);
 }
 
 // Lists the non-empty work items by output row band (in the order
@@ -476,7 +486,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   float* xs = reinterpret_cast<float*>(t_buf + 4 * C::kTBytes);        // [row buffer][hi, lo] x kXLen staged row
   float* trans = xs + 4 * kXLen;                                       // [epilogue warp] transpose tile
   long long* offs = reinterpret_cast<long long*>(trans + kEpiWarps * 32 * (C::kTransW + 1));  // [warp][lane row]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(offs + kEpiWarps * 32);
+  uint32_t* ktab_all = reinterpret_cast<uint32_t*>(offs + kEpiWarps * 32);  // [half][K-step, then reset]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(ktab_all + 2 * (kMaxKSteps + 1) + 2);
   uint64_t* a_full = bars;                   // [kStages] right-row tile landed
   uint64_t* a_empty = bars + C::kStages;     // [kStages] tile consumed
   uint64_t* r_full = bars + 2 * C::kStages;  // [2] Toeplitz row buffer written
@@ -535,7 +546,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (!round_item(p, n_items, round, &w)) continue;
         for (int ai = 0; ai < w.n_rows && ok; ++ai) {
           const int a = w.a_lo + ai;
-          for (int kc = 0; kc < p.nkc && ok; ++kc) {
+          for (int kc = 0; kc < w.nkc && ok; ++kc) {
             for (int pl = 0; pl < 2; ++pl, ++it) {
               const int s = it % C::kStages;
               if (!wait_or_abort_sleep(&a_empty[s], ((it / C::kStages) & 1) ^ 1, abort_flag, p.flags, 11)) {
@@ -545,7 +556,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               mbar_arrive_expect_tx(&a_full[s], kStageBytes);
               unsigned char* dst = a_tiles + s * kStageBytes;
               const CUtensorMap* map = pl == 0 ? &map_hi : &map_lo;
-              const int x = kc * 4 * p.kstep;  // first column of the chunk
+              const int x = w.kbase + kc * 4 * p.kstep;  // first column of the chunk
               if (p.mats_mode) {
                 for (int d = 0; d < p.DY; ++d)
                   tma_load_4d(dst + d * p.P * 128, map, &a_full[s], x, a - (w.dy0 + d), w.rdim2, w.p0);
@@ -569,7 +580,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     // shift half h (its own accumulator, tensor-memory columns
     // [256 h, 256 h + 256)) and commits to the shared consumed barriers.
     const int h = warp == 1 ? 0 : 1;
-    if (lane == 0) {
+    uint32_t* ktab = ktab_all + h * (kMaxKSteps + 1);
+    {
       // A (right-row tile): SBO 1024 B (8 rows x 128 B), 128-byte swizzle.  B
       // (Toeplitz buffer): no swizzle, LBO 128 B along K, SBO 128 B (BF16) or
       // 256 B (TF32) along N.
@@ -578,8 +590,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t idesc0 = TF ? idesc_tf32_f32(128, 0) : idesc_bf16_f32(128, 0);
       const uint32_t a_word = ((smem_u32(a_tiles) >> 4) & 0x3FFFu) | (1u << 16);
       const uint32_t t_word = ((smem_u32(t_buf) >> 4) & 0x3FFFu) | ((128u >> 4) << 16);
-      const uint32_t* ktab = p.ktab[h];
-      const uint32_t kres = p.kreset[h];
       int s = 0, rb = 0;                      // stage, Toeplitz row buffer
       uint32_t s_phase = 0, r_phase = 0, t_phase = 1;
       bool s_ready = false;                   // stage s seen landed ahead of time
@@ -587,6 +597,14 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long round = 0; round < n_round && ok; ++round) {
         TcItem w;
         if (!round_item(p, n_items, round, &w)) continue;
+        // the item's windows, one K-step per lane (the whole warp), then lane
+        // 0 issues
+        __syncwarp();
+        ktab[lane] = kstep_window(p, w.s0, w.kbase, h, w.kbase + lane * p.kstep, false);
+        if (lane == 0) ktab[kMaxKSteps] = kstep_window(p, w.s0, w.kbase, h, w.kbase, true);
+        __syncwarp();
+        if (lane == 0) {
+        const uint32_t kres = ktab[kMaxKSteps];
         const int n_rows = w.n_rows;
         const int flush = p.flush_tab[w.l * p.n_pgroups + w.p0 / p.P];
         int rows_in = 0;
@@ -606,7 +624,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           // this row's Toeplitz buffers (hi, lo), 16-byte units
           const uint32_t th = t_word + (uint32_t)rb * (2 * C::kTBytes >> 4);
           const uint32_t tl = th + (C::kTBytes >> 4);
-          for (int kc = 0; kc < p.nkc && ok; ++kc) {
+          for (int kc = 0; kc < w.nkc && ok; ++kc) {
             // the window's first MMA covers the whole half and starts the
             // accumulator afresh
             const uint32_t reset = (rows_in == 0 && kc == 0) ? 1u : 0u;
@@ -659,15 +677,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             rows_in = 0;
           }
         }
+        }
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
       }
       // All MMAs issued by this thread must finish before TMEM is released.
-      mma_commit(&mma_done[h]);
-      mbar_wait_bounded(&mma_done[h], 0, 1u << 22);
+      if (lane == 0) {
+        mma_commit(&mma_done[h]);
+        mbar_wait_bounded(&mma_done[h], 0, 1u << 22);
+      }
     }
   } else if (warp < 2 + kBuilderWarps) {
     // ------------------------------------------------------------ Toeplitz builders
-    // Per left row: stage the centred, split row X[i] = Lp[i] (hi and lo
-    // parts; Lp[i] = L[a][i - (Wr-1)], zero outside the row), then write the
+    // Per left row: stage the centred, split row X[i] = Lp[s0 + kbase + i]
+    // (hi and lo parts; Lp[j] = L[a][j - (Wr-1)], zero outside the row), then write the
     // core-matrix buffer T[q][r][t] = X[kCm q + r + t] of both parts into the
     // free row buffer.
     const int bt = threadIdx.x - 64;  // 0..127
@@ -679,7 +701,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!round_item(p, n_items, round, &w)) continue;
       const float* lrow_base = p.left + (long long)w.l * p.Hl * p.Wl;
       const float mu = __ldg(p.mu_left + w.l);
-      const int x_off = -(p.Wr - 1);  // left column of X[0]
+      const int x_off = w.s0 + w.kbase - (p.Wr - 1);  // left column of X[0]
       int ai = 0;
       for (; ai < w.n_rows; ++ai, ++rows_done) {
         const int rbuf = rows_done & 1;
@@ -795,15 +817,16 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           tc_fence_after();
-          const int sx_base = h * p.half_w + 64 * cq;
-          const bool live = sx_base < min(p.Sx, (h + 1) * p.half_w);
+          const int sx_end = min(p.Sx, w.s0 + (h + 1) * p.half_w);  // this half's shifts end here
+          const int sx_base = w.s0 + h * p.half_w + 64 * cq;
+          const bool live = sx_base < sx_end;
           const uint32_t col0 = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * kHalfCols + 64 * cq);
           // reductions of lane rows x TW shifts from the transpose tile: shift
           // column cc, lane rows (lane / TW) + (32 / TW) i
           auto reduce_tile = [&](int sx0) {
             const int cc = lane & (TW - 1);
             const int sx = sx0 + cc;
-            const uint32_t in_x = (sx < p.Sx && sx < (h + 1) * p.half_w) ? 1u : 0u;
+            const uint32_t in_x = sx < sx_end ? 1u : 0u;
 #pragma unroll
             for (int i = 0; i < TW; ++i) {
               const int r = (lane / TW) + (32 / TW) * i;
@@ -1186,14 +1209,17 @@ __global__ void __launch_bounds__(256) rowscan_kernel(const PrepSide a, const Pr
 // bound by instruction issue, hence the column-wise reuse of the index
 // arithmetic.  FP32 (the centred sums are small, and the result's rounding
 // stays near 1e-7 of max|out|).
-constexpr int kCorrLeft = 516, kCorrRight = 260;  // staged widths: Wl + 1 <= 513, Wr + 1 <= 257
-constexpr int kCorrStage = kCorrLeft + kCorrRight;
+// Staged floats per output row: D_L (Wl + 1) and D_R (Wr + 1), padded to 4.
+inline int corr_stage(int Wl, int Wr) { return (Wl + Wr + 2 + 3) / 4 * 4; }
 __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out, const float* __restrict__ SL,
                                                          const float* __restrict__ SR,
                                                          const float* __restrict__ mu_l,
                                                          const float* __restrict__ mu_r, int Hl, int Wl, int Hr,
-                                                         int Wr, int Sy, int Sx, long long n_rows, PairMap pm) {
-  __shared__ float stage[8][kCorrStage];  // per row: D_L in [0, Wl], D_R in [Wl + 1, Wl + Wr + 1]
+                                                         int Wr, int Sy, int Sx, long long n_rows, PairMap pm,
+                                                         int stage_w) {
+  // per row: D_L in [0, Wl], D_R in [Wl + 1, Wl + Wr + 1] (dynamic: 8 x stage_w floats)
+  extern __shared__ float stage_all[];
+  auto stage = [&](int r) { return stage_all + r * stage_w; };
   __shared__ float coef[8][4];            // per row: mu_L, mu_R, mu_L mu_R, overlap rows
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long long row0 = blockIdx.x * 8LL;
@@ -1220,7 +1246,7 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
     const float* l1 = SL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
     const float* r0 = SR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
     const float* r1 = SR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
-    float* st = stage[wid];
+    float* st = stage(wid);
     const int nl = Wl + 1, nt = Wl + Wr + 2;
     for (int t0 = 0; t0 < nt; t0 += 256) {
       float a[8], b[8];
@@ -1270,7 +1296,7 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 #pragma unroll
     for (int w = 0; w < 8; ++w) {
       if (w < n_here) {
-        const float* st = stage[w];
+        const float* st = stage(w);
         const float sl = st[x1] - st[x0];
         const float sr = st[j1] - st[j0];
         o[(long long)w * Sx] = fmaf(cr[w], sl, fmaf(cl[w], sr, clr[w] * (cy[w] * width)));
@@ -1280,7 +1306,7 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
 }
 
 struct TcPlan {
-  int P, DY, mats_mode, half_w, nkc, kstep, es, pitch, n_chunks, chunk_rows;
+  int P, DY, mats_mode, half_w, nkc, kstep, es, pitch, n_chunks, chunk_rows, n_parts, n_kparts;
   long long n_items;
   long long n_items_ws;  // items at 32-row chunks: the work list and schedule space of either form of launch
   int smem_bytes;
@@ -1290,17 +1316,21 @@ int chunk_rows_fixed();
 int sm_count();
 
 bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool banded = false) {
-  if (g.Sx > 512 || g.Wr > 256) return false;  // two 256-shift halves, 256 right columns
+  // the mean-correction kernel stages 8 output rows' table differences
+  if ((size_t)8 * corr_stage(g.Wl, g.Wr) * sizeof(float) > 200 * 1024) return false;
   int P = 1;
   while (P < kLanes && P < pm.K) P *= 2;
   t->P = P;
   t->DY = kLanes / P;
   t->mats_mode = P >= 8 ? 1 : 0;
-  t->half_w = ((g.Sx + 1) / 2 + 15) / 16 * 16;
+  // x-parts of 512 shifts (two halves), k-parts of 256 right columns
+  t->half_w = g.Sx > 512 ? 256 : ((g.Sx + 1) / 2 + 15) / 16 * 16;
+  t->n_kparts = (g.Wr + 255) / 256;
+  t->n_parts = ((g.Sx + 511) / 512) * t->n_kparts;
   t->es = tf32 ? 4 : 2;                 // bytes per operand element
   t->kstep = tf32 ? 8 : 16;             // columns per MMA K-step (32 bytes)
   const int chunk = 128 / t->es;        // columns per 128-byte TMA box row
-  t->nkc = (g.Wr + chunk - 1) / chunk;
+  t->nkc = (std::min(g.Wr, 256) + chunk - 1) / chunk;
   t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
   // left rows per item: at most 64, fewer when that leaves fewer than two
   // items per SM (small problems), at least 4.  Longer items end fewer
@@ -1309,8 +1339,8 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool ba
   // host plan cuts each band into pieces of half to one item, and 152 CTAs
   // need that many pieces per band.
   const long long span = t->DY - 1 + std::min(g.Hl, g.Hr);
-  const long long rows_all = span * div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, P);
-  const long long per_tile_key = (long long)div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P);
+  const long long per_tile_key = (long long)div_up(g.Sy, t->DY) * pm.n_left * div_up(pm.K, t->P) * t->n_parts;
+  const long long rows_all = span * per_tile_key;
   const long long fair = rows_all / (2LL * sm_count());
   const int chunk32 = chunk_rows_fixed() > 0 ? chunk_rows_fixed() : (int)std::max(4LL, std::min(32LL, fair));
   t->chunk_rows = chunk_rows_fixed() > 0 || banded ? chunk32 : (int)std::max(4LL, std::min(64LL, fair));
@@ -1432,16 +1462,19 @@ xc_status upload_band_schedule(const TcParams& prm, int G, int* region, long lon
   in.DY = prm.DY;
   in.n_dytiles = prm.n_dytiles;
   in.per_rank = prm.pm.n_left * prm.n_pgroups;
-  in.n_halves = 1;
+  in.n_halves = prm.n_parts;
   in.chunk_rows = prm.chunk_rows;
   in.n_bands = prm.n_bands;
   for (int b = 0; b <= prm.n_bands; ++b) in.band_start[b] = prm.band_start[b];
   for (int b = 0; b < prm.n_bands; ++b) in.band_rank[b] = prm.band_rank[b];
-  // cost of a left row: the MMA windows of both halves, in 16-shift units
+  // cost of a left row of a part: the MMA windows of both halves (of the
+  // first part), in 16-shift units
   int units = 0;
   for (int h = 0; h < 2; ++h)
-    for (int j = 0; j < kMaxKSteps; ++j)
-      if ((prm.ktab[h][j] >> 14) & 1u) units += (int)((prm.ktab[h][j] >> 9) & 31u);
+    for (int j = 0; j < 4 * prm.nkc; ++j) {
+      const uint32_t e = kstep_window(prm, 0, 0, h, j * prm.kstep, false);
+      if ((e >> 14) & 1u) units += (int)((e >> 9) & 31u);
+    }
   in.ks[0] = in.ks[1] = std::max(1, units);
   std::vector<BandPiece> sched;
   plan_band_schedule(in, G, &sched, band_items);
@@ -1477,7 +1510,7 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   TcPlan t;
   if (!tc_plan(g, pm, tf32, &t, band_done != nullptr))
     return fail(XC_ERR_UNSUPPORTED,
-                "split tensor-core paths support outputs up to 512 columns and right widths up to 256");
+                "split tensor-core paths need Wl + Wr below 6400");
   const size_t need = ws_layout(nullptr, g, pm, t).bytes;
   if (workspace == nullptr || ws_bytes < need)
     return fail(XC_ERR_WORKSPACE, "split tensor-core path needs " + std::to_string(need) + " bytes of workspace");
@@ -1527,10 +1560,14 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   }
   // 4. the mean terms initialise the output
   {
-    if (g.Wl + 1 > kCorrLeft || g.Wr + 1 > kCorrRight) return fail(XC_ERR_UNSUPPORTED, "correction widths");
+    const int stage_w = corr_stage(g.Wl, g.Wr);
+    const size_t corr_smem = (size_t)8 * stage_w * sizeof(float);
+    if (corr_smem > 200 * 1024) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths: Wl + Wr above 6400");
+    if (corr_smem > 48 * 1024)
+      XC_CUDA_TRY(cudaFuncSetAttribute(correction_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
     const long long n_rows = (long long)n_out * g.Sy;
-    correction_kernel<<<(unsigned)((n_rows + 7) / 8), 256, 0, stream>>>(
-        out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, n_rows, pm);
+    correction_kernel<<<(unsigned)((n_rows + 7) / 8), 256, corr_smem, stream>>>(
+        out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, n_rows, pm, stage_w);
   }
   XC_CUDA_TRY(cudaGetLastError());
 
@@ -1570,11 +1607,11 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   prm.mats_mode = t.mats_mode;
   prm.n_pgroups = div_up(pm.K, t.P);
   prm.n_dytiles = div_up(g.Sy, t.DY);
-  prm.n_halves = 1;
+  prm.n_parts = t.n_parts;
+  prm.n_kparts = t.n_kparts;
   prm.half_w = t.half_w;
   prm.nkc = t.nkc;
   prm.kstep = t.kstep;
-  kstep_windows(g.Wl, g.Wr, g.Sx, t.half_w, t.kstep, tf32 ? 4 : 8, 4 * t.nkc, prm.ktab, prm.kreset);
   prm.flush_tab = w.flush;
   prm.chunk_rows = t.chunk_rows;
   prm.n_chunks = t.n_chunks;
@@ -1698,7 +1735,7 @@ extern "C" xc_status xc_correlate_tc_noalloc(xc_mode mode, const float* d_left, 
   TcPlan t;
   if (!tc_plan(g, pm, false, &t))
     return fail(XC_ERR_UNSUPPORTED,
-                "split-BF16 tensor path supports outputs up to 512 columns and right widths up to 256");
+                "split-BF16 tensor path needs Wl + Wr below 6400");
   const size_t need = ws_layout(nullptr, g, pm, t).bytes;
   if (need > (size_t)XC_TC_NOALLOC_SCRATCH_BYTES)
     return fail(XC_ERR_WORKSPACE, "xc_correlate_tc_noalloc: this problem needs " + std::to_string(need) +

@@ -51,6 +51,13 @@ TC_SHAPES = [
     ("one_to_many", 1, 130, (9, 11), (8, 13), "uniform"),
     ("n_to_mn", 2, 10, (12, 180), (10, 150), "signed"),
     ("one_to_one", 1, 1, (40, 60), (30, 50), "uniform"),
+    # beyond 512 output columns (x-parts of 512 shifts) and 256 right columns
+    # (k-parts of 256 columns), including a small template on a wide left
+    ("one_to_many", 1, 3, (30, 700), (20, 300), "uniform"),
+    ("one_to_one", 1, 1, (8, 300), (8, 300), "normal"),
+    ("n_to_m", 2, 2, (12, 520), (10, 260), "signed"),
+    ("one_to_many", 1, 9, (40, 1100), (16, 16), "uniform"),
+    ("one_to_one", 1, 1, (6, 40), (5, 600), "normal"),
 ]
 
 
@@ -86,8 +93,10 @@ def test_tc_bench_shape_accuracy(method):
 
 @pytest.mark.parametrize("method", TC_METHODS)
 def test_tc_rejects_unsupported_sizes(method):
+    """Wl + Wr above 6400: the mean-correction kernel's staged rows would
+    pass its shared-memory budget."""
     with pytest.raises(xcorr.XcError) as e:
-        xcorr.correlate("one_to_one", dev(seeded((1, 8, 300), 1)), dev(seeded((1, 8, 300), 2)), method=method)
+        xcorr.correlate("one_to_one", dev(seeded((1, 2, 4000), 1)), dev(seeded((1, 2, 2500), 2)), method=method)
     assert e.value.status == 4
 
 
