@@ -358,6 +358,7 @@ def run_ours(args, rank, world, local_rank):
     if rank == 0 and not args.no_configs:
         line["configs"] = config_studies(torch, xcorr)
         line["large_fft"] = large_fft_study(torch, xcorr)
+        line["templates"] = template_study(torch, xcorr)
     if rank == 0 and not args.no_reference_gpu:
         line["reference_gpu"] = reference_gpu_study(torch, xcorr, line)
     if rank == 0 and not args.no_cpu_baseline:
@@ -394,6 +395,46 @@ def sampled_fp64(left, right, outs, ref_scale, rng, n_shifts):
             exact = float(np.sum(L[y0 + dy:y1 + dy, x0 + dx:x1 + dx] * R[y0:y1, x0:x1]))
             worst = max(worst, abs(float(outs[k][oy, ox]) - exact) / ref_scale[k])
     return worst
+
+
+def template_study(torch, xcorr, reps=5):
+    """Small templates on large lefts (one_to_many, U[0,1), seed 6): 16 right
+    matrices of 16x16, 32x32 or 64x64 on a left of 256x256 to 2048x2048, the
+    regime where the FFT path transforms the whole padded left for a few
+    small products.  Every method's time and its error against the library's
+    FP64 FFT; the fastest at <= 1e-5 is named."""
+    out = []
+    for side in (256, 512, 1024, 2048):
+        for t in (16, 32, 64):
+            rng = np.random.default_rng(6)
+            left = torch.from_numpy(rng.random((1, side, side)).astype(np.float32)).cuda()
+            right = torch.from_numpy(rng.random((16, t, t)).astype(np.float32)).cuda()
+            ref = xcorr.correlate("one_to_many", left.double(), right.double(), method="fft")
+            scale = ref.abs().amax(dim=(1, 2))
+            row = {"left": side, "template": t, "rights": 16}
+            best = None
+            for method in ("direct", "fft", "tc_bf16x3"):
+                ws_bytes = xcorr.workspace_size("one_to_many", "f32", method, (side, side), 1, (t, t), 16)
+                ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device="cuda")
+                o = xcorr.correlate("one_to_many", left, right, method=method, workspace=ws if ws_bytes else None)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for _ in range(reps):
+                    xcorr.correlate("one_to_many", left, right, method=method, out=o, workspace=ws if ws_bytes else None)
+                e1.record()
+                e1.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                err = float(((o.double() - ref).abs().amax(dim=(1, 2)) / scale).max())
+                row[method] = {"ms": ms, "max_rel_err_vs_fp64": err}
+                if err <= GATE and (best is None or ms < row[best]["ms"]):
+                    best = method
+                del o, ws
+            row["fastest_within_gate"] = best
+            out.append(row)
+            del left, right, ref
+    torch.cuda.empty_cache()
+    return out
 
 
 def large_fft_study(torch, xcorr, reps=5):
