@@ -20,7 +20,7 @@
 namespace xc {
 const char* last_error_cstr();
 xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32);
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows = 64);
 size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32);
 }  // namespace xc
 
@@ -208,10 +208,16 @@ size_t fft_workspace_bytes(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t
 }
 
 // ---------------------------------------------------------------------------
-// Method selection for XC_METHOD_AUTO: the MLP's prediction when weights are
-// installed, else the last exhaustive-autotune result for the problem, else
-// the plain kernel.
+// Algorithm selection for XC_METHOD_AUTO: the MLP's prediction when weights
+// are installed, else the last exhaustive-autotune result for the problem,
+// else (in xc_correlate, which has the buffers) an exhaustive autotune.
 // ---------------------------------------------------------------------------
+// The selector's candidates, in the order of the network's outputs: the
+// plain kernel's three tile shapes, the FFT path, the split-BF16 path with
+// items of at most 32 or 64 left rows, the split-TF32 path.
+const xc_algo kAlgos[XC_N_ALGOS] = {{XC_METHOD_DIRECT, 1}, {XC_METHOD_DIRECT, 2},    {XC_METHOD_DIRECT, 3},
+                                    {XC_METHOD_FFT, 0},    {XC_METHOD_TC_BF16X3, 32}, {XC_METHOD_TC_BF16X3, 64},
+                                    {XC_METHOD_TC_TF32X3, 0}};
 std::mutex g_sel_mutex;
 #if __has_include("selector_weights.inc")
 #include "selector_weights.inc"
@@ -223,13 +229,25 @@ std::vector<float> g_sel_params(kSelectorBuiltin, kSelectorBuiltin + XC_MLP_PARA
 std::vector<float> g_sel_params;  // empty: no network installed
 #endif
 using SelKey = std::tuple<int, int, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t>;
-std::map<SelKey, xc_method> g_tuned;
+std::map<SelKey, xc_algo> g_tuned;
 
 bool method_supported(xc_method m, xc_dtype dtype, xc_size2 left, xc_size2 right) {
   if (m == XC_METHOD_TC_BF16X3 || m == XC_METHOD_TC_TF32X3)
     // FP32 only; the mean-correction kernel stages Wl + Wr + 2 floats per output row (8 rows, <= 200 KB)
     return dtype == XC_F32 && (uint64_t)left.x + right.x + 2 <= 6400;
   return m == XC_METHOD_DIRECT || m == XC_METHOD_FFT;
+}
+
+// Tiles: plain kernel 0 (its default) to 3; FFT 0; split paths 0 (items of
+// at most 64 left rows) or the item length cap, 4 to 1024.
+bool tile_valid(xc_algo a) {
+  switch (a.method) {
+    case XC_METHOD_DIRECT: return a.tile >= 0 && a.tile <= 3;
+    case XC_METHOD_FFT: return a.tile == 0;
+    case XC_METHOD_TC_BF16X3:
+    case XC_METHOD_TC_TF32X3: return a.tile == 0 || (a.tile >= 4 && a.tile <= 1024);
+    default: return false;
+  }
 }
 
 void selector_features(xc_mode mode, xc_size2 left, uint32_t n_left, xc_size2 right, uint32_t n_right,
@@ -271,24 +289,69 @@ void host_forward(const std::vector<float>& P, const float* x, float* y) {
   }
 }
 
-xc_method select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
-                        uint32_t n_right) {
-  static const xc_method order[XC_MLP_OUT] = {XC_METHOD_DIRECT, XC_METHOD_FFT, XC_METHOD_TC_BF16X3};
+// The algorithm XC_METHOD_AUTO runs: the network's fastest prediction among
+// the supported candidates, else the tuning record; false when neither
+// exists.
+bool select_algorithm(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                      uint32_t n_right, xc_algo* algo) {
   std::lock_guard<std::mutex> lock(g_sel_mutex);
   PairMap pm;
   uint64_t n_out = 1;
-  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out)) return XC_METHOD_DIRECT;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out)) return false;
   if (!g_sel_params.empty()) {
     float f[XC_MLP_IN], y[XC_MLP_OUT];
     selector_features(mode, left, n_left, right, n_right, n_out, f);
     host_forward(g_sel_params, f, y);
     int best = -1;
     for (int o = 0; o < XC_MLP_OUT; ++o)
-      if (method_supported(order[o], dtype, left, right) && (best < 0 || y[o] < y[best])) best = o;
-    return best >= 0 ? order[best] : XC_METHOD_DIRECT;
+      if (method_supported(kAlgos[o].method, dtype, left, right) && (best < 0 || y[o] < y[best])) best = o;
+    if (best >= 0) {
+      *algo = kAlgos[best];
+      return true;
+    }
   }
   auto it = g_tuned.find(SelKey{(int)mode, (int)dtype, left.x, left.y, n_left, right.x, right.y, n_right});
-  return it != g_tuned.end() ? it->second : XC_METHOD_DIRECT;
+  if (it == g_tuned.end()) return false;
+  *algo = it->second;
+  return true;
+}
+
+size_t algo_workspace(xc_mode mode, xc_dtype dtype, xc_algo a, xc_size2 left, uint32_t n_left, xc_size2 right,
+                      uint32_t n_right, const PairMap& pm) {
+  switch (a.method) {
+    case XC_METHOD_FFT: return fft_workspace_bytes(mode, dtype, left, n_left, right, n_right);
+    case XC_METHOD_TC_BF16X3:
+    case XC_METHOD_TC_TF32X3:
+      return dtype == XC_F32 ? tc_workspace_size(make_geometry(left, right), pm, a.method == XC_METHOD_TC_TF32X3) : 0;
+    default: return 0;
+  }
+}
+
+// One correlation with a given algorithm (method and tile); arguments
+// already checked.
+xc_status run_algo(xc_mode mode, xc_dtype dtype, xc_algo a, const void* d_left, xc_size2 left, uint32_t n_left,
+                   const void* d_right, xc_size2 right, uint32_t n_right, void* d_out, void* d_workspace,
+                   size_t workspace_bytes, cudaStream_t stream) {
+  if (!tile_valid(a)) return fail(XC_ERR_INVALID_ARGUMENT, "invalid tile for the method");
+  PairMap pm;
+  uint64_t n_out;
+  make_pair_map(mode, n_left, n_right, &pm, &n_out);
+  const Geometry g = make_geometry(left, right);
+  switch (a.method) {
+    case XC_METHOD_DIRECT:
+      return direct_launch(dtype, d_left, d_right, d_out, g, pm, stream, -1, DirectAccumulate::kAuto, a.tile);
+    case XC_METHOD_FFT: {
+      FftPlanImpl* plan = nullptr;
+      XC_TRY(cached_plan(mode, dtype, left, n_left, right, n_right, &plan));
+      return fft_plan_execute(plan, d_left, d_right, d_out, 1, d_workspace, workspace_bytes, stream);
+    }
+    case XC_METHOD_TC_BF16X3:
+    case XC_METHOD_TC_TF32X3:
+      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split tensor-core paths are FP32 only");
+      return tc_correlate((const float*)d_left, (const float*)d_right, (float*)d_out, g, pm, d_workspace,
+                          workspace_bytes, stream, a.method == XC_METHOD_TC_TF32X3, a.tile == 0 ? 64 : a.tile);
+    default: return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
+  }
 }
 
 }  // namespace
@@ -359,14 +422,28 @@ xc_status xc_workspace_size(xc_mode mode, xc_dtype dtype, xc_method method, xc_s
   PairMap pm;
   uint64_t n_out;
   if (!make_pair_map(mode, n_left, n_right, &pm, &n_out)) return fail(XC_ERR_INVALID_ARGUMENT, "invalid counts");
-  if (method == XC_METHOD_AUTO) method = select_method(mode, dtype, left, n_left, right, n_right);
+  if (method == XC_METHOD_AUTO) {
+    xc_algo a;
+    if (select_algorithm(mode, dtype, left, n_left, right, n_right, &a)) {
+      *bytes = algo_workspace(mode, dtype, a, left, n_left, right, n_right, pm);
+    } else {
+      // undecided (the first call autotunes): enough for any candidate
+      *bytes = 0;
+      for (const xc_algo& c : kAlgos)
+        if (method_supported(c.method, dtype, left, right))
+          *bytes = std::max(*bytes, algo_workspace(mode, dtype, c, left, n_left, right, n_right, pm));
+    }
+    return XC_OK;
+  }
   switch (method) {
-    case XC_METHOD_DIRECT: *bytes = 0; return XC_OK;
-    case XC_METHOD_FFT: *bytes = fft_workspace_bytes(mode, dtype, left, n_left, right, n_right); return XC_OK;
+    case XC_METHOD_DIRECT:
+    case XC_METHOD_FFT:
+      *bytes = algo_workspace(mode, dtype, xc_algo{method, 0}, left, n_left, right, n_right, pm);
+      return XC_OK;
     case XC_METHOD_TC_BF16X3:
     case XC_METHOD_TC_TF32X3:
       if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split tensor-core paths are FP32 only");
-      *bytes = tc_workspace_size(make_geometry(left, right), pm, method == XC_METHOD_TC_TF32X3);
+      *bytes = algo_workspace(mode, dtype, xc_algo{method, 0}, left, n_left, right, n_right, pm);
       return XC_OK;
     default: return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
   }
@@ -383,22 +460,37 @@ xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const voi
   uint64_t n_out;
   if (!make_pair_map(mode, n_left, n_right, &pm, &n_out))
     return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts for the mode");
-  const Geometry g = make_geometry(left, right);
-  if (method == XC_METHOD_AUTO) method = select_method(mode, dtype, left, n_left, right, n_right);
-  switch (method) {
-    case XC_METHOD_DIRECT: return direct_launch(dtype, d_left, d_right, d_out, g, pm, as_stream(stream), -1);
-    case XC_METHOD_FFT: {
-      FftPlanImpl* plan = nullptr;
-      XC_TRY(cached_plan(mode, dtype, left, n_left, right, n_right, &plan));
-      return fft_plan_execute(plan, d_left, d_right, d_out, 1, d_workspace, workspace_bytes, as_stream(stream));
-    }
-    case XC_METHOD_TC_BF16X3:
-    case XC_METHOD_TC_TF32X3:
-      if (dtype != XC_F32) return fail(XC_ERR_UNSUPPORTED, "the split tensor-core paths are FP32 only");
-      return tc_correlate((const float*)d_left, (const float*)d_right, (float*)d_out, g, pm, d_workspace,
-                          workspace_bytes, as_stream(stream), method == XC_METHOD_TC_TF32X3);
-    default: return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
+  xc_algo a{method, 0};
+  if (method == XC_METHOD_AUTO && !select_algorithm(mode, dtype, left, n_left, right, n_right, &a)) {
+    // no network and no record for this problem: the exhaustive autotune on
+    // these buffers decides (and is remembered)
+    double ms = 0.0;
+    XC_TRY(xc_autotune_algorithm(mode, dtype, d_left, left, n_left, d_right, right, n_right, d_out, stream, &a, &ms));
   }
+  if (a.method != XC_METHOD_DIRECT && a.method != XC_METHOD_FFT && a.method != XC_METHOD_TC_BF16X3 &&
+      a.method != XC_METHOD_TC_TF32X3)
+    return fail(XC_ERR_INVALID_ARGUMENT, "unknown method");
+  return run_algo(mode, dtype, a, d_left, left, n_left, d_right, right, n_right, d_out, d_workspace,
+                  workspace_bytes, as_stream(stream));
+}
+
+xc_status xc_correlate_algo(xc_mode mode, xc_dtype dtype, xc_algo algo, const void* d_left, xc_size2 left,
+                            uint32_t n_left, const void* d_right, xc_size2 right, uint32_t n_right, void* d_out,
+                            void* d_workspace, size_t workspace_bytes, void* stream) {
+  if (d_left == nullptr || d_right == nullptr || d_out == nullptr)
+    return fail(XC_ERR_INVALID_ARGUMENT, "NULL device buffer");
+  if (dtype != XC_F32 && dtype != XC_F64) return fail(XC_ERR_INVALID_ARGUMENT, "unknown dtype");
+  XC_TRY(check_sizes(left, right));
+  PairMap pm;
+  uint64_t n_out;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out))
+    return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts for the mode");
+  if (algo.method == XC_METHOD_AUTO) return xc_correlate(mode, dtype, XC_METHOD_AUTO, d_left, left, n_left, d_right,
+                                                         right, n_right, d_out, d_workspace, workspace_bytes, stream);
+  if (!method_supported(algo.method, dtype, left, right))
+    return fail(XC_ERR_UNSUPPORTED, "the method does not support this problem");
+  return run_algo(mode, dtype, algo, d_left, left, n_left, d_right, right, n_right, d_out, d_workspace,
+                  workspace_bytes, as_stream(stream));
 }
 
 xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
@@ -436,8 +528,10 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
   // 16 MiB of output (measured on 64 outputs of 511x511: 1, 2, 4 and 8 bands
   // took 1.91, 1.84, 1.88 and 1.78 ms).  XC_HOST_BANDS fixes the count (1
   // turns it off).
-  const xc_method resolved =
-      method == XC_METHOD_AUTO ? select_method(mode, dtype, left, n_left, right, n_right) : method;
+  xc_algo sel{method, 0};
+  if (method == XC_METHOD_AUTO && !select_algorithm(mode, dtype, left, n_left, right, n_right, &sel))
+    sel = xc_algo{XC_METHOD_AUTO, 0};  // the first chunk's call autotunes
+  const xc_method resolved = sel.method;
   int n_bands = ob >= ((size_t)16 << 20) ? 8 : 1;
   if (const char* e = std::getenv("XC_HOST_BANDS")) n_bands = std::max(1, std::atoi(e));
   const bool banded = (resolved == XC_METHOD_TC_BF16X3 || resolved == XC_METHOD_TC_TF32X3) && dtype == XC_F32 &&
@@ -643,62 +737,112 @@ xc_status xc_selector_load_builtin(void) {
 #endif
 }
 
-xc_status xc_select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
-                           uint32_t n_right, xc_method* method) {
-  if (method == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "method is NULL");
+xc_status xc_algorithm(uint32_t index, xc_algo* algo) {
+  if (algo == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "algo is NULL");
+  if (index >= XC_N_ALGOS) return fail(XC_ERR_INVALID_ARGUMENT, "candidate index out of range");
+  *algo = kAlgos[index];
+  return XC_OK;
+}
+
+xc_status xc_select_algorithm(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                              uint32_t n_right, xc_algo* algo) {
+  if (algo == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "algo is NULL");
   XC_TRY(check_sizes(left, right));
   uint64_t n_out = 0;
   XC_TRY(xc_output_count(mode, n_left, n_right, &n_out));
-  *method = select_method(mode, dtype, left, n_left, right, n_right);
+  if (!select_algorithm(mode, dtype, left, n_left, right, n_right, algo)) *algo = xc_algo{XC_METHOD_AUTO, 0};
+  return XC_OK;
+}
+
+xc_status xc_select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                           uint32_t n_right, xc_method* method) {
+  if (method == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "method is NULL");
+  xc_algo a;
+  XC_TRY(xc_select_algorithm(mode, dtype, left, n_left, right, n_right, &a));
+  *method = a.method;
+  return XC_OK;
+}
+
+xc_status xc_time_algorithm(xc_mode mode, xc_dtype dtype, xc_algo algo, const void* d_left, xc_size2 left,
+                            uint32_t n_left, const void* d_right, xc_size2 right, uint32_t n_right, void* d_out,
+                            void* d_workspace, size_t workspace_bytes, uint32_t reps, void* stream, double* ms) {
+  if (ms == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "ms is NULL");
+  if (reps == 0) return fail(XC_ERR_INVALID_ARGUMENT, "reps must be positive");
+  if (algo.method == XC_METHOD_AUTO) return fail(XC_ERR_INVALID_ARGUMENT, "time a concrete algorithm");
+  cudaStream_t s = as_stream(stream);
+  // the warm-up call also creates plans and checks the arguments
+  XC_TRY(xc_correlate_algo(mode, dtype, algo, d_left, left, n_left, d_right, right, n_right, d_out, d_workspace,
+                           workspace_bytes, stream));
+  cudaEvent_t e0, e1;
+  XC_CUDA_TRY(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(XC_ERR_CUDA, "cudaEventCreate failed");
+  }
+  xc_status st = XC_OK;
+  float t = 0.f;
+  if (cudaEventRecord(e0, s) != cudaSuccess) st = fail(XC_ERR_CUDA, "cudaEventRecord failed");
+  for (uint32_t r = 0; r < reps && st == XC_OK; ++r)
+    st = run_algo(mode, dtype, algo, d_left, left, n_left, d_right, right, n_right, d_out, d_workspace,
+                  workspace_bytes, s);
+  if (st == XC_OK && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                      cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+    st = fail(XC_ERR_CUDA, "event timing failed");
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  XC_TRY(st);
+  *ms = t / reps;
+  return XC_OK;
+}
+
+xc_status xc_autotune_algorithm(xc_mode mode, xc_dtype dtype, const void* d_left, xc_size2 left, uint32_t n_left,
+                                const void* d_right, xc_size2 right, uint32_t n_right, void* d_out, void* stream,
+                                xc_algo* best, double* best_ms) {
+  if (best == nullptr || best_ms == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL result pointer");
+  XC_TRY(check_sizes(left, right));
+  PairMap pm;
+  uint64_t n_out;
+  if (!make_pair_map(mode, n_left, n_right, &pm, &n_out))
+    return fail(XC_ERR_INVALID_ARGUMENT, "invalid matrix counts for the mode");
+  double bms = 1e300;
+  xc_algo ba{XC_METHOD_DIRECT, 0};
+  xc_status st = XC_OK;
+  for (const xc_algo& c : kAlgos) {
+    if (!method_supported(c.method, dtype, left, right)) continue;
+    const size_t wb = algo_workspace(mode, dtype, c, left, n_left, right, n_right, pm);
+    void* ws = nullptr;
+    if (wb > 0 && cudaMalloc(&ws, wb) != cudaSuccess) {
+      st = fail(XC_ERR_CUDA, "workspace allocation failed");
+      break;
+    }
+    double ms = 0.0;
+    st = xc_time_algorithm(mode, dtype, c, d_left, left, n_left, d_right, right, n_right, d_out, ws, wb, 3, stream,
+                           &ms);
+    cudaFree(ws);
+    if (st != XC_OK) break;
+    if (ms < bms) {
+      bms = ms;
+      ba = c;
+    }
+  }
+  XC_TRY(st);
+  {
+    std::lock_guard<std::mutex> lock(g_sel_mutex);
+    g_tuned[SelKey{(int)mode, (int)dtype, left.x, left.y, n_left, right.x, right.y, n_right}] = ba;
+  }
+  *best = ba;
+  *best_ms = bms;
   return XC_OK;
 }
 
 xc_status xc_autotune_method(xc_mode mode, xc_dtype dtype, const void* d_left, xc_size2 left, uint32_t n_left,
                              const void* d_right, xc_size2 right, uint32_t n_right, void* d_out, void* stream,
                              xc_method* best, double* best_ms) {
-  if (best == nullptr || best_ms == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL result pointer");
-  cudaStream_t s = as_stream(stream);
-  const xc_method cands[3] = {XC_METHOD_DIRECT, XC_METHOD_FFT, XC_METHOD_TC_BF16X3};
-  cudaEvent_t e0, e1;
-  XC_CUDA_TRY(cudaEventCreate(&e0));
-  XC_CUDA_TRY(cudaEventCreate(&e1));
-  double bms = 1e300;
-  xc_method bm = XC_METHOD_DIRECT;
-  xc_status st = XC_OK;
-  for (xc_method m : cands) {
-    if (!method_supported(m, dtype, left, right)) continue;
-    size_t wb = 0;
-    if ((st = xc_workspace_size(mode, dtype, m, left, n_left, right, n_right, &wb)) != XC_OK) break;
-    void* ws = nullptr;
-    if (wb > 0 && cudaMalloc(&ws, wb) != cudaSuccess) {
-      st = fail(XC_ERR_CUDA, "workspace allocation failed");
-      break;
-    }
-    float ms = 0.f;
-    st = xc_correlate(mode, dtype, m, d_left, left, n_left, d_right, right, n_right, d_out, ws, wb, stream);
-    if (st == XC_OK && cudaEventRecord(e0, s) == cudaSuccess) {
-      for (int r = 0; r < 3 && st == XC_OK; ++r)
-        st = xc_correlate(mode, dtype, m, d_left, left, n_left, d_right, right, n_right, d_out, ws, wb, stream);
-      cudaEventRecord(e1, s);
-      cudaEventSynchronize(e1);
-      cudaEventElapsedTime(&ms, e0, e1);
-    }
-    cudaFree(ws);
-    if (st != XC_OK) break;
-    if (ms / 3.0 < bms) {
-      bms = ms / 3.0;
-      bm = m;
-    }
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  XC_TRY(st);
-  {
-    std::lock_guard<std::mutex> lock(g_sel_mutex);
-    g_tuned[SelKey{(int)mode, (int)dtype, left.x, left.y, n_left, right.x, right.y, n_right}] = bm;
-  }
-  *best = bm;
-  *best_ms = bms;
+  if (best == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL result pointer");
+  xc_algo a;
+  XC_TRY(xc_autotune_algorithm(mode, dtype, d_left, left, n_left, d_right, right, n_right, d_out, stream, &a,
+                               best_ms));
+  *best = a.method;
   return XC_OK;
 }
 

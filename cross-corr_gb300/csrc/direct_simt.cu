@@ -655,19 +655,26 @@ RaggedShape shape_of() {
 }  // namespace
 
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
-                        const PairMap& pm, cudaStream_t stream, int force_loader, DirectAccumulate acc) {
+                        const PairMap& pm, cudaStream_t stream, int force_loader, DirectAccumulate acc, int tile) {
+  // tile 0: 8 partners per CTA when there are 4 or more (3 for FP64), else
+  // one; 1: 8 (FP64: 4) partners, 32 x 64 shifts; 2: one partner, 64 x 64
+  // shifts (FP64: 32 x 64); 3: one partner, 32 x 64 shifts
+  if (tile < 0 || tile > 3) return fail(XC_ERR_INVALID_ARGUMENT, "plain kernel tiles are 0-3");
   if (dtype == XC_F32) {
-    if (pm.K >= 4)
-      return launch_uniform<CfgF32Multi>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
-                                         force_loader, acc);
-    return launch_uniform<CfgF32Single>((const float*)left, (const float*)right, (float*)out, g, pm, stream,
-                                        force_loader, acc);
+    const int t = tile != 0 ? tile : (pm.K >= 4 ? 1 : 2);
+    const float* l = (const float*)left;
+    const float* r = (const float*)right;
+    float* o = (float*)out;
+    if (t == 1) return launch_uniform<CfgF32Multi>(l, r, o, g, pm, stream, force_loader, acc);
+    if (t == 2) return launch_uniform<CfgF32Single>(l, r, o, g, pm, stream, force_loader, acc);
+    return launch_uniform<CfgF32Small>(l, r, o, g, pm, stream, force_loader, acc);
   }
-  if (pm.K >= 3)
-    return launch_uniform<CfgF64Multi>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
-                                       force_loader, acc);
-  return launch_uniform<CfgF64Single>((const double*)left, (const double*)right, (double*)out, g, pm, stream,
-                                      force_loader, acc);
+  const int t = tile != 0 ? tile : (pm.K >= 3 ? 1 : 2);
+  const double* l = (const double*)left;
+  const double* r = (const double*)right;
+  double* o = (double*)out;
+  if (t == 1) return launch_uniform<CfgF64Multi>(l, r, o, g, pm, stream, force_loader, acc);
+  return launch_uniform<CfgF64Single>(l, r, o, g, pm, stream, force_loader, acc);
 }
 
 // Tile shapes a ragged plan may pick from (the autotuner's candidates).

@@ -54,55 +54,85 @@ constexpr int kGlueRows = 8;  // rows per block in the row-walking glue kernels
 // block.  Each row is written as a scalar head up to its first 16-byte
 // boundary (rows of the in-place R2C layout, pitch 2 (px/2 + 1), start only
 // 8-byte aligned every other row), a body of 16-byte stores and a scalar
-// tail; rows outside the source are zeros and read nothing.
+// tail; rows outside the source are zeros and read nothing.  A thread loads
+// its 16-byte chunk of every one of the block's rows before it stores any,
+// so up to kGlueRows loads per thread are in flight; a chunk whose source is
+// 8-byte but not 16-byte aligned (the odd rows' bodies) is read as two
+// 8-byte loads.
 template <typename T>
 __device__ __forceinline__ T pad_value(const T* srow, bool row_in, int sx, int cols) {
   return (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
+}
+
+template <typename T, typename Vec>
+__device__ __forceinline__ Vec pad_chunk(const T* srow, bool row_in, int sx0, int cols) {
+  constexpr int V = 16 / (int)sizeof(T);
+  T v[V];
+  if (!row_in || sx0 >= cols || sx0 + V <= 0) {
+#pragma unroll
+    for (int e = 0; e < V; ++e) v[e] = T(0);
+  } else if (sx0 >= 0 && sx0 + V <= cols && (((uintptr_t)(srow + sx0)) & 15) == 0) {
+    const Vec f = __ldg(reinterpret_cast<const Vec*>(srow + sx0));
+    memcpy(v, &f, sizeof(f));
+  } else if (sizeof(T) == 4 && sx0 >= 0 && sx0 + V <= cols && (((uintptr_t)(srow + sx0)) & 7) == 0) {
+    const float2 a = __ldg(reinterpret_cast<const float2*>(srow + sx0));
+    const float2 b = __ldg(reinterpret_cast<const float2*>(srow + sx0 + 2));
+    memcpy(v, &a, 8);
+    memcpy(reinterpret_cast<char*>(v) + 8, &b, 8);
+  } else {
+#pragma unroll
+    for (int e = 0; e < V; ++e) v[e] = pad_value(srow, true, sx0 + e, cols);
+  }
+  Vec o;
+  memcpy(&o, v, sizeof(o));
+  return o;
 }
 
 template <typename T>
 __global__ void pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int rows, int cols, int count, int pad_rows,
                            int pad_cols, int dst_pitch, int dst_y, int dst_x, int rows_per_block) {
   constexpr int V = 16 / (int)sizeof(T);  // elements per 16-byte store
+  constexpr int R = kGlueRows;
   using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
   const long long n_rows = (long long)count * pad_rows;
   const long long r0 = (long long)blockIdx.x * rows_per_block;
+  const int nr = (int)min((long long)min(rows_per_block, R), n_rows - r0);
   long long m = r0 / pad_rows;
   int y = (int)(r0 - m * pad_rows);
-  for (int i = 0; i < rows_per_block && r0 + i < n_rows; ++i) {
+  const T* srow[R];
+  T* drow[R];
+  bool row_in[R];
+  int lead[R], n_body[R];
+  int nb_max = 0;
+#pragma unroll
+  for (int i = 0; i < R; ++i) {
     const int sy = y - dst_y;
-    const bool row_in = sy >= 0 && sy < rows;
-    const T* srow = src + (m * rows + (row_in ? sy : 0)) * (long long)cols;
-    T* drow = dst + (r0 + i) * (long long)dst_pitch;
-    const int lead = min(pad_cols, (int)(((16u - ((uint32_t)(uintptr_t)drow & 15u)) & 15u) / sizeof(T)));
-    const int n_body = (pad_cols - lead) / V;
-    const int tail0 = lead + n_body * V;
-    if ((int)threadIdx.x < lead) drow[threadIdx.x] = pad_value(srow, row_in, (int)threadIdx.x - dst_x, cols);
-    if ((int)threadIdx.x < pad_cols - tail0)
-      drow[tail0 + threadIdx.x] = pad_value(srow, row_in, tail0 + (int)threadIdx.x - dst_x, cols);
-    Vec* body = reinterpret_cast<Vec*>(drow + lead);
-    for (int k = threadIdx.x; k < n_body; k += blockDim.x) {
-      const int x0 = lead + k * V;
-      const int sx0 = x0 - dst_x;
-      T v[V];
-      if (!row_in || sx0 >= cols || sx0 + V <= 0) {
-#pragma unroll
-        for (int e = 0; e < V; ++e) v[e] = T(0);
-      } else if (sx0 >= 0 && sx0 + V <= cols && (((uintptr_t)(srow + sx0)) & 15) == 0) {
-        const Vec f = __ldg(reinterpret_cast<const Vec*>(srow + sx0));
-        memcpy(v, &f, sizeof(f));
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e) v[e] = pad_value(srow, true, sx0 + e, cols);
-      }
-      Vec o;
-      memcpy(&o, v, sizeof(o));
-      body[k] = o;
+    row_in[i] = i < nr && sy >= 0 && sy < rows;
+    srow[i] = src + (m * rows + (row_in[i] ? sy : 0)) * (long long)cols;
+    drow[i] = dst + (r0 + min(i, nr - 1)) * (long long)dst_pitch;
+    lead[i] = min(pad_cols, (int)(((16u - ((uint32_t)(uintptr_t)drow[i] & 15u)) & 15u) / sizeof(T)));
+    n_body[i] = i < nr ? (pad_cols - lead[i]) / V : 0;
+    nb_max = max(nb_max, n_body[i]);
+    if (i < nr) {
+      const int tail0 = lead[i] + n_body[i] * V;
+      if ((int)threadIdx.x < lead[i])
+        drow[i][threadIdx.x] = pad_value(srow[i], row_in[i], (int)threadIdx.x - dst_x, cols);
+      if ((int)threadIdx.x < pad_cols - tail0)
+        drow[i][tail0 + threadIdx.x] = pad_value(srow[i], row_in[i], tail0 + (int)threadIdx.x - dst_x, cols);
     }
     if (++y == pad_rows) {
       y = 0;
       ++m;
     }
+  }
+  for (int k = threadIdx.x; k < nb_max; k += blockDim.x) {
+    Vec v[R];
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+      if (k < n_body[i]) v[i] = pad_chunk<T, Vec>(srow[i], row_in[i], lead[i] + k * V - dst_x, cols);
+#pragma unroll
+    for (int i = 0; i < R; ++i)
+      if (k < n_body[i]) reinterpret_cast<Vec*>(drow[i] + lead[i])[k] = v[i];
   }
 }
 

@@ -1,15 +1,16 @@
 // mlp.cu -- the method selector's network: a 3-layer, 64-wide FP32 MLP
-//   x (8 features) -> Linear 8x64 -> ReLU -> Linear 64x64 -> ReLU -> Linear 64x3
-// that predicts the (standardised) log run time of each correlation method,
+//   x (8 features) -> Linear 8x64 -> ReLU -> Linear 64x64 -> ReLU -> Linear 64x7
+// that predicts the (standardised) log run time of each candidate algorithm
+// (method and tile, xc_algorithm),
 // with hand-written inference, gradient and Adam kernels.  New in this
 // library: the reference picks algorithms by hand (its YAML sweeps,
 // benchmarking/args_test/*.yml).
 //
 // Parameter layout (XC_MLP_PARAMS floats):
-//   W1[64][8], b1[64], W2[64][64], b2[64], W3[3][64], b3[3]
+//   W1[64][8], b1[64], W2[64][64], b2[64], W3[7][64], b3[7]
 // The forward kernel runs one 64-thread block per sample; the gradient kernel
 // recomputes the activations per sample and accumulates the mean-squared
-// error gradients (masked: unavailable methods carry mask 0) with atomics.
+// error gradients (masked: unavailable candidates carry mask 0) with atomics.
 #include "xc_common.cuh"
 #include "xc_internal.h"
 

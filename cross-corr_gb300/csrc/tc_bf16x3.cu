@@ -1315,7 +1315,7 @@ struct TcPlan {
 int chunk_rows_fixed();
 int sm_count();
 
-bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool banded = false) {
+bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool banded = false, int max_rows = 64) {
   // the mean-correction kernel stages 8 output rows' table differences
   if ((size_t)8 * corr_stage(g.Wl, g.Wr) * sizeof(float) > 200 * 1024) return false;
   int P = 1;
@@ -1343,7 +1343,7 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool ba
   const long long rows_all = span * per_tile_key;
   const long long fair = rows_all / (2LL * sm_count());
   const int chunk32 = chunk_rows_fixed() > 0 ? chunk_rows_fixed() : (int)std::max(4LL, std::min(32LL, fair));
-  t->chunk_rows = chunk_rows_fixed() > 0 || banded ? chunk32 : (int)std::max(4LL, std::min(64LL, fair));
+  t->chunk_rows = chunk_rows_fixed() > 0 || banded ? chunk32 : (int)std::max(4LL, std::min((long long)max_rows, fair));
   t->n_chunks = (int)div_up(span, (long long)t->chunk_rows);
   t->n_items = (long long)t->n_chunks * per_tile_key;
   t->n_items_ws = std::max(t->n_items, div_up(span, (long long)chunk32) * per_tile_key);
@@ -1506,9 +1506,9 @@ size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32) {
 
 xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
                               const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
-                              int want_bands, int* band_done, TcBands* bands) {
+                              int want_bands, int* band_done, TcBands* bands, int max_rows) {
   TcPlan t;
-  if (!tc_plan(g, pm, tf32, &t, band_done != nullptr))
+  if (!tc_plan(g, pm, tf32, &t, band_done != nullptr, max_rows))
     return fail(XC_ERR_UNSUPPORTED,
                 "split tensor-core paths need Wl + Wr below 6400");
   const size_t need = ws_layout(nullptr, g, pm, t).bytes;
@@ -1673,8 +1673,9 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
 }
 
 xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32) {
-  return tc_correlate_banded(left, right, out, g, pm, workspace, ws_bytes, stream, tf32, 1, nullptr, nullptr);
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows) {
+  return tc_correlate_banded(left, right, out, g, pm, workspace, ws_bytes, stream, tf32, 1, nullptr, nullptr,
+                             max_rows);
 }
 
 // ---------------------------------------------------------------------------
@@ -1745,5 +1746,5 @@ extern "C" xc_status xc_correlate_tc_noalloc(xc_mode mode, const float* d_left, 
   void* scratch = nullptr;
   XC_TRY(noalloc_scratch(&scratch));
   return tc_correlate(d_left, d_right, d_out, g, pm, scratch, (size_t)XC_TC_NOALLOC_SCRATCH_BYTES,
-                      reinterpret_cast<cudaStream_t>(stream), false);
+                      reinterpret_cast<cudaStream_t>(stream), false, 64);
 }

@@ -60,7 +60,7 @@ xc_status kernel_timing_read(double* total_ms, uint32_t* launches);
 enum class DirectAccumulate { kAuto = 0, kCaller = 1, kNever = 2 };
 xc_status direct_launch(xc_dtype dtype, const void* left, const void* right, void* out, const Geometry& g,
                         const PairMap& pm, cudaStream_t stream, int force_loader /* -1 auto, 0 cp.async, 1 TMA */,
-                        DirectAccumulate acc = DirectAccumulate::kAuto);
+                        DirectAccumulate acc = DirectAccumulate::kAuto, int tile = 0);
 
 // Ragged batches (ragged.cu drives direct_simt.cu's persistent mode).
 struct RaggedTile {     // one tile of shifts of one pair
@@ -152,6 +152,6 @@ struct TcBands {
 };
 xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
                               const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
-                              int want_bands, int* band_done, TcBands* bands);
+                              int want_bands, int* band_done, TcBands* bands, int max_rows = 64);
 
 }  // namespace xc

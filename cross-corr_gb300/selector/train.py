@@ -1,5 +1,8 @@
-"""Train the method selector on a measured timing dataset and report its
-regret against the exhaustive autotune on the held-out workloads.
+"""Train the algorithm selector on a measured timing dataset and report its
+regret against the exhaustive autotune (over the same candidates: method and
+tile) on the held-out workloads, beside what selection without the network
+costs: the best fixed candidate, and the exhaustive autotune that
+XC_METHOD_AUTO runs on a problem's first call when no network is installed.
 
 Usage: python train.py TIMINGS.npz WEIGHTS.npz [--inc selector_weights.inc]
                        [--steps 3000] [--seed 0]
@@ -21,13 +24,39 @@ sys.path.insert(0, os.path.dirname(HERE))
 from xcorr import selector  # noqa: E402
 
 
-def baselines(times, M, X):
-    """Selectors without the network, for comparison."""
+FFT = selector.ALGO_NAMES.index("fft")  # supported by every problem
+
+
+def baselines(times, M):
+    """Fixed choices without the network (the FFT path where the fixed
+    candidate does not support a problem), for comparison."""
     out = {}
-    for k, name in enumerate(selector.METHOD_NAMES):
-        chosen = np.where(M[:, k] > 0, k, 0)  # fall back to direct where unsupported
+    for k, name in enumerate(selector.ALGO_NAMES):
+        chosen = np.where(M[:, k] > 0, k, FFT)
         out[f"always_{name}"] = selector.regret(times, chosen)
     return out
+
+
+def default_tiles(timings_path):
+    """Per workload, the candidate index each method runs with its default
+    tile (tile 0): the plain kernel takes 8 partners per CTA (direct:1) when
+    a left matrix has 4 or more partners, else one (direct:2); the split-BF16
+    path takes items of 64 rows."""
+    z = np.load(timings_path)
+    idx = np.zeros((len(z["modes"]), 4), dtype=np.int64)
+    for j, (m, b) in enumerate(zip(z["modes"], z["batch"])):
+        n_l, n_r = selector.counts(str(m), int(b))
+        partners = {"one_to_one": 1, "one_to_many": n_r, "n_to_mn": n_r // max(1, n_l), "n_to_m": n_r}[str(m)]
+        idx[j] = [selector.ALGO_NAMES.index("direct:1" if partners >= 4 else "direct:2"),
+                  selector.ALGO_NAMES.index("fft"), selector.ALGO_NAMES.index("tc_bf16x3:64"),
+                  selector.ALGO_NAMES.index("tc_tf32x3")]
+    return idx
+
+
+def autotune_cost(times, M):
+    """Total time of the exhaustive autotune's first call per problem: every
+    supported candidate timed once, then the best run."""
+    return float((np.where(M > 0, times, 0).sum(axis=1) + times.min(axis=1)).sum())
 
 
 def write_inc(path, params, source, steps, seed):
@@ -56,15 +85,29 @@ def main():
     params = trainer.params()
     pred = selector.predict(params, X[te])
     chosen = selector.choose(pred, M[te])
-    res = {"train_loss": hist, "heldout_regret_total": selector.regret(times[te], chosen)[0],
-           "heldout_regret_mean": selector.regret(times[te], chosen)[1],
-           "heldout_pick_accuracy": float(np.mean(chosen == times[te].argmin(axis=1))),
-           "baselines_heldout": {k: v[0] for k, v in baselines(times[te], M[te], X[te]).items()},
-           "exhaustive_autotune_cost_over_best": float(
-               (np.where(M[te] > 0, times[te], 0).sum(axis=1) + times[te].min(axis=1)).sum()
-               / times[te].min(axis=1).sum()),
-           "fft_2048x2048x16_choice": selector.METHOD_NAMES[int(chosen[-1])],
+    t = times[te]
+    best = t.min(axis=1).sum()
+    ours = t[np.arange(len(te)), chosen].sum()
+    fixed = baselines(t, M[te])
+    res = {"train_loss": hist, "heldout_regret_total": selector.regret(t, chosen)[0],
+           "heldout_regret_mean": selector.regret(t, chosen)[1],
+           "heldout_pick_accuracy": float(np.mean(chosen == t.argmin(axis=1))),
+           "baselines_heldout": {k: v[0] for k, v in fixed.items()},
+           "best_fixed": min(fixed, key=lambda k: fixed[k][0]),
+           "network_over_best_fixed": float(ours / ((1 + min(v[0] for v in fixed.values())) * best)),
+           "exhaustive_autotune_cost_over_best": autotune_cost(t, M[te]) / best,
+           "fft_2048x2048x16_choice": selector.ALGO_NAMES[int(chosen[-1])],
            "n_train": int(len(tr)), "n_heldout": int(len(te))}
+    # selection by method alone: the measured fastest method, each with its
+    # default tile (what choosing the tile adds)
+    dflt = default_tiles(args.timings)[te]
+    by_method = dflt[np.arange(len(te)), np.argmin(np.take_along_axis(t, dflt, axis=1), axis=1)]
+    z = np.load(args.timings)
+    est = z["estimated"][te] if "estimated" in z else np.zeros_like(t, dtype=bool)
+    res["method_only_oracle_regret_total"] = selector.regret(t, by_method)[0]
+    res["fastest_candidate_counts_heldout"] = {n: int(np.sum(t.argmin(axis=1) == k))
+                                               for k, n in enumerate(selector.ALGO_NAMES)}
+    res["estimated_entries_heldout"] = int(est.sum())
     np.savez(args.weights, params=params, t_mean=mu, t_std=sd, steps=args.steps, seed=args.seed)
     if args.inc:
         write_inc(args.inc, params, os.path.basename(args.timings), args.steps, args.seed)

@@ -60,6 +60,7 @@ EXPORTED = [
     "xc_ragged_plan_create", "xc_ragged_autotune", "xc_ragged_execute", "xc_ragged_plan_destroy",
     "xc_correlate_pairs", "xc_selector_features", "xc_mlp_forward", "xc_mlp_gradient", "xc_mlp_adam_step",
     "xc_selector_load", "xc_selector_load_builtin", "xc_select_method", "xc_autotune_method",
+    "xc_algorithm", "xc_select_algorithm", "xc_correlate_algo", "xc_time_algorithm", "xc_autotune_algorithm",
 ]
 
 
@@ -75,6 +76,11 @@ class XcError(RuntimeError):
 
 class Size2(ctypes.Structure):
     _fields_ = [("x", ctypes.c_uint32), ("y", ctypes.c_uint32)]
+
+
+class Algo(ctypes.Structure):
+    """xc_algo: a method and one of its tile configurations."""
+    _fields_ = [("method", ctypes.c_int), ("tile", ctypes.c_int32)]
 
 
 class MatrixDesc(ctypes.Structure):
@@ -141,6 +147,12 @@ def lib():
         L.xc_selector_load.argtypes = [vp]
         L.xc_select_method.argtypes = [i, i, Size2, u32, Size2, u32, P(i)]
         L.xc_autotune_method.argtypes = [i, i, vp, Size2, u32, vp, Size2, u32, vp, vp, P(i), P(c.c_double)]
+        L.xc_algorithm.argtypes = [u32, P(Algo)]
+        L.xc_select_algorithm.argtypes = [i, i, Size2, u32, Size2, u32, P(Algo)]
+        L.xc_correlate_algo.argtypes = [i, i, Algo, vp, Size2, u32, vp, Size2, u32, vp, vp, sz, vp]
+        L.xc_time_algorithm.argtypes = [i, i, Algo, vp, Size2, u32, vp, Size2, u32, vp, vp, sz, u32, vp,
+                                        P(c.c_double)]
+        L.xc_autotune_algorithm.argtypes = [i, i, vp, Size2, u32, vp, Size2, u32, vp, vp, P(Algo), P(c.c_double)]
         for t in ("f32", "f64"):
             getattr(L, f"xc_run_ccn_shuffle_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, vp]
             getattr(L, f"xc_run_ccn_shuffle_multimat_right_{t}").argtypes = [vp, vp, vp, Size2, Size2, u32, u32, u32,
@@ -199,6 +211,7 @@ def _stream_ptr(stream) -> Optional[int]:
 def correlate(mode: str, left, right, method: str = "direct", out=None, workspace=None, stream=None):
     """Correlate CUDA tensors ``left`` (n,Hl,Wl) and ``right`` (m,Hr,Wr) on the device.
 
+    ``method`` is a method name or ``"method:tile"`` (xc_correlate_algo).
     Returns the (n_out, Hl+Hr-1, Wl+Wr-1) output tensor.  ``workspace`` (a uint8
     CUDA tensor) is allocated when not given and the method needs one.
     """
@@ -218,13 +231,19 @@ def correlate(mode: str, left, right, method: str = "direct", out=None, workspac
     n_out = output_count(mode, n, m)
     if out is None:
         out = torch.empty((n_out, hl + hr - 1, wl + wr - 1), dtype=left.dtype, device=left.device)
-    ws_bytes = workspace_size(mode, dtype, method, (hl, wl), n, (hr, wr), m)
+    base, _, tile = method.partition(":")
+    ws_bytes = workspace_size(mode, dtype, base, (hl, wl), n, (hr, wr), m)
     if ws_bytes and (workspace is None or workspace.numel() < ws_bytes):
         workspace = torch.empty(ws_bytes, dtype=torch.uint8, device=left.device)
     wptr = workspace.data_ptr() if (workspace is not None and ws_bytes) else None
-    check(lib().xc_correlate(MODES[mode], DTYPES[dtype], METHODS[method], left.data_ptr(), size2(hl, wl), n,
-                             right.data_ptr(), size2(hr, wr), m, out.data_ptr(), wptr, ws_bytes,
-                             _stream_ptr(stream)))
+    if tile:
+        check(lib().xc_correlate_algo(MODES[mode], DTYPES[dtype], Algo(METHODS[base], int(tile)), left.data_ptr(),
+                                      size2(hl, wl), n, right.data_ptr(), size2(hr, wr), m, out.data_ptr(), wptr,
+                                      ws_bytes, _stream_ptr(stream)))
+    else:
+        check(lib().xc_correlate(MODES[mode], DTYPES[dtype], METHODS[base], left.data_ptr(), size2(hl, wl), n,
+                                 right.data_ptr(), size2(hr, wr), m, out.data_ptr(), wptr, ws_bytes,
+                                 _stream_ptr(stream)))
     return out
 
 
@@ -363,6 +382,30 @@ class RaggedPlan:
         check(lib().xc_correlate_pairs(DTYPES[self.dtype], self.left.data_ptr(), self.ldesc, len(self.ldesc),
                                        self.right.data_ptr(), self.rdesc, len(self.rdesc), self.pdesc,
                                        len(self.pdesc), out.data_ptr(), _stream_ptr(stream)))
+
+    def per_pair_streams(self, out, n_streams=8):
+        """The reference's multi-stream driver (src/n_to_m.hpp:198-212): pair i
+        goes to stream i % n_streams, one plain-kernel launch each; the
+        current stream waits for all of them."""
+        import torch
+
+        if not hasattr(self, "_streams") or len(self._streams) != n_streams:
+            self._streams = [torch.cuda.Stream() for _ in range(n_streams)]
+            self._subsets = []
+            for s in range(n_streams):
+                sub = list(self.pdesc)[s::n_streams]
+                self._subsets.append((PairDesc * len(sub))(*sub))
+        cur = torch.cuda.current_stream()
+        start = torch.cuda.Event()
+        start.record(cur)
+        for st, sub in zip(self._streams, self._subsets):
+            st.wait_event(start)
+            if len(sub):
+                check(lib().xc_correlate_pairs(DTYPES[self.dtype], self.left.data_ptr(), self.ldesc, len(self.ldesc),
+                                               self.right.data_ptr(), self.rdesc, len(self.rdesc), sub, len(sub),
+                                               out.data_ptr(), st.cuda_stream))
+        for st in self._streams:
+            cur.wait_stream(st)
 
     def outputs(self, flat=None):
         flat = self.out if flat is None else flat

@@ -1,12 +1,14 @@
-"""The learned method selector: data, training on the GPU with the library's
-own MLP kernels (xc_mlp_gradient / xc_mlp_adam_step), evaluation against the
-exhaustive autotune, and installation for XC_METHOD_AUTO.
+"""The learned algorithm selector: data, training on the GPU with the
+library's own MLP kernels (xc_mlp_gradient / xc_mlp_adam_step), evaluation
+against the exhaustive autotune, and installation for XC_METHOD_AUTO.
 
-The network predicts the standardised log run time of each method (direct,
-fft, tc_bf16x3) from 8 features (xc_selector_features); the selector picks
-the smallest prediction among the methods a problem supports.  Its regret is
-measured against the exhaustive autotune (the measured fastest method) on
-held-out workloads.
+The network predicts the standardised log run time of each candidate
+algorithm -- a method and one of its tiles (xc_algorithm): the plain kernel's
+three tile shapes, the FFT path, split-BF16 with items of at most 32 or 64
+left rows, split-TF32 -- from 8 features (xc_selector_features); the selector
+picks the smallest prediction among the candidates a problem supports.  Its
+regret is measured against the exhaustive autotune over the same candidates
+(the measured fastest) on held-out workloads.
 """
 from __future__ import annotations
 
@@ -15,10 +17,25 @@ import math
 
 import numpy as np
 
-from . import DTYPES, METHODS, MODES, check, lib, size2
+from . import DTYPES, METHODS, MODES, Algo, check, lib, size2
 
-METHOD_NAMES = ["direct", "fft", "tc_bf16x3"]
-N_PARAMS = 64 * 8 + 64 + 64 * 64 + 64 + 3 * 64 + 3
+# the candidates in the order of the network's outputs (xc_algorithm)
+ALGO_NAMES = ["direct:1", "direct:2", "direct:3", "fft", "tc_bf16x3:32", "tc_bf16x3:64", "tc_tf32x3"]
+N_OUT = len(ALGO_NAMES)
+N_PARAMS = 64 * 8 + 64 + 64 * 64 + 64 + N_OUT * 64 + N_OUT
+
+
+def algo_struct(name):
+    """'method' or 'method:tile' -> xc_algo."""
+    method, _, tile = name.partition(":")
+    return Algo(METHODS[method], int(tile) if tile else 0)
+
+
+def algo_name(a):
+    method = {v: k for k, v in METHODS.items()}[a.method]
+    if method in ("auto", "fft", "tc_tf32x3") or a.tile == 0:
+        return method
+    return f"{method}:{a.tile}"
 
 
 def counts(mode, batch):
@@ -39,7 +56,7 @@ def features(mode, left_shape, n_left, right_shape, n_right):
 
 
 def load_dataset(path):
-    """Features X (n,8), log10 times T (n,3) with inf for unsupported, mask M."""
+    """Features X (n,8), log10 times T (n,7) with inf for unsupported, mask M."""
     z = np.load(path)
     modes = [str(m) for m in z["modes"]]
     rows = []
@@ -64,7 +81,7 @@ def init_params(seed=0):
     """He-normal weights, zero biases."""
     rng = np.random.default_rng(seed)
     parts = []
-    for shape in [(64, 8), (64,), (64, 64), (64,), (3, 64), (3,)]:
+    for shape in [(64, 8), (64,), (64, 64), (64,), (N_OUT, 64), (N_OUT,)]:
         parts.append(rng.standard_normal(shape) * math.sqrt(2.0 / shape[1]) if len(shape) == 2 else np.zeros(shape))
     return np.concatenate([p.ravel() for p in parts]).astype(np.float32)
 
@@ -119,7 +136,7 @@ def predict(params, X):
     import torch
     p = torch.from_numpy(np.ascontiguousarray(params, dtype=np.float32)).cuda()
     x = torch.as_tensor(X, dtype=torch.float32).cuda().contiguous()
-    y = torch.empty((x.shape[0], 3), device="cuda")
+    y = torch.empty((x.shape[0], N_OUT), device="cuda")
     check(lib().xc_mlp_forward(p.data_ptr(), x.data_ptr(), x.shape[0], y.data_ptr(),
                                torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
@@ -158,43 +175,45 @@ def install(params):
 
 
 def select(mode, dtype, left_shape, n_left, right_shape, n_right):
-    m = ctypes.c_int()
-    check(lib().xc_select_method(MODES[mode], DTYPES[dtype], size2(*left_shape), n_left, size2(*right_shape),
-                                 n_right, ctypes.byref(m)))
-    return {v: k for k, v in METHODS.items()}[m.value]
+    """The candidate XC_METHOD_AUTO runs ('auto' when neither a network nor a
+    tuning record decides: the first correlation then autotunes)."""
+    a = Algo()
+    check(lib().xc_select_algorithm(MODES[mode], DTYPES[dtype], size2(*left_shape), n_left, size2(*right_shape),
+                                    n_right, ctypes.byref(a)))
+    return algo_name(a)
 
 
 def autotune(mode, left, right, out, stream=None):
-    """Exhaustive autotune (xc_autotune_method) on device tensors: returns the
-    fastest method's name and its time in ms."""
+    """Exhaustive autotune (xc_autotune_algorithm) on device tensors: returns
+    the fastest candidate's name and its time in ms."""
     import torch
     n_l, hl, wl = left.shape
     n_r, hr, wr = right.shape
     dtype = "f32" if left.dtype == torch.float32 else "f64"
-    m = ctypes.c_int()
+    a = Algo()
     ms = ctypes.c_double()
     st = torch.cuda.current_stream().cuda_stream if stream is None else int(stream)
-    check(lib().xc_autotune_method(MODES[mode], DTYPES[dtype], left.data_ptr(), size2(hl, wl), n_l, right.data_ptr(),
-                                   size2(hr, wr), n_r, out.data_ptr(), st, ctypes.byref(m), ctypes.byref(ms)))
-    return {v: k for k, v in METHODS.items()}[m.value], ms.value
+    check(lib().xc_autotune_algorithm(MODES[mode], DTYPES[dtype], left.data_ptr(), size2(hl, wl), n_l,
+                                      right.data_ptr(), size2(hr, wr), n_r, out.data_ptr(), st, ctypes.byref(a),
+                                      ctypes.byref(ms)))
+    return algo_name(a), ms.value
 
 
-def time_method(mode, left, right, out, method, reps=5):
-    """Mean CUDA-event time (ms) of one correlation with `method`, workspace
-    allocated outside the timed calls."""
+def time_algo(mode, left, right, out, name, reps=5):
+    """Mean time (ms) of one correlation with candidate `name`, measured in
+    the library (xc_time_algorithm: a warm-up call, then `reps` calls between
+    CUDA events); the workspace is allocated outside the timed calls."""
     import torch
-    from . import correlate, workspace_size
+    from . import workspace_size
     n_l, hl, wl = left.shape
     n_r, hr, wr = right.shape
     dtype = "f32" if left.dtype == torch.float32 else "f64"
+    a = algo_struct(name)
+    method = {v: k for k, v in METHODS.items()}[a.method]
     wb = workspace_size(mode, dtype, method, (hl, wl), n_l, (hr, wr), n_r)
     ws = torch.empty(max(wb, 1), dtype=torch.uint8, device=left.device)
-    correlate(mode, left, right, method=method, out=out, workspace=ws)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
-        correlate(mode, left, right, method=method, out=out, workspace=ws)
-    e1.record()
-    e1.synchronize()
-    return e0.elapsed_time(e1) / reps
+    ms = ctypes.c_double()
+    check(lib().xc_time_algorithm(MODES[mode], DTYPES[dtype], a, left.data_ptr(), size2(hl, wl), n_l,
+                                  right.data_ptr(), size2(hr, wr), n_r, out.data_ptr(), ws.data_ptr(), wb, reps,
+                                  torch.cuda.current_stream().cuda_stream, ctypes.byref(ms)))
+    return ms.value

@@ -61,6 +61,19 @@ typedef enum xc_method {
   XC_METHOD_TC_TF32X3 = 4  /* the same with split-TF32 operands (kind::tf32): more accurate, half the rate */
 } xc_method;
 
+/* An algorithm: a method and one of its tile configurations.  Tiles: the
+ * plain kernel 0 (its default: 8 partners per CTA when there are 4 or more,
+ * else one), 1 (8 partners, 32 x 64 shifts; FP64: 4), 2 (one partner,
+ * 64 x 64 shifts; FP64: 32 x 64), 3 (one partner, 32 x 64 shifts); the FFT
+ * path 0; the split tensor-core paths 0 (items of at most 64 left rows) or
+ * the item length cap, 4 to 1024.  The reference names algorithm and tile
+ * arguments by hand (src/main.cpp:361-411, the JSON tile arguments of each
+ * plug-in). */
+typedef struct xc_algo {
+  xc_method method;
+  int32_t tile;
+} xc_algo;
+
 typedef struct xc_size2 {
   uint32_t x; /* columns */
   uint32_t y; /* rows */
@@ -242,11 +255,13 @@ xc_status xc_correlate_pairs(xc_dtype dtype, const void* d_left, const xc_matrix
 /* ------------------------------------------------------------------------ */
 /* Method selector (new; the reference picks algorithms and tiles by hand,  */
 /* benchmarking/args_test/*.yml): a 3-layer 64-wide FP32 MLP predicting the */
-/* log run time of each method, trained on timings measured on this GPU.    */
+/* log run time of each candidate algorithm (method and tile), trained on   */
+/* timings measured on this GPU.                                            */
 /* ------------------------------------------------------------------------ */
 #define XC_MLP_IN 8
 #define XC_MLP_HIDDEN 64
-#define XC_MLP_OUT 3 /* direct, fft, tc_bf16x3 */
+#define XC_MLP_OUT 7 /* one per selector candidate (xc_algorithm) */
+#define XC_N_ALGOS 7
 #define XC_MLP_PARAMS                                                                                       \
   (XC_MLP_HIDDEN * XC_MLP_IN + XC_MLP_HIDDEN + XC_MLP_HIDDEN * XC_MLP_HIDDEN + XC_MLP_HIDDEN +            \
    XC_MLP_OUT * XC_MLP_HIDDEN + XC_MLP_OUT)
@@ -273,15 +288,43 @@ xc_status xc_selector_load(const float* h_params);
 /* Reinstalls that built-in network (XC_ERR_UNSUPPORTED if the library was
  * built without one). */
 xc_status xc_selector_load_builtin(void);
-/* The method XC_METHOD_AUTO runs for a problem: the network's fastest
- * prediction among the methods that support it; without weights, the
- * method xc_autotune_method last measured fastest for this problem, else
- * XC_METHOD_DIRECT. */
+/* The selector's candidates (the network's outputs, in order): index
+ * 0-2 the plain kernel's tiles 1-3, 3 the FFT path, 4-5 split-BF16 with
+ * items of at most 32 and 64 left rows, 6 split-TF32. */
+xc_status xc_algorithm(uint32_t index, xc_algo* algo);
+/* The algorithm XC_METHOD_AUTO runs for a problem: the network's fastest
+ * prediction among the candidates that support it; without weights, the
+ * candidate xc_autotune_algorithm last measured fastest for this problem;
+ * with neither, {XC_METHOD_AUTO, 0}: xc_correlate's first call for the
+ * problem then runs the exhaustive autotune on its own buffers (allocating
+ * temporary workspaces and synchronising its stream) and remembers the
+ * result. */
+xc_status xc_select_algorithm(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
+                              uint32_t n_right, xc_algo* algo);
+/* The method of xc_select_algorithm's choice. */
 xc_status xc_select_method(xc_mode mode, xc_dtype dtype, xc_size2 left, uint32_t n_left, xc_size2 right,
                            uint32_t n_right, xc_method* method);
+/* xc_correlate with a given algorithm (method and tile); {XC_METHOD_AUTO, *}
+ * is xc_correlate's automatic choice.  The workspace is the method's
+ * (xc_workspace_size). */
+xc_status xc_correlate_algo(xc_mode mode, xc_dtype dtype, xc_algo algo, const void* d_left, xc_size2 left,
+                            uint32_t n_left, const void* d_right, xc_size2 right, uint32_t n_right, void* d_out,
+                            void* d_workspace, size_t workspace_bytes, void* stream);
+/* Time of one correlation with `algo`: one warm-up call, then `reps` calls
+ * back to back between CUDA events on `stream` (synchronised); *ms is the
+ * mean.  The timing the selector's dataset is measured with (no per-call
+ * overhead of a binding inside the timed region). */
+xc_status xc_time_algorithm(xc_mode mode, xc_dtype dtype, xc_algo algo, const void* d_left, xc_size2 left,
+                            uint32_t n_left, const void* d_right, xc_size2 right, uint32_t n_right, void* d_out,
+                            void* d_workspace, size_t workspace_bytes, uint32_t reps, void* stream, double* ms);
 /* Exhaustive autotune (the selector's fallback and judge): times every
- * method on the given device buffers (CUDA events, synchronising `stream`),
+ * candidate that supports the problem on the given device buffers
+ * (xc_time_algorithm, 3 calls each, workspaces allocated for the run),
  * remembers the fastest for this problem and returns it with its time. */
+xc_status xc_autotune_algorithm(xc_mode mode, xc_dtype dtype, const void* d_left, xc_size2 left, uint32_t n_left,
+                                const void* d_right, xc_size2 right, uint32_t n_right, void* d_out, void* stream,
+                                xc_algo* best, double* best_ms);
+/* The method of xc_autotune_algorithm's choice. */
 xc_status xc_autotune_method(xc_mode mode, xc_dtype dtype, const void* d_left, xc_size2 left, uint32_t n_left,
                              const void* d_right, xc_size2 right, uint32_t n_right, void* d_out, void* stream,
                              xc_method* best, double* best_ms);

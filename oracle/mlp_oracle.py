@@ -1,15 +1,15 @@
 """CPU oracle of the selector network (test infrastructure only).
 
 numpy restatement of cross-corr_gb300/csrc/mlp.cu: a 3-layer MLP
-8 -> 64 -> ReLU -> 64 -> ReLU -> 3 with parameters packed as
-W1[64][8], b1[64], W2[64][64], b2[64], W3[3][64], b3[3], the masked
+8 -> 64 -> ReLU -> 64 -> ReLU -> 7 with parameters packed as
+W1[64][8], b1[64], W2[64][64], b2[64], W3[7][64], b3[7], the masked
 mean-squared error and its analytic gradient, in float64.
 """
 from __future__ import annotations
 
 import numpy as np
 
-IN, H, OUT = 8, 64, 3
+IN, H, OUT = 8, 64, 7
 SIZES = [("W1", (H, IN)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (OUT, H)), ("b3", (OUT,))]
 N_PARAMS = sum(int(np.prod(s)) for _, s in SIZES)
 
