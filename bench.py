@@ -377,6 +377,8 @@ def run_ours(args, rank, world, local_rank):
         line["configs"] = config_studies(torch, xcorr)
         line["large_fft"] = large_fft_study(torch, xcorr)
         line["templates"] = template_study(torch, xcorr)
+    if rank == 0 and not args.no_csv:
+        line["csv_io"] = csv_study(xcorr)
     if rank == 0 and not args.no_reference_gpu:
         line["reference_gpu"] = reference_gpu_study(torch, xcorr, line)
     if rank == 0 and not args.no_cpu_baseline:
@@ -393,6 +395,43 @@ def run_ours(args, rank, world, local_rank):
             line["cpu_baseline"]["scipy_correlate2d"] = scipy_rate
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def csv_study(xcorr, loops=3):
+    """CSV throughput of the `cross` CLI, the reference's on-disk format
+    (`# rows,cols,count` header, one matrix row per line; src/matrix.hpp:94-185):
+    the workload's inputs (1 + 64 matrices of 256x256, written by numpy with
+    9 significant digits) are loaded and the 64 outputs of 511x511 stored by
+    `cross run -b CommonSteps`, whose Load and Store columns time exactly
+    those steps (nanoseconds per loop, `loops` loops; the median is kept)."""
+    import csv
+    import tempfile
+
+    left, right = make_inputs()
+    with tempfile.TemporaryDirectory() as d:
+        paths = {}
+        for name, a in (("left", left), ("right", right)):
+            paths[name] = os.path.join(d, f"{name}.csv")
+            with open(paths[name], "w") as f:
+                f.write(f"# {a.shape[1]},{a.shape[2]},{a.shape[0]}\n")
+                np.savetxt(f, a.reshape(-1, a.shape[2]), delimiter=",", fmt="%.9g")
+        times, out = os.path.join(d, "times.csv"), os.path.join(d, "out.csv")
+        r = subprocess.run([xcorr.CLI_PATH, "run", "-b", "CommonSteps", "-l", str(loops), "-m", "0", "-t", times,
+                            "-o", out, "nai_shuffle_multimat_right_one_to_many", paths["left"], paths["right"]],
+                           capture_output=True, text=True, timeout=600)
+        if r.returncode != 0:
+            return {"error": (r.stderr or r.stdout).strip()[-300:]}
+        with open(times) as f:
+            rows = list(csv.DictReader(f))
+        load_ms = statistics.median(float(row["Load"]) for row in rows) / 1e6
+        store_ms = statistics.median(float(row["Store"]) for row in rows) / 1e6
+        in_bytes = os.path.getsize(paths["left"]) + os.path.getsize(paths["right"])
+        out_bytes = os.path.getsize(os.path.join(d, "out_0.csv"))
+    return {"command": "cross run -b CommonSteps nai_shuffle_multimat_right_one_to_many", "loops": loops,
+            "input_mb": in_bytes / 1e6, "output_mb": out_bytes / 1e6, "load_ms": load_ms, "store_ms": store_ms,
+            "load_mb_per_s": in_bytes / 1e3 / load_ms, "store_mb_per_s": out_bytes / 1e3 / store_ms,
+            "values_per_s_load": (left.size + right.size) / (load_ms / 1e3),
+            "values_per_s_store": 64 * 511 * 511 / (store_ms / 1e3), "host_threads": os.cpu_count()}
 
 
 def sampled_fp64(left, right, outs, ref_scale, rng, n_shifts):
@@ -786,6 +825,7 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the other fixed configurations")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip the baseline leg that times the reference's own GPU kernels")
+    ap.add_argument("--no-csv", action="store_true", help="skip the CSV load/store study of the cross CLI")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
