@@ -5,7 +5,8 @@
 //                        (src/matrix.hpp:33-46) and the memset + scatter pair
 //                        (src/scatter.cu:16-102, src/one_to_many.hpp:705-725):
 //                        one pass writes every element of the padded buffer
-//                        (data or zero) with 16-byte stores.
+//                        (data or zero), a warp per row, in 8- or 16-byte
+//                        units.
 //  conj_multiply_kernel  replaces hadamard_original (src/hadamard.cu:33-58) and
 //                        hadamard_n_to_m_over_output (src/hadamard.cu:116-149):
 //                        out[o] = L[l] * conj(R[r]) for every output of the
@@ -49,90 +50,44 @@ constexpr int kGlueRows = 8;  // rows per block in the row-walking glue kernels
 
 // dst[m][y][x] = src[m][y - dst_y][x - dst_x] inside the source, 0 elsewhere;
 // dst rows have pitch `dst_pitch` elements (>= pad_cols; the tail of a row
-// beyond pad_cols is left untouched).  A block walks `rows_per_block`
-// consecutive (matrix, row) pairs, so the row indices cost one division per
-// block.  Each row is written as a scalar head up to its first 16-byte
-// boundary (rows of the in-place R2C layout, pitch 2 (px/2 + 1), start only
-// 8-byte aligned every other row), a body of 16-byte stores and a scalar
-// tail; rows outside the source are zeros and read nothing.  A thread loads
-// its 16-byte chunk of every one of the block's rows before it stores any,
-// so up to kGlueRows loads per thread are in flight; a chunk whose source is
-// 8-byte but not 16-byte aligned (the odd rows' bodies) is read as two
-// 8-byte loads.
-template <typename T>
-__device__ __forceinline__ T pad_value(const T* srow, bool row_in, int sx, int cols) {
-  return (row_in && sx >= 0 && sx < cols) ? __ldg(srow + sx) : T(0);
-}
-
-template <typename T, typename Vec>
-__device__ __forceinline__ Vec pad_chunk(const T* srow, bool row_in, int sx0, int cols) {
-  constexpr int V = 16 / (int)sizeof(T);
-  T v[V];
-  if (!row_in || sx0 >= cols || sx0 + V <= 0) {
+// beyond pad_cols is left untouched).  One warp per destination row (the
+// (matrix, row) pair costs one division per warp).  The row moves in units
+// U of E = sizeof(U) / sizeof(T) elements: E = 2 (8-byte floats, 16-byte
+// doubles) when the row starts, the pitch, the source width and the offset
+// dst_x allow it -- rows of the in-place R2C layout, pitch 2 (px/2 + 1),
+// start 8-byte aligned, so 16-byte units would not do for FP32 -- else
+// E = 1.  A lane loads its units of eight 32-unit strips before it stores
+// any, so eight loads per lane are in flight; rows outside the source are
+// zeros and read nothing.
+template <typename T, typename U>
+__global__ void __launch_bounds__(256) pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int rows, int cols,
+                                                  long long n_rows, int pad_rows, int pad_cols, int dst_pitch,
+                                                  int dst_y, int dst_x) {
+  constexpr int E = (int)(sizeof(U) / sizeof(T));
+  constexpr int kStrips = 8;
+  const int lane = threadIdx.x & 31;
+  const long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (row >= n_rows) return;  // warp-uniform
+  const long long m = row / pad_rows;
+  const int sy = (int)(row - m * pad_rows) - dst_y;
+  const bool row_in = sy >= 0 && sy < rows;
+  const U* __restrict__ su = reinterpret_cast<const U*>(src + (m * rows + (row_in ? sy : 0)) * (long long)cols);
+  U* __restrict__ du = reinterpret_cast<U*>(dst + row * (long long)dst_pitch);
+  const int units = pad_cols / E, src_units = cols / E, dxu = dst_x / E;
+  U zero;
+  memset(&zero, 0, sizeof(zero));
+  for (int u0 = 0; u0 < units; u0 += 32 * kStrips) {
+    U v[kStrips];
 #pragma unroll
-    for (int e = 0; e < V; ++e) v[e] = T(0);
-  } else if (sx0 >= 0 && sx0 + V <= cols && (((uintptr_t)(srow + sx0)) & 15) == 0) {
-    const Vec f = __ldg(reinterpret_cast<const Vec*>(srow + sx0));
-    memcpy(v, &f, sizeof(f));
-  } else if (sizeof(T) == 4 && sx0 >= 0 && sx0 + V <= cols && (((uintptr_t)(srow + sx0)) & 7) == 0) {
-    const float2 a = __ldg(reinterpret_cast<const float2*>(srow + sx0));
-    const float2 b = __ldg(reinterpret_cast<const float2*>(srow + sx0 + 2));
-    memcpy(v, &a, 8);
-    memcpy(reinterpret_cast<char*>(v) + 8, &b, 8);
-  } else {
-#pragma unroll
-    for (int e = 0; e < V; ++e) v[e] = pad_value(srow, true, sx0 + e, cols);
-  }
-  Vec o;
-  memcpy(&o, v, sizeof(o));
-  return o;
-}
-
-template <typename T>
-__global__ void pad_kernel(const T* __restrict__ src, T* __restrict__ dst, int rows, int cols, int count, int pad_rows,
-                           int pad_cols, int dst_pitch, int dst_y, int dst_x, int rows_per_block) {
-  constexpr int V = 16 / (int)sizeof(T);  // elements per 16-byte store
-  constexpr int R = kGlueRows;
-  using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
-  const long long n_rows = (long long)count * pad_rows;
-  const long long r0 = (long long)blockIdx.x * rows_per_block;
-  const int nr = (int)min((long long)min(rows_per_block, R), n_rows - r0);
-  long long m = r0 / pad_rows;
-  int y = (int)(r0 - m * pad_rows);
-  const T* srow[R];
-  T* drow[R];
-  bool row_in[R];
-  int lead[R], n_body[R];
-  int nb_max = 0;
-#pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int sy = y - dst_y;
-    row_in[i] = i < nr && sy >= 0 && sy < rows;
-    srow[i] = src + (m * rows + (row_in[i] ? sy : 0)) * (long long)cols;
-    drow[i] = dst + (r0 + min(i, nr - 1)) * (long long)dst_pitch;
-    lead[i] = min(pad_cols, (int)(((16u - ((uint32_t)(uintptr_t)drow[i] & 15u)) & 15u) / sizeof(T)));
-    n_body[i] = i < nr ? (pad_cols - lead[i]) / V : 0;
-    nb_max = max(nb_max, n_body[i]);
-    if (i < nr) {
-      const int tail0 = lead[i] + n_body[i] * V;
-      if ((int)threadIdx.x < lead[i])
-        drow[i][threadIdx.x] = pad_value(srow[i], row_in[i], (int)threadIdx.x - dst_x, cols);
-      if ((int)threadIdx.x < pad_cols - tail0)
-        drow[i][tail0 + threadIdx.x] = pad_value(srow[i], row_in[i], tail0 + (int)threadIdx.x - dst_x, cols);
+    for (int j = 0; j < kStrips; ++j) {
+      const int u = u0 + 32 * j + lane, x = u - dxu;
+      v[j] = (row_in && u < units && x >= 0 && x < src_units) ? __ldg(su + x) : zero;
     }
-    if (++y == pad_rows) {
-      y = 0;
-      ++m;
+#pragma unroll
+    for (int j = 0; j < kStrips; ++j) {
+      const int u = u0 + 32 * j + lane;
+      if (u < units) du[u] = v[j];
     }
-  }
-  for (int k = threadIdx.x; k < nb_max; k += blockDim.x) {
-    Vec v[R];
-#pragma unroll
-    for (int i = 0; i < R; ++i)
-      if (k < n_body[i]) v[i] = pad_chunk<T, Vec>(srow[i], row_in[i], lead[i] + k * V - dst_x, cols);
-#pragma unroll
-    for (int i = 0; i < R; ++i)
-      if (k < n_body[i]) reinterpret_cast<Vec*>(drow[i] + lead[i])[k] = v[i];
   }
 }
 
@@ -242,18 +197,29 @@ xc_status glue_pad_pitched(xc_dtype dtype, const void* src, void* dst, int rows,
                            int pad_cols, int dst_pitch, int dst_y, int dst_x, cudaStream_t stream) {
   if (count <= 0) return XC_OK;
   const long long n_rows = (long long)count * pad_rows;
-  // a few rows per block when there are many (fewer index divisions), one
-  // when there are few (enough blocks to fill the GPU)
-  const int rpb = (int)std::max(1LL, std::min((long long)kGlueRows, n_rows / (152LL * 16)));
-  const long long blocks = (n_rows + rpb - 1) / rpb;
+  const long long blocks = (n_rows + 7) / 8;  // 8 warps, one row each
   if (blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "too many rows for one launch");
-  const int threads = pad_cols >= 512 ? 128 : 64;
-  if (dtype == XC_F32)
-    pad_kernel<float><<<(unsigned)blocks, threads, 0, stream>>>((const float*)src, (float*)dst, rows, cols, count,
-                                                                pad_rows, pad_cols, dst_pitch, dst_y, dst_x, rpb);
-  else
-    pad_kernel<double><<<(unsigned)blocks, threads, 0, stream>>>((const double*)src, (double*)dst, rows, cols, count,
-                                                                 pad_rows, pad_cols, dst_pitch, dst_y, dst_x, rpb);
+  const size_t es = dtype == XC_F32 ? 4 : 8;
+  // two-element units: every row start, source and destination, and the
+  // placement of the source on a two-element boundary
+  const bool pairs = dst_x % 2 == 0 && cols % 2 == 0 && pad_cols % 2 == 0 && dst_pitch % 2 == 0 &&
+                     (uintptr_t)src % (2 * es) == 0 && (uintptr_t)dst % (2 * es) == 0;
+  const long long nr = n_rows;
+  if (dtype == XC_F32) {
+    if (pairs)
+      pad_kernel<float, float2><<<(unsigned)blocks, 256, 0, stream>>>((const float*)src, (float*)dst, rows, cols, nr,
+                                                                     pad_rows, pad_cols, dst_pitch, dst_y, dst_x);
+    else
+      pad_kernel<float, float><<<(unsigned)blocks, 256, 0, stream>>>((const float*)src, (float*)dst, rows, cols, nr,
+                                                                    pad_rows, pad_cols, dst_pitch, dst_y, dst_x);
+  } else {
+    if (pairs)
+      pad_kernel<double, double2><<<(unsigned)blocks, 256, 0, stream>>>((const double*)src, (double*)dst, rows, cols,
+                                                                       nr, pad_rows, pad_cols, dst_pitch, dst_y, dst_x);
+    else
+      pad_kernel<double, double><<<(unsigned)blocks, 256, 0, stream>>>((const double*)src, (double*)dst, rows, cols,
+                                                                      nr, pad_rows, pad_cols, dst_pitch, dst_y, dst_x);
+  }
   XC_CUDA_TRY(cudaGetLastError());
   return XC_OK;
 }
