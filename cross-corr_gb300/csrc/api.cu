@@ -46,51 +46,95 @@ struct PlanDeleter {
   void operator()(FftPlanImpl* p) const { fft_plan_destroy(p); }
 };
 
-struct ThreadCache {
-  std::map<PlanKey, std::unique_ptr<FftPlanImpl, PlanDeleter>> plans;
-  // xc_correlate_host buffers (grow-only).
+// One slot of the host-buffer pipeline: the device copies of one call's
+// inputs and output, its band counters, and the events that order its copies
+// and its correlation.  Two slots let one call's copies overlap the
+// neighbouring calls' kernels (xc_correlate_host_async).
+struct HostSlot {
   void* d_left = nullptr;
   void* d_right = nullptr;
   void* d_out = nullptr;
+  size_t left_bytes = 0, right_bytes = 0, out_bytes = 0;
+  int* d_bands = nullptr;          // band completion counters of the split path (8 ints)
+  cudaEvent_t ev_in = nullptr;     // inputs copied in
+  cudaEvent_t ev_start = nullptr;  // band counters cleared
+  cudaEvent_t ev_comp = nullptr;   // correlation done: inputs and workspace free
+  cudaEvent_t ev_out = nullptr;    // output copied out: the call is complete
+  uint64_t ticket = 0;             // the call that used the slot last
+  bool pending = false;            // enqueued and not yet waited for
+
+  xc_status create_events() {
+    for (cudaEvent_t* e : {&ev_in, &ev_start, &ev_comp, &ev_out})
+      XC_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    return XC_OK;
+  }
+  void release() {
+    cudaFree(d_left);
+    cudaFree(d_right);
+    cudaFree(d_out);
+    cudaFree(d_bands);
+    d_left = d_right = d_out = nullptr;
+    d_bands = nullptr;
+    left_bytes = right_bytes = out_bytes = 0;
+    for (cudaEvent_t* e : {&ev_in, &ev_start, &ev_comp, &ev_out}) {
+      if (*e != nullptr) cudaEventDestroy(*e);
+      *e = nullptr;
+    }
+    pending = false;
+  }
+};
+
+struct ThreadCache {
+  std::map<PlanKey, std::unique_ptr<FftPlanImpl, PlanDeleter>> plans;
+  // xc_correlate_host[_async] buffers (grow-only): two slots, and one
+  // workspace that the calls' correlations share (they run one after another)
+  HostSlot slots[2];
   void* d_ws = nullptr;
-  size_t left_bytes = 0, right_bytes = 0, out_bytes = 0, ws_bytes = 0;
-  int* d_bands = nullptr;  // band completion counters of the split path (8 ints)
+  size_t ws_bytes = 0;
+  uint64_t next_ticket = 1;
   int device = -1;
-  // xc_correlate_host pipeline: copy-in and copy-out streams, per-chunk events
-  cudaStream_t s_in = nullptr, s_out = nullptr;
+  // copy-in and copy-out streams, a stream for reading the device flags, and
+  // the per-chunk events of the chunked (large-output) pipeline
+  cudaStream_t s_in = nullptr, s_out = nullptr, s_flag = nullptr;
   cudaEvent_t ev_start = nullptr, ev_in[4] = {}, ev_comp[4] = {};
 
   xc_status ensure_streams() {
     if (s_in != nullptr) return XC_OK;
     XC_CUDA_TRY(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
     XC_CUDA_TRY(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
+    XC_CUDA_TRY(cudaStreamCreateWithFlags(&s_flag, cudaStreamNonBlocking));
     XC_CUDA_TRY(cudaEventCreateWithFlags(&ev_start, cudaEventDisableTiming));
     for (int i = 0; i < 4; ++i) {
       XC_CUDA_TRY(cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming));
       XC_CUDA_TRY(cudaEventCreateWithFlags(&ev_comp[i], cudaEventDisableTiming));
     }
+    for (HostSlot& sl : slots) XC_TRY(sl.create_events());
     return XC_OK;
   }
 
   void release() {
+    // calls still in flight finish before their buffers go
+    for (HostSlot& sl : slots)
+      if (sl.pending) cudaEventSynchronize(sl.ev_out);
+    if (s_in != nullptr) {
+      cudaStreamSynchronize(s_in);
+      cudaStreamSynchronize(s_out);
+    }
     plans.clear();
-    cudaFree(d_left);
-    cudaFree(d_right);
-    cudaFree(d_out);
+    for (HostSlot& sl : slots) sl.release();
     cudaFree(d_ws);
-    cudaFree(d_bands);
-    d_bands = nullptr;
-    d_left = d_right = d_out = d_ws = nullptr;
-    left_bytes = right_bytes = out_bytes = ws_bytes = 0;
+    d_ws = nullptr;
+    ws_bytes = 0;
     if (s_in != nullptr) {
       cudaStreamDestroy(s_in);
       cudaStreamDestroy(s_out);
+      cudaStreamDestroy(s_flag);
       cudaEventDestroy(ev_start);
       for (int i = 0; i < 4; ++i) {
         cudaEventDestroy(ev_in[i]);
         cudaEventDestroy(ev_comp[i]);
       }
-      s_in = s_out = nullptr;
+      s_in = s_out = s_flag = nullptr;
     }
   }
   ~ThreadCache() {
@@ -135,18 +179,18 @@ WaitValue32 wait_value32() {
 // kernel runs: the kernel counts each band's finished work items, and the
 // copy stream waits on each count (stream memory wait) before a 2D copy of
 // the band's rows of every output.  Inputs are already on the device.
-xc_status host_banded_tc(ThreadCache& c, xc_mode mode, bool tf32, xc_size2 left, uint32_t n_left, xc_size2 right,
-                         uint32_t n_right, uint64_t n_out, void* h_out, int n_bands, cudaStream_t s) {
+xc_status host_banded_tc(ThreadCache& c, HostSlot& sl, xc_mode mode, bool tf32, xc_size2 left, uint32_t n_left,
+                         xc_size2 right, uint32_t n_right, uint64_t n_out, void* h_out, int n_bands, cudaStream_t s) {
   const Geometry g = make_geometry(left, right);
   PairMap pm;
   uint64_t tmp = 0;
   if (!make_pair_map(mode, n_left, n_right, &pm, &tmp)) return fail(XC_ERR_INVALID_ARGUMENT, "bad pair map");
-  XC_CUDA_TRY(cudaMemsetAsync(c.d_bands, 0, 8 * sizeof(int), s));
-  XC_CUDA_TRY(cudaEventRecord(c.ev_start, s));
-  XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, c.ev_start, 0));
+  XC_CUDA_TRY(cudaMemsetAsync(sl.d_bands, 0, 8 * sizeof(int), s));
+  XC_CUDA_TRY(cudaEventRecord(sl.ev_start, s));
+  XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, sl.ev_start, 0));
   TcBands bands;
-  XC_TRY(tc_correlate_banded((const float*)c.d_left, (const float*)c.d_right, (float*)c.d_out, g, pm, c.d_ws,
-                             c.ws_bytes, s, tf32, n_bands, c.d_bands, &bands));
+  XC_TRY(tc_correlate_banded((const float*)sl.d_left, (const float*)sl.d_right, (float*)sl.d_out, g, pm, c.d_ws,
+                             c.ws_bytes, s, tf32, n_bands, sl.d_bands, &bands));
   const size_t row = (size_t)g.Sx * sizeof(float), mat = row * g.Sy;
   // Once the kernel is queued, a failure to queue a band's wait or copy still
   // lets the copies already queued finish (the release after the kernel
@@ -159,11 +203,11 @@ xc_status host_banded_tc(ThreadCache& c, xc_mode mode, bool tf32, xc_size2 left,
   };
   for (int k = 0; k < bands.n; ++k) {
     const int b = bands.order[k];
-    if (wait_value32()(reinterpret_cast<CUstream>(c.s_out), reinterpret_cast<CUdeviceptr>(c.d_bands + b),
+    if (wait_value32()(reinterpret_cast<CUstream>(c.s_out), reinterpret_cast<CUdeviceptr>(sl.d_bands + b),
                        (cuuint32_t)bands.items[b], CU_STREAM_WAIT_VALUE_GEQ) != CUDA_SUCCESS)
       return drain(XC_ERR_CUDA, "stream wait on an output band failed");
     const size_t off = row * bands.row_lo[b];
-    if (cudaMemcpy2DAsync(static_cast<char*>(h_out) + off, mat, static_cast<char*>(c.d_out) + off, mat,
+    if (cudaMemcpy2DAsync(static_cast<char*>(h_out) + off, mat, static_cast<char*>(sl.d_out) + off, mat,
                           row * (bands.row_hi[b] - bands.row_lo[b]), n_out, cudaMemcpyDeviceToHost,
                           c.s_out) != cudaSuccess)
       return drain(XC_ERR_CUDA, "copy of an output band failed to queue");
@@ -493,9 +537,30 @@ xc_status xc_correlate_algo(xc_mode mode, xc_dtype dtype, xc_algo algo, const vo
                   workspace_bytes, as_stream(stream));
 }
 
-xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
-                            uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
-                            void* stream) {
+}  // extern "C"
+
+namespace {
+
+// Waits for the call in `sl`, if it has not been waited for: its output
+// copied out and its correlation finished (its buffers and the workspace are
+// then free); its status.
+xc_status finish_slot(ThreadCache& c, HostSlot& sl) {
+  if (!sl.pending) return XC_OK;
+  sl.pending = false;
+  XC_CUDA_TRY(cudaEventSynchronize(sl.ev_out));
+  XC_CUDA_TRY(cudaEventSynchronize(sl.ev_comp));
+  return check_device_flags(c.s_flag);
+}
+
+// Enqueues one host-buffer correlation in pipeline slot ticket % 2: copy-in
+// on the copy-in stream, the correlation on the caller's stream, copy-out on
+// the copy-out stream.  With `after_stream` the copies also wait for work
+// already queued on the caller's stream.  Problems cut into chunks (192 MiB
+// of output or more) run to completion here.
+xc_status host_submit(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
+                      uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
+                      void* stream, bool after_stream, uint64_t* ticket) {
+  if (ticket == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "ticket is NULL");
   if (h_left == nullptr || h_right == nullptr || h_out == nullptr)
     return fail(XC_ERR_INVALID_ARGUMENT, "NULL host buffer");
   XC_TRY(check_sizes(left, right));
@@ -526,13 +591,18 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
   // The split tensor-core path instead copies the output out in row bands
   // while its kernel runs (one call, no per-chunk costs): eight bands from
   // 16 MiB of output (measured on 64 outputs of 511x511: 1, 2, 4 and 8 bands
-  // took 1.91, 1.84, 1.88 and 1.78 ms).  XC_HOST_BANDS fixes the count (1
-  // turns it off).
+  // took 1.91, 1.84, 1.88 and 1.78 ms).  A stream of calls
+  // (xc_correlate_host_async) copies the output out after the kernel
+  // instead: the next call's kernel hides that copy, and the kernel runs
+  // with its own work list rather than a banded schedule (at 64 outputs of
+  // 511x511 in a stream of calls: 1.149 ms per call against 1.221 with
+  // bands; kernel 1.036 against 1.063 ms).  XC_HOST_BANDS fixes the count
+  // (1 turns bands off).
   xc_algo sel{method, 0};
   if (method == XC_METHOD_AUTO && !select_algorithm(mode, dtype, left, n_left, right, n_right, &sel))
     sel = xc_algo{XC_METHOD_AUTO, 0};  // the first chunk's call autotunes
   const xc_method resolved = sel.method;
-  int n_bands = ob >= ((size_t)16 << 20) ? 8 : 1;
+  int n_bands = after_stream && ob >= ((size_t)16 << 20) ? 8 : 1;
   if (const char* e = std::getenv("XC_HOST_BANDS")) n_bands = std::max(1, std::atoi(e));
   const bool banded = (resolved == XC_METHOD_TC_BF16X3 || resolved == XC_METHOD_TC_TF32X3) && dtype == XC_F32 &&
                       n_bands > 1 && std::getenv("XC_HOST_CHUNKS") == nullptr && wait_value32() != nullptr &&
@@ -567,6 +637,19 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
     wb = std::max(wb, w);
   }
   ThreadCache& c = cache();
+  XC_TRY(c.ensure_streams());
+  const uint64_t t = c.next_ticket;
+  HostSlot& sl = c.slots[t % 2];
+  HostSlot& other = c.slots[(t + 1) % 2];
+  // the call two tickets back used this slot: it completes before the
+  // slot's buffers are reused (a failure of it is reported here)
+  XC_TRY(finish_slot(c, sl));
+  ++c.next_ticket;
+  *ticket = t;
+  sl.ticket = t;
+  // the shared workspace is regrown, and chunked problems run, only with
+  // the other slot's call complete
+  if (n_chunks > 1 || wb > c.ws_bytes) XC_TRY(finish_slot(c, other));
   auto grow = [](void** p, size_t* have, size_t need) -> xc_status {
     if (need <= *have) return XC_OK;
     cudaFree(*p);
@@ -576,52 +659,108 @@ xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, cons
     *have = need;
     return XC_OK;
   };
-  XC_TRY(grow(&c.d_left, &c.left_bytes, lb));
-  XC_TRY(grow(&c.d_right, &c.right_bytes, rb));
-  XC_TRY(grow(&c.d_out, &c.out_bytes, ob));
+  XC_TRY(grow(&sl.d_left, &sl.left_bytes, lb));
+  XC_TRY(grow(&sl.d_right, &sl.right_bytes, rb));
+  XC_TRY(grow(&sl.d_out, &sl.out_bytes, ob));
   if (wb > 0) XC_TRY(grow(&c.d_ws, &c.ws_bytes, wb));
-  XC_TRY(c.ensure_streams());
+  if (banded && sl.d_bands == nullptr) XC_CUDA_TRY(cudaMalloc(&sl.d_bands, 8 * sizeof(int)));
   cudaStream_t s = as_stream(stream);
-  if (banded) {
-    if (c.d_bands == nullptr) XC_CUDA_TRY(cudaMalloc(&c.d_bands, 8 * sizeof(int)));
-    XC_CUDA_TRY(cudaMemcpyAsync(c.d_left, h_left, lb, cudaMemcpyHostToDevice, s));
-    XC_CUDA_TRY(cudaMemcpyAsync(c.d_right, h_right, rb, cudaMemcpyHostToDevice, s));
-    XC_TRY(host_banded_tc(c, mode, resolved == XC_METHOD_TC_TF32X3, left, n_left, right, n_right, n_out, h_out,
-                          n_bands, s));
-    XC_CUDA_TRY(cudaStreamSynchronize(c.s_out));
-    XC_CUDA_TRY(cudaStreamSynchronize(s));
+  // Once a copy is queued, a failure lets everything queued finish before
+  // returning: no copy may touch the caller's buffers after the call.
+  const auto enqueue = [&]() -> xc_status {
+    if (after_stream || n_chunks > 1) {
+      // the copy streams start after work already queued on the caller's stream
+      XC_CUDA_TRY(cudaEventRecord(c.ev_start, s));
+      XC_CUDA_TRY(cudaStreamWaitEvent(c.s_in, c.ev_start, 0));
+      XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, c.ev_start, 0));
+    }
+    if (n_chunks > 1) {
+      char* dl = static_cast<char*>(sl.d_left);
+      char* dr = static_cast<char*>(sl.d_right);
+      char* dout = static_cast<char*>(sl.d_out);
+      for (int i = 0; i < n_chunks; ++i) {
+        uint32_t nl, nr;
+        size_t l_off, r_off, o_off, l_len, r_len, o_len;
+        chunk_shape(i, &nl, &nr, &l_off, &r_off, &o_off, &l_len, &r_len, &o_len);
+        if (l_len) XC_CUDA_TRY(cudaMemcpyAsync(dl + l_off, static_cast<const char*>(h_left) + l_off, l_len,
+                                               cudaMemcpyHostToDevice, c.s_in));
+        if (r_len) XC_CUDA_TRY(cudaMemcpyAsync(dr + r_off, static_cast<const char*>(h_right) + r_off, r_len,
+                                               cudaMemcpyHostToDevice, c.s_in));
+        XC_CUDA_TRY(cudaEventRecord(c.ev_in[i], c.s_in));
+        XC_CUDA_TRY(cudaStreamWaitEvent(s, c.ev_in[i], 0));
+        // a chunk reads every left (partner chunks) or every right (n_to_m):
+        // those were copied with chunk 0, which this stream has already waited for
+        const char* cl = by_left ? dl + l_off : dl;
+        const char* cr = by_left ? dr : dr + r_off;
+        XC_TRY(xc_correlate(mode, dtype, method, cl, left, nl, cr, right, nr, dout + o_off, c.d_ws, c.ws_bytes,
+                            stream));
+        XC_CUDA_TRY(cudaEventRecord(c.ev_comp[i], s));
+        XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, c.ev_comp[i], 0));
+        XC_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(h_out) + o_off, dout + o_off, o_len, cudaMemcpyDeviceToHost,
+                                    c.s_out));
+      }
+      return XC_OK;
+    }
+    XC_CUDA_TRY(cudaMemcpyAsync(sl.d_left, h_left, lb, cudaMemcpyHostToDevice, c.s_in));
+    XC_CUDA_TRY(cudaMemcpyAsync(sl.d_right, h_right, rb, cudaMemcpyHostToDevice, c.s_in));
+    XC_CUDA_TRY(cudaEventRecord(sl.ev_in, c.s_in));
+    XC_CUDA_TRY(cudaStreamWaitEvent(s, sl.ev_in, 0));
+    // the workspace is free once the other slot's correlation is done
+    XC_CUDA_TRY(cudaStreamWaitEvent(s, other.ev_comp, 0));
+    if (banded) {
+      XC_TRY(host_banded_tc(c, sl, mode, resolved == XC_METHOD_TC_TF32X3, left, n_left, right, n_right, n_out, h_out,
+                            n_bands, s));
+      XC_CUDA_TRY(cudaEventRecord(sl.ev_comp, s));
+    } else {
+      XC_TRY(xc_correlate(mode, dtype, method, sl.d_left, left, n_left, sl.d_right, right, n_right, sl.d_out, c.d_ws,
+                          c.ws_bytes, stream));
+      XC_CUDA_TRY(cudaEventRecord(sl.ev_comp, s));
+      XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, sl.ev_comp, 0));
+      XC_CUDA_TRY(cudaMemcpyAsync(h_out, sl.d_out, ob, cudaMemcpyDeviceToHost, c.s_out));
+    }
+    XC_CUDA_TRY(cudaEventRecord(sl.ev_out, c.s_out));
+    return XC_OK;
+  };
+  const xc_status st = enqueue();
+  if (st != XC_OK || n_chunks > 1) {
+    cudaStreamSynchronize(c.s_in);
+    cudaStreamSynchronize(c.s_out);
+    cudaStreamSynchronize(s);
+    XC_TRY(st);
     return check_device_flags(s);
   }
-  // the copy streams start after work already queued on the caller's stream
-  XC_CUDA_TRY(cudaEventRecord(c.ev_start, s));
-  XC_CUDA_TRY(cudaStreamWaitEvent(c.s_in, c.ev_start, 0));
-  XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, c.ev_start, 0));
-  char* dl = static_cast<char*>(c.d_left);
-  char* dr = static_cast<char*>(c.d_right);
-  char* dout = static_cast<char*>(c.d_out);
-  for (int i = 0; i < n_chunks; ++i) {
-    uint32_t nl, nr;
-    size_t l_off, r_off, o_off, l_len, r_len, o_len;
-    chunk_shape(i, &nl, &nr, &l_off, &r_off, &o_off, &l_len, &r_len, &o_len);
-    if (l_len) XC_CUDA_TRY(cudaMemcpyAsync(dl + l_off, static_cast<const char*>(h_left) + l_off, l_len,
-                                           cudaMemcpyHostToDevice, c.s_in));
-    if (r_len) XC_CUDA_TRY(cudaMemcpyAsync(dr + r_off, static_cast<const char*>(h_right) + r_off, r_len,
-                                           cudaMemcpyHostToDevice, c.s_in));
-    XC_CUDA_TRY(cudaEventRecord(c.ev_in[i], c.s_in));
-    XC_CUDA_TRY(cudaStreamWaitEvent(s, c.ev_in[i], 0));
-    // a chunk reads every left (partner chunks) or every right (n_to_m):
-    // those were copied with chunk 0, which this stream has already waited for
-    const char* cl = by_left ? dl + l_off : dl;
-    const char* cr = by_left ? dr : dr + r_off;
-    XC_TRY(xc_correlate(mode, dtype, method, cl, left, nl, cr, right, nr, dout + o_off, c.d_ws, c.ws_bytes, stream));
-    XC_CUDA_TRY(cudaEventRecord(c.ev_comp[i], s));
-    XC_CUDA_TRY(cudaStreamWaitEvent(c.s_out, c.ev_comp[i], 0));
-    XC_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(h_out) + o_off, dout + o_off, o_len, cudaMemcpyDeviceToHost,
-                                c.s_out));
-  }
-  XC_CUDA_TRY(cudaStreamSynchronize(c.s_out));
-  XC_CUDA_TRY(cudaStreamSynchronize(s));
-  return check_device_flags(s);
+  sl.pending = true;
+  return XC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
+                            uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
+                            void* stream) {
+  uint64_t t = 0;
+  XC_TRY(host_submit(mode, dtype, method, h_left, left, n_left, h_right, right, n_right, h_out, stream, true, &t));
+  XC_TRY(xc_host_wait(t));
+  XC_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  return XC_OK;
+}
+
+xc_status xc_correlate_host_async(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
+                                  uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
+                                  void* stream, uint64_t* ticket) {
+  return host_submit(mode, dtype, method, h_left, left, n_left, h_right, right, n_right, h_out, stream, false,
+                     ticket);
+}
+
+xc_status xc_host_wait(uint64_t ticket) {
+  ThreadCache& c = cache();
+  if (ticket == 0 || ticket >= c.next_ticket) return fail(XC_ERR_INVALID_ARGUMENT, "unknown ticket");
+  HostSlot& sl = c.slots[ticket % 2];
+  // a reused slot means the call completed (and was waited for) already
+  if (sl.ticket != ticket) return XC_OK;
+  return finish_slot(c, sl);
 }
 
 void xc_release_thread_cache(void) { cache().release(); }

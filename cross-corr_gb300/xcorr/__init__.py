@@ -33,7 +33,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "cuFFT error", 4: 
 EXPORTED = [
     "xc_version", "xc_status_string", "xc_last_error", "xc_device_check", "xc_check_device",
     "xc_debug_expire_wait", "xc_kernel_timing", "xc_kernel_timing_read", "xc_output_count", "xc_output_size",
-    "xc_workspace_size", "xc_correlate", "xc_correlate_host", "xc_release_thread_cache", "xc_correlate_tc_noalloc",
+    "xc_workspace_size", "xc_correlate", "xc_correlate_host", "xc_correlate_host_async", "xc_host_wait",
+    "xc_release_thread_cache", "xc_correlate_tc_noalloc",
     "xc_fft_plan_create", "xc_fft_plan_workspace_size", "xc_fft_plan_pad_size", "xc_fft_execute",
     "xc_fft_forward", "xc_fft_multiply", "xc_fft_inverse", "xc_fft_plan_destroy",
     "xc_run_ccn_shuffle_f32", "xc_run_ccn_shuffle_f64",
@@ -121,6 +122,9 @@ def lib():
         L.xc_workspace_size.argtypes = [i, i, i, Size2, u32, Size2, u32, c.POINTER(sz)]
         L.xc_correlate.argtypes = [i, i, i, vp, Size2, u32, vp, Size2, u32, vp, vp, sz, vp]
         L.xc_correlate_host.argtypes = [i, i, i, vp, Size2, u32, vp, Size2, u32, vp, vp]
+        L.xc_correlate_host_async.argtypes = [i, i, i, vp, Size2, u32, vp, Size2, u32, vp, vp,
+                                              c.POINTER(c.c_uint64)]
+        L.xc_host_wait.argtypes = [c.c_uint64]
         L.xc_release_thread_cache.restype = None
         L.xc_correlate_tc_noalloc.argtypes = [i, vp, Size2, u32, vp, Size2, u32, vp, vp]
         L.xc_fft_plan_create.argtypes = [c.POINTER(vp), i, i, Size2, u32, Size2, u32, Size2]
@@ -266,6 +270,32 @@ def correlate_host(mode: str, left: np.ndarray, right: np.ndarray, method: str =
                                   right.ctypes.data, size2(hr, wr), m, out.ctypes.data,
                                   None if stream is None else int(stream)))
     return out
+
+
+def correlate_host_async(mode: str, left: np.ndarray, right: np.ndarray, out: np.ndarray, method: str = "direct",
+                         stream=None) -> int:
+    """Enqueue a host-buffer correlation (xc_correlate_host_async) and return
+    its ticket; `left`, `right` and `out` are C-contiguous arrays of the
+    problem's dtype (pinned memory lets the copies overlap kernels) that must
+    stay alive, and `out` unread, until ``host_wait(ticket)``."""
+    n, hl, wl = left.shape
+    m, hr, wr = right.shape
+    dtype = "f64" if left.dtype == np.float64 else "f32"
+    for a in (left, right, out):
+        if not a.flags["C_CONTIGUOUS"] or a.dtype != left.dtype:
+            raise ValueError("left, right and out must be C-contiguous arrays of one dtype")
+    if out.shape != (output_count(mode, n, m), hl + hr - 1, wl + wr - 1):
+        raise ValueError("out has the wrong shape")
+    t = ctypes.c_uint64()
+    check(lib().xc_correlate_host_async(MODES[mode], DTYPES[dtype], METHODS[method], left.ctypes.data,
+                                        size2(hl, wl), n, right.ctypes.data, size2(hr, wr), m, out.ctypes.data,
+                                        None if stream is None else int(stream), ctypes.byref(t)))
+    return t.value
+
+
+def host_wait(ticket: int) -> None:
+    """Block until the xc_correlate_host_async call `ticket` is complete."""
+    check(lib().xc_host_wait(ctypes.c_uint64(ticket)))
 
 
 class kernel_timing:

@@ -159,7 +159,30 @@ xc_status xc_correlate(xc_mode mode, xc_dtype dtype, xc_method method, const voi
 xc_status xc_correlate_host(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left, xc_size2 left,
                             uint32_t n_left, const void* h_right, xc_size2 right, uint32_t n_right, void* h_out,
                             void* stream);
-/* Releases the calling thread's cached buffers and plans. */
+/* xc_correlate_host for a stream of independent problems (new; the
+ * reference runs one problem per process, src/main.cpp:123-174): enqueues
+ * the call's copy-in, correlation (on `stream`) and copy-out, returns at
+ * once and names the call in *ticket.  Two calls per thread are in flight:
+ * the next call's copy-in runs while this one's kernel does, and this one's
+ * copy-out (after its kernel, not in row bands) runs under the next one's
+ * kernel.  A call first waits for
+ * the call two tickets back (and returns its error, enqueueing nothing, if
+ * that call failed unwaited).  Unlike xc_correlate_host, the copies do not
+ * wait for work already queued on `stream`: the host inputs must be ready
+ * when the call is made.  h_left, h_right and h_out must stay valid, and
+ * h_out unread, until xc_host_wait(ticket) returns; pinned host buffers
+ * let the copies run asynchronously.  Problems cut into chunks (192 MiB of
+ * output or more) run to completion before the call returns.  Tickets
+ * belong to the calling thread. */
+xc_status xc_correlate_host_async(xc_mode mode, xc_dtype dtype, xc_method method, const void* h_left,
+                                  xc_size2 left, uint32_t n_left, const void* h_right, xc_size2 right,
+                                  uint32_t n_right, void* h_out, void* stream, uint64_t* ticket);
+/* Blocks until the call `ticket` has its output in h_out; its status (a
+ * bounded device wait that expired reports XC_ERR_TIMEOUT).  Waiting again,
+ * or for a call whose slot a later call has reused, returns XC_OK. */
+xc_status xc_host_wait(uint64_t ticket);
+/* Releases the calling thread's cached buffers and plans (after the calls
+ * in flight complete). */
 void xc_release_thread_cache(void);
 
 /* ------------------------------------------------------------------------ */
