@@ -277,7 +277,7 @@ std::map<SelKey, xc_algo> g_tuned;
 
 bool method_supported(xc_method m, xc_dtype dtype, xc_size2 left, xc_size2 right) {
   if (m == XC_METHOD_TC_BF16X3 || m == XC_METHOD_TC_TF32X3)
-    // FP32 only; the mean-correction kernel stages Wl + Wr + 2 floats per output row (8 rows, <= 200 KB)
+    // FP32 only; sizes with Wl + Wr below 6400 (the mean-correction kernel's staging)
     return dtype == XC_F32 && (uint64_t)left.x + right.x + 2 <= 6400;
   return m == XC_METHOD_DIRECT || m == XC_METHOD_FFT;
 }

@@ -915,9 +915,13 @@ struct PrepSide {
   int slices;        // sum_kernel blocks per matrix
   double* sums;      // per-matrix sums and sums of squares
   double* sq;
-  const float* mu;   // per-matrix means
+  float* mu;         // per-matrix means (written by colsum_kernel)
   float* sat;        // (H+1) x (W+1) summed-area table per matrix
   long long sat_rows;  // matrices x (H+1)
+  void* hi;          // split planes of the centred matrices (right side only;
+  void* lo;          // nullptr: no split), rows of `pitch` elements
+  int pitch;
+  int split_tf32;    // 1: TF32-rounded FP32 planes, 0: BF16
 };
 
 // Matrix sums and sums of squares (means and spreads): blocks over (matrix,
@@ -1001,44 +1005,39 @@ __device__ __forceinline__ MeanSd mean_sd(const double* __restrict__ sums, const
   return {(float)mean, (float)sqrt(fmax(0.0, sq[m] / area - mean * mean))};
 }
 
-// Blocks [0, mean_blocks) write the means and standard deviations of all
-// matrices; the others find the windows (from the same sums, so the values
-// agree bit for bit), one warp per (left matrix, partner group), lanes over
-// the partners.
-__global__ void __launch_bounds__(256) stats_kernel(const double* __restrict__ sums, const double* __restrict__ sq,
-                                                    int n_left, double left_area, int n_total, double right_area,
-                                                    float* __restrict__ mu, float* __restrict__ sd,
-                                                    unsigned mean_blocks, PairMap pm, int n_pgroups, int P,
-                                                    int base_rows, int max_rows, int fixed, int* __restrict__ flush) {
-  if (blockIdx.x < mean_blocks) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m < n_total) {
-      const MeanSd v = mean_sd(sums, sq, m, n_left, left_area, right_area);
-      mu[m] = v.mu;
-      sd[m] = v.sd;
-    }
-    return;
-  }
-  const long long i = ((blockIdx.x - mean_blocks) * (long long)blockDim.x + threadIdx.x) >> 5;
+// Accumulation windows: one warp per (left matrix, partner group), lanes
+// over the partners; from the same sums as the means, so the values agree
+// bit for bit with the means the other kernels use.
+struct WinArgs {
+  const double* sums;
+  const double* sq;
+  int n_left;
+  double left_area, right_area;
+  PairMap pm;
+  int n_pgroups, P, base_rows, max_rows, fixed;
+  int* flush;
+};
+__device__ __forceinline__ void window_block(const WinArgs& wa, long long b) {
+  const long long i = (b * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (i >= (long long)n_left * n_pgroups) return;  // warp-uniform
-  const int l = (int)(i / n_pgroups), pg = (int)(i % n_pgroups);
-  const MeanSd vl = mean_sd(sums, sq, l, n_left, left_area, right_area);
+  if (i >= (long long)wa.n_left * wa.n_pgroups) return;  // warp-uniform
+  const int l = (int)(i / wa.n_pgroups), pg = (int)(i % wa.n_pgroups);
+  const MeanSd vl = mean_sd(wa.sums, wa.sq, l, wa.n_left, wa.left_area, wa.right_area);
   const float ml = vl.mu, sl = vl.sd;
   float rho = 0.0f;
-  for (int k = pg * P + lane; k < min(pm.K, pg * P + P); k += 32) {
-    const long long r = (long long)l * pm.r_l + (long long)k * pm.r_k + n_left;
-    const MeanSd vr = mean_sd(sums, sq, (int)r, n_left, left_area, right_area);
+  for (int k = pg * wa.P + lane; k < min(wa.pm.K, pg * wa.P + wa.P); k += 32) {
+    const long long r = (long long)l * wa.pm.r_l + (long long)k * wa.pm.r_k + wa.n_left;
+    const MeanSd vr = mean_sd(wa.sums, wa.sq, (int)r, wa.n_left, wa.left_area, wa.right_area);
     const float den = fabsf(ml * vr.mu) + sl * vr.sd;
     if (den > 0.0f) rho = fmaxf(rho, sl * vr.sd / den);
   }
   for (int o = 16; o > 0; o >>= 1) rho = fmaxf(rho, __shfl_xor_sync(0xffffffffu, rho, o));
-  int rows = max_rows;
-  if (fixed > 0)
-    rows = fixed;
+  int rows = wa.max_rows;
+  if (wa.fixed > 0)
+    rows = wa.fixed;
   else if (rho > 0.0f)
-    rows = (int)fminf((float)max_rows, fmaxf((float)base_rows, base_rows / rho));
-  if (lane == 0) flush[i] = max(1, rows);
+    rows = (int)fminf((float)wa.max_rows, fmaxf((float)wa.base_rows, wa.base_rows / rho));
+  if (lane == 0) wa.flush[i] = max(1, rows);
 }
 
 // Summed-area tables of the centred matrices fl32(M - mu) (the values the
@@ -1050,10 +1049,68 @@ __global__ void __launch_bounds__(256) stats_kernel(const double* __restrict__ s
 // 64-row chunk), which keeps every FP32 chain short.  One block per (matrix,
 // 32-column strip); each of its 8 warps loads 8 consecutive rows of a chunk
 // (coalesced, independent loads).
+// Split planes of the centred right matrices fl32(R - mu_R), hi/lo with a
+// padded pitch: BF16 (T = __nv_bfloat16) or TF32-rounded FP32 (T = float).
+// Block b covers 1/bpm of matrix b / bpm (its mean computed once, from the
+// sums); a thread writes one 16-byte chunk of each plane (8 BF16 or 4 FP32
+// values) and reads the row as float4 when it is 16-byte aligned; zeros in
+// the pitch padding.
+template <typename T>
+__device__ __forceinline__ void split_block(const PrepSide& sd_, int b, int bpm) {
+  constexpr int E = 16 / (int)sizeof(T);
+  const int H = sd_.H, W = sd_.W, cpr = sd_.pitch / E;  // chunks per row
+  const int m = b / bpm, part = b % bpm;
+  const float mv = (float)(sd_.sums[m] / (double)sd_.area);
+  const long long per = (long long)H * cpr;
+  const long long lo = per * part / bpm, hi = per * (part + 1) / bpm;
+  const float* src = sd_.src + (long long)m * H * W;
+  const bool vec = (W % 4) == 0 && (reinterpret_cast<uintptr_t>(sd_.src) & 15) == 0;
+  uint4* ph4 = reinterpret_cast<uint4*>(sd_.hi) + (long long)m * per;
+  uint4* pl4 = reinterpret_cast<uint4*>(sd_.lo) + (long long)m * per;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    const int r = (int)(i / cpr);
+    const int c0 = (int)(i - (long long)r * cpr) * E;
+    const float* row = src + (long long)r * W;
+    float v[E];
+    if (vec && c0 + E <= W) {
+#pragma unroll
+      for (int q = 0; q < E; q += 4) {
+        const float4 f = __ldg(reinterpret_cast<const float4*>(row + c0 + q));
+        v[q] = f.x;
+        v[q + 1] = f.y;
+        v[q + 2] = f.z;
+        v[q + 3] = f.w;
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < E; ++q) v[q] = c0 + q < W ? __ldg(row + c0 + q) : mv;
+    }
+    uint4 oh, ol;
+    uint32_t* ph = reinterpret_cast<uint32_t*>(&oh);
+    uint32_t* pl = reinterpret_cast<uint32_t*>(&ol);
+#pragma unroll
+    for (int q = 0; q < E; q += (sizeof(T) == 4 ? 1 : 2)) {
+      if constexpr (sizeof(T) == 4) {
+        const float x = c0 + q < W ? v[q] - mv : 0.0f;
+        const float h = tf32_round(x);
+        ph[q] = __float_as_uint(h);
+        pl[q] = __float_as_uint(tf32_round(x - h));
+      } else {
+        const float x0 = c0 + q < W ? v[q] - mv : 0.0f, x1 = c0 + q + 1 < W ? v[q + 1] - mv : 0.0f;
+        const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+        const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h));
+        ph[q / 2] = *reinterpret_cast<const uint32_t*>(&h);
+        pl[q / 2] = *reinterpret_cast<const uint32_t*>(&l);
+      }
+    }
+    ph4[i] = oh;
+    pl4[i] = ol;
+  }
+}
+
 __device__ __forceinline__ void colsum_block(const PrepSide& sd_, int b) {
   const float* __restrict__ src = sd_.src;
   const int H = sd_.H, W = sd_.W;
-  const float* __restrict__ mu = sd_.mu;
   float* __restrict__ C = sd_.sat;
   __shared__ float seg[8][32];
   __shared__ float carry[32];
@@ -1064,7 +1121,10 @@ __device__ __forceinline__ void colsum_block(const PrepSide& sd_, int b) {
   const int w = threadIdx.x >> 5;
   const float* a = src + (long long)m * H * W;
   float* c = C + (long long)m * (H + 1) * (W + 1) + 1;  // column x of C is column x + 1 of S
-  const float mv = mu[m];
+  // the mean as the statistics of every other kernel see it: FP64 sum over
+  // the area, rounded once
+  const float mv = (float)(sd_.sums[m] / (double)sd_.area);
+  if (b % strips == 0 && threadIdx.x == 0) sd_.mu[m] = mv;
   if (w == 0) {
     carry[lane] = 0.0f;
     if (x < W) c[x] = 0.0f;
@@ -1098,66 +1158,24 @@ __device__ __forceinline__ void colsum_block(const PrepSide& sd_, int b) {
   }
 }
 
-// One block per (matrix, 32-column strip) of either side.
-__global__ void __launch_bounds__(256) colsum_kernel(const PrepSide a, const PrepSide b, unsigned a_blocks) {
+// One block per (matrix, 32-column strip) of either side (which also writes
+// the means), then the blocks of the right side's split planes, then those
+// of the accumulation windows: four independent jobs in one launch, the
+// split filling the SMs the latency-bound column sums leave idle.
+__global__ void __launch_bounds__(256) colsum_kernel(const PrepSide a, const PrepSide b, unsigned a_blocks,
+                                                     unsigned ab_blocks, unsigned split_end, int split_bpm,
+                                                     const WinArgs wa) {
   if (blockIdx.x < a_blocks)
     colsum_block(a, (int)blockIdx.x);
-  else
+  else if (blockIdx.x < ab_blocks)
     colsum_block(b, (int)(blockIdx.x - a_blocks));
-}
-
-// Splits the centred right matrices fl32(R - mu_R) into hi/lo planes with a
-// padded pitch: BF16 (T = __nv_bfloat16) or TF32-rounded FP32 (T = float).
-// A thread writes one 16-byte chunk of each plane (8 BF16 or 4 FP32 values);
-// when the rows are 16-byte multiples (and aligned) it reads them as float4.
-template <typename T>
-__global__ void __launch_bounds__(256) split_kernel(const float* __restrict__ src, const float* __restrict__ mu,
-                                                    T* __restrict__ hi, T* __restrict__ lo, long long rows,
-                                                    int rows_per_matrix, int cols, int pitch) {
-  constexpr int E = 16 / (int)sizeof(T);
-  const int cpr = pitch / E;  // chunks per row
-  const long long total = rows * cpr;
-  const bool vec = (cols % 4) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long r = i / cpr;
-    const int c0 = (int)(i - r * cpr) * E;
-    const float m = __ldg(mu + r / rows_per_matrix);
-    const float* row = src + r * cols;
-    float v[E];
-    if (vec && c0 + E <= cols) {
-#pragma unroll
-      for (int q = 0; q < E; q += 4) {
-        const float4 f = __ldg(reinterpret_cast<const float4*>(row + c0 + q));
-        v[q] = f.x;
-        v[q + 1] = f.y;
-        v[q + 2] = f.z;
-        v[q + 3] = f.w;
-      }
-    } else {
-#pragma unroll
-      for (int q = 0; q < E; ++q) v[q] = c0 + q < cols ? __ldg(row + c0 + q) : m;
-    }
-    uint4 oh, ol;
-    uint32_t* ph = reinterpret_cast<uint32_t*>(&oh);
-    uint32_t* pl = reinterpret_cast<uint32_t*>(&ol);
-#pragma unroll
-    for (int q = 0; q < E; q += (sizeof(T) == 4 ? 1 : 2)) {
-      if constexpr (sizeof(T) == 4) {
-        const float x = c0 + q < cols ? v[q] - m : 0.0f;
-        const float h = tf32_round(x);
-        ph[q] = __float_as_uint(h);
-        pl[q] = __float_as_uint(tf32_round(x - h));
-      } else {
-        const float x0 = c0 + q < cols ? v[q] - m : 0.0f, x1 = c0 + q + 1 < cols ? v[q + 1] - m : 0.0f;
-        const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
-        const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - __low2float(h), x1 - __high2float(h));
-        ph[q / 2] = *reinterpret_cast<const uint32_t*>(&h);
-        pl[q / 2] = *reinterpret_cast<const uint32_t*>(&l);
-      }
-    }
-    reinterpret_cast<uint4*>(hi)[i] = oh;
-    reinterpret_cast<uint4*>(lo)[i] = ol;
+  else if (blockIdx.x < split_end) {
+    if (b.split_tf32)
+      split_block<float>(b, (int)(blockIdx.x - ab_blocks), split_bpm);
+    else
+      split_block<__nv_bfloat16>(b, (int)(blockIdx.x - ab_blocks), split_bpm);
+  } else {
+    window_block(wa, blockIdx.x - split_end);
   }
 }
 
@@ -1198,108 +1216,89 @@ __global__ void __launch_bounds__(256) rowscan_kernel(const PrepSide a, const Pr
 
 // out[o][sy][sx] = mu_R * S_L' + mu_L * S_R' + mu_L * mu_R * area over the
 // overlap of shift (sy, sx), where S' are sums of the centred matrices over
-// the overlap, read from the summed-area tables.  A block covers 8 output
-// rows.  Along a row the overlap's rows y0..y1 are fixed, so each warp first
-// stages its row's table-row differences D_L[x] = S_L[y1][x] - S_L[y0][x]
-// and D_R likewise in shared memory (four coalesced table rows instead of
-// eight table reads per shift; 16 loads in flight per lane).  Then each
-// thread takes one shift column sx (the overlap's columns x0..x1 depend on
-// sx alone) through the block's 8 rows: S'_L = D_L[x1] - D_L[x0], S'_R =
-// D_R[x1 - dx] - D_R[x0 - dx].  The kernel writes every output once and is
-// bound by instruction issue, hence the column-wise reuse of the index
-// arithmetic.  FP32 (the centred sums are small, and the result's rounding
-// stays near 1e-7 of max|out|).
-// Staged floats per output row: D_L (Wl + 1) and D_R (Wr + 1), padded to 4.
-inline int corr_stage(int Wl, int Wr) { return (Wl + Wr + 2 + 3) / 4 * 4; }
+// the overlap, read from the summed-area tables.  A block covers one row
+// shift sy of up to 8 outputs that share a left matrix (partners k0..k0+7
+// of left l).  Along a row the overlap's rows y0..y1 are fixed, so the block
+// first stages the table-row differences D_L[x] = S_L[y1][x] - S_L[y0][x]
+// once (the same for all its partners) and each warp stages its partner's
+// D_R likewise, in shared memory (coalesced table rows, 8 loads in flight
+// per lane).  Then each thread takes one shift column sx (the overlap's
+// columns x0..x1 depend on sx alone): S'_L = D_L[x1] - D_L[x0] once, and
+// per partner S'_R = D_R[x1 - dx] - D_R[x0 - dx].  The kernel writes every
+// output once and is bound by instruction issue, hence the reuse of the
+// left differences and of the index arithmetic across partners.  FP32 (the
+// centred sums are small, and the result's rounding stays near 1e-7 of
+// max|out|).
+// Staged floats: D_L (Wl + 1) and D_R (Wr + 1), each padded to 4.
+inline int corr_stage(int W) { return (W + 1 + 3) / 4 * 4; }
+constexpr int kCorrPartners = 8;  // partners per block, one warp each
 __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out, const float* __restrict__ SL,
                                                          const float* __restrict__ SR,
                                                          const float* __restrict__ mu_l,
                                                          const float* __restrict__ mu_r, int Hl, int Wl, int Hr,
-                                                         int Wr, int Sy, int Sx, long long n_rows, PairMap pm,
-                                                         int stage_w) {
-  // per row: D_L in [0, Wl], D_R in [Wl + 1, Wl + Wr + 1] (dynamic: 8 x stage_w floats)
-  extern __shared__ float stage_all[];
-  auto stage = [&](int r) { return stage_all + r * stage_w; };
-  __shared__ float coef[8][4];            // per row: mu_L, mu_R, mu_L mu_R, overlap rows
+                                                         int Wr, int Sy, int Sx, PairMap pm, int n_kgroups,
+                                                         int stage_l, int stage_r) {
+  extern __shared__ float stage_all[];  // D_L, then one D_R per warp
+  __shared__ float mr[kCorrPartners];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const long long row0 = blockIdx.x * 8LL;
-  const long long row = row0 + wid;  // o * Sy + sy
-  if (row < n_rows) {                // warp-uniform
-    const long long o = row / Sy;
-    const int sy = (int)(row % Sy);
-    // invert o = l*o_l + k*o_k for the three pair-map forms
-    long long l, k;
-    if (pm.o_l == 0) {  // one_to_one / one_to_many: o = k
-      l = 0;
-      k = o;
-    } else if (pm.o_k == 1 && pm.o_l == pm.K) {  // n_to_m: o = l*K + k
-      l = o / pm.K;
-      k = o % pm.K;
-    } else {  // n_to_mn: o = l + k*n
-      l = o % pm.n_left;
-      k = o / pm.n_left;
-    }
-    const long long r = l * pm.r_l + k * pm.r_k;
-    const int dy = sy - (Hr - 1);
-    const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
+  long long bid = blockIdx.x;
+  const int sy = (int)(bid % Sy);
+  bid /= Sy;
+  const int kg = (int)(bid % n_kgroups);
+  const long long l = bid / n_kgroups;
+  const int k0 = kg * kCorrPartners;
+  const int n_here = min(kCorrPartners, pm.K - k0);
+  const int dy = sy - (Hr - 1);
+  const int y0 = max(0, dy), y1 = min(Hl, Hr + dy);
+  {  // D_L, all threads
     const float* l0 = SL + (l * (Hl + 1) + y0) * (long long)(Wl + 1);
     const float* l1 = SL + (l * (Hl + 1) + y1) * (long long)(Wl + 1);
+    for (int t = threadIdx.x; t < Wl + 1; t += blockDim.x) stage_all[t] = __ldg(l1 + t) - __ldg(l0 + t);
+  }
+  if (wid < n_here) {  // warp-uniform: D_R of partner k0 + wid
+    const long long r = l * pm.r_l + (long long)(k0 + wid) * pm.r_k;
     const float* r0 = SR + (r * (Hr + 1) + (y0 - dy)) * (long long)(Wr + 1);
     const float* r1 = SR + (r * (Hr + 1) + (y1 - dy)) * (long long)(Wr + 1);
-    float* st = stage(wid);
-    const int nl = Wl + 1, nt = Wl + Wr + 2;
-    for (int t0 = 0; t0 < nt; t0 += 256) {
+    float* st = stage_all + stage_l + wid * stage_r;
+    for (int t0 = 0; t0 < Wr + 1; t0 += 256) {
       float a[8], b[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int t = t0 + 32 * u + lane;
-        a[u] = 0.0f;
-        b[u] = 0.0f;
-        if (t < nl) {
-          a[u] = __ldg(l1 + t);
-          b[u] = __ldg(l0 + t);
-        } else if (t < nt) {
-          a[u] = __ldg(r1 + (t - nl));
-          b[u] = __ldg(r0 + (t - nl));
-        }
+        a[u] = t < Wr + 1 ? __ldg(r1 + t) : 0.0f;
+        b[u] = t < Wr + 1 ? __ldg(r0 + t) : 0.0f;
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int t = t0 + 32 * u + lane;
-        if (t < nt) st[t] = a[u] - b[u];
+        if (t < Wr + 1) st[t] = a[u] - b[u];
       }
     }
-    if (lane == 0) {
-      const float ml = mu_l[l], mr = mu_r[r];
-      coef[wid][0] = ml;
-      coef[wid][1] = mr;
-      coef[wid][2] = ml * mr;
-      coef[wid][3] = (float)(y1 - y0);
-    }
+    if (lane == 0) mr[wid] = mu_r[r];
   }
   __syncthreads();
-  const int n_here = (int)min(8LL, n_rows - row0);
-  float cl[8], cr[8], clr[8], cy[8];
+  const float cl = mu_l[l], cy = (float)(y1 - y0);
+  float cr[kCorrPartners], clr[kCorrPartners];
 #pragma unroll
-  for (int w = 0; w < 8; ++w) {
-    cl[w] = coef[w][0];
-    cr[w] = coef[w][1];
-    clr[w] = coef[w][2];
-    cy[w] = coef[w][3];
+  for (int w = 0; w < kCorrPartners; ++w) {
+    cr[w] = w < n_here ? mr[w] : 0.0f;
+    clr[w] = cl * cr[w];
   }
-  for (int sx = threadIdx.x; sx < Sx; sx += 256) {
+  const float* dl = stage_all;
+  float* o0 = out + ((l * pm.o_l + (long long)k0 * pm.o_k) * Sy + sy) * (long long)Sx;
+  const long long ostep = (long long)pm.o_k * Sy * Sx;  // next partner's output row
+  for (int sx = threadIdx.x; sx < Sx; sx += blockDim.x) {
     const int dx = sx - (Wr - 1);
     const int x0 = max(0, dx), x1 = min(Wl, Wr + dx);
-    const int j1 = Wl + 1 + x1 - dx, j0 = Wl + 1 + x0 - dx;
-    const float width = (float)(x1 - x0);
-    float* o = out + row0 * Sx + sx;
+    const int j0 = x0 - dx, j1 = x1 - dx;
+    const float area = cy * (float)(x1 - x0);
+    const float sl = dl[x1] - dl[x0];
 #pragma unroll
-    for (int w = 0; w < 8; ++w) {
+    for (int w = 0; w < kCorrPartners; ++w) {
       if (w < n_here) {
-        const float* st = stage(w);
-        const float sl = st[x1] - st[x0];
-        const float sr = st[j1] - st[j0];
-        o[(long long)w * Sx] = fmaf(cr[w], sl, fmaf(cl[w], sr, clr[w] * (cy[w] * width)));
+        const float* dr = stage_all + stage_l + w * stage_r;
+        const float sr = dr[j1] - dr[j0];
+        o0[w * ostep + sx] = fmaf(cr[w], sl, fmaf(cl, sr, clr[w] * area));
       }
     }
   }
@@ -1316,8 +1315,9 @@ int chunk_rows_fixed();
 int sm_count();
 
 bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool banded = false, int max_rows = 64) {
-  // the mean-correction kernel stages 8 output rows' table differences
-  if ((size_t)8 * corr_stage(g.Wl, g.Wr) * sizeof(float) > 200 * 1024) return false;
+  // sizes accepted: Wl + Wr below 6400 (the correction kernel stages
+  // (Wl + 1) + 8 (Wr + 1) floats, well inside 200 KB there)
+  if ((size_t)8 * ((g.Wl + g.Wr + 2 + 3) / 4 * 4) * sizeof(float) > 200 * 1024) return false;
   int P = 1;
   while (P < kLanes && P < pm.K) P *= 2;
   t->P = P;
@@ -1367,7 +1367,7 @@ int env_int(const char* name, int def) {
 // chunk of a right row: 4 K-steps x 3 products) per accumulator.  Measured on
 // zero-mean 256x256 data: windows of 5 rows (240 MMAs) 6.0e-6 of max|out|,
 // 8 rows 8e-6, 12 rows 1.1e-5, 32 rows 3e-5 (the split alone gives ~6e-6).
-// stats_kernel widens it for data whose means dominate.  Every drain stalls
+// The window blocks of colsum_kernel widen it for data whose means dominate.  Every drain stalls
 // the MMAs while the epilogue reads the accumulators.
 // XC_TC_FLUSH_ROWS fixes the window, XC_TC_CHUNK_ROWS the item length (studies).
 int flush_rows(int nkc) { return std::max(1, std::min(32, 240 / (12 * nkc))); }
@@ -1390,7 +1390,6 @@ int sm_count() {
 // Workspace layout (each part 256-byte aligned).
 struct TcWs {
   float* mu;        // n_left + n_right means
-  float* sd;        // n_left + n_right standard deviations
   double* sums;     // n_left + n_right matrix sums
   double* sq;       // n_left + n_right sums of squares
   int* flush;       // n_left x n_pgroups accumulation windows
@@ -1417,7 +1416,6 @@ TcWs ws_layout(void* base, const Geometry& g, const PairMap& pm, const TcPlan& t
     return ptr;
   };
   w.mu = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
-  w.sd = reinterpret_cast<float*>(take(sizeof(float) * (pm.n_left + nr)));
   w.sums = reinterpret_cast<double*>(take(2 * sizeof(double) * (pm.n_left + nr)));
   w.sq = w.sums ? w.sums + (pm.n_left + nr) : nullptr;  // zeroed together with the sums
   w.flush = reinterpret_cast<int*>(take(sizeof(int) * (size_t)pm.n_left * div_up(pm.K, t.P)));
@@ -1519,55 +1517,53 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   const int nl = pm.n_left;
   const uint64_t n_out = (uint64_t)((long long)(nl - 1) * pm.o_l + (long long)(pm.K - 1) * pm.o_k + 1);
 
-  // 1. per-matrix means, 2. column prefix sums of the centred matrices
+  // 1. per-matrix sums; 2. means, column prefix sums of the centred
+  // matrices, the split planes of the centred right matrices and the
+  // accumulation windows (one launch); 3. row scans of the tables
   {
     const long long la = (long long)g.Hl * g.Wl, ra = (long long)g.Hr * g.Wr;
     // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
     // (2048-element slices took 19 us instead of 10 at 64 x 256x256: the
     // blocks' FP64 atomics on one matrix's sum serialise)
     const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
-    const PrepSide sl{left,  g.Hl, g.Wl, la, ls, w.sums,      w.sq,      w.mu,      w.CL, (long long)nl * (g.Hl + 1)};
-    const PrepSide sr{right, g.Hr, g.Wr, ra, rs, w.sums + nl, w.sq + nl, w.mu + nl, w.CR, (long long)nr * (g.Hr + 1)};
+    const PrepSide sl{left,  g.Hl, g.Wl, la, ls, w.sums,      w.sq,      w.mu,      w.CL, (long long)nl * (g.Hl + 1),
+                      nullptr, nullptr, 0, 0};
+    const PrepSide sr{right, g.Hr, g.Wr, ra, rs, w.sums + nl, w.sq + nl, w.mu + nl, w.CR, (long long)nr * (g.Hr + 1),
+                      w.hi, w.lo, t.pitch, tf32 ? 1 : 0};
     XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, 2 * sizeof(double) * (nl + nr), stream));
     sum_kernel<<<(unsigned)(nl * ls + nr * rs), 256, 0, stream>>>(sl, sr, (unsigned)(nl * ls));
     XC_CUDA_TRY(cudaGetLastError());
     const int npg = div_up(pm.K, t.P);
-    const unsigned mean_blocks = (unsigned)((nl + nr + 255) / 256);
-    stats_kernel<<<(unsigned)(mean_blocks + (32LL * nl * npg + 255) / 256), 256, 0, stream>>>(
-        w.sums, w.sq, nl, (double)la, (int)(nl + nr), (double)ra, w.mu, w.sd, mean_blocks, pm, npg, t.P,
-        flush_rows(t.nkc), t.chunk_rows, flush_fixed(), w.flush);
-    XC_CUDA_TRY(cudaGetLastError());
+    const WinArgs wa{w.sums, w.sq, nl, (double)la, (double)ra, pm, npg, t.P, flush_rows(t.nkc), t.chunk_rows,
+                     flush_fixed(), w.flush};
     const unsigned lc = (unsigned)(nl * ((g.Wl + 31) / 32));
-    colsum_kernel<<<(unsigned)(lc + nr * ((g.Wr + 31) / 32)), 256, 0, stream>>>(sl, sr, lc);
+    const unsigned lrc = lc + (unsigned)(nr * ((g.Wr + 31) / 32));
+    // split: blocks of about 2048 chunks of 16 bytes, each within one matrix
+    const long long chunks = (long long)g.Hr * (t.pitch / (16 / t.es));
+    const int bpm = (int)std::max(1LL, std::min(64LL, chunks / 2048));
+    const unsigned split_end = lrc + (unsigned)(nr * bpm);
+    const unsigned wb = (unsigned)((32LL * nl * npg + 255) / 256);
+    if ((long long)split_end + wb > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+    colsum_kernel<<<split_end + wb, 256, 0, stream>>>(sl, sr, lc, lrc, split_end, bpm, wa);
     XC_CUDA_TRY(cudaGetLastError());
     // second pass: every row of the left and of the right tables
     const unsigned lb = (unsigned)((sl.sat_rows + 7) / 8);
     rowscan_kernel<<<(unsigned)(lb + (sr.sat_rows + 7) / 8), 256, 0, stream>>>(sl, sr, lb);
     XC_CUDA_TRY(cudaGetLastError());
   }
-  // 3. split of the centred right matrices
-  {
-    const long long rows = nr * g.Hr;
-    long long blocks = (rows * (t.pitch / (16 / t.es)) + 255) / 256;
-    if (blocks > 152 * 32) blocks = 152 * 32;
-    if (tf32)
-      split_kernel<float><<<(unsigned)blocks, 256, 0, stream>>>(right, w.mu + nl, (float*)w.hi, (float*)w.lo, rows,
-                                                                 g.Hr, g.Wr, t.pitch);
-    else
-      split_kernel<__nv_bfloat16><<<(unsigned)blocks, 256, 0, stream>>>(
-          right, w.mu + nl, (__nv_bfloat16*)w.hi, (__nv_bfloat16*)w.lo, rows, g.Hr, g.Wr, t.pitch);
-    XC_CUDA_TRY(cudaGetLastError());
-  }
   // 4. the mean terms initialise the output
   {
-    const int stage_w = corr_stage(g.Wl, g.Wr);
-    const size_t corr_smem = (size_t)8 * stage_w * sizeof(float);
-    if (corr_smem > 200 * 1024) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths: Wl + Wr above 6400");
+    const int stage_l = corr_stage(g.Wl), stage_r = corr_stage(g.Wr);
+    const size_t corr_smem = (size_t)(stage_l + kCorrPartners * stage_r) * sizeof(float);
+    if (corr_smem > 200 * 1024) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths: right matrices too wide");
     if (corr_smem > 48 * 1024)
       XC_CUDA_TRY(cudaFuncSetAttribute(correction_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
-    const long long n_rows = (long long)n_out * g.Sy;
-    correction_kernel<<<(unsigned)((n_rows + 7) / 8), 256, corr_smem, stream>>>(
-        out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl, g.Hr, g.Wr, g.Sy, g.Sx, n_rows, pm, stage_w);
+    const int n_kgroups = div_up(pm.K, kCorrPartners);
+    const long long n_blocks = (long long)nl * n_kgroups * g.Sy;
+    if (n_blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+    correction_kernel<<<(unsigned)n_blocks, 256, corr_smem, stream>>>(out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl,
+                                                                      g.Hr, g.Wr, g.Sy, g.Sx, pm, n_kgroups, stage_l,
+                                                                      stage_r);
   }
   XC_CUDA_TRY(cudaGetLastError());
 
