@@ -388,12 +388,14 @@ __host__ __device__ __forceinline__ bool tc_piece(const TcParams& p, int part, i
 // idx = ((chunk * n_dytiles + rank) * per_rank + lp) * n_parts + part; false
 // when the item has no left rows.
 __host__ __device__ __forceinline__ bool tc_item(const TcParams& p, long long idx, TcItem* w) {
+  // 32-bit index arithmetic: launches hold fewer than 2^31 items
+  const int i = (int)idx;
   const int per_rank = p.pm.n_left * p.n_pgroups;
-  const int part = (int)(idx % p.n_parts);
-  const long long key = idx / p.n_parts;
-  const int lp = (int)(key % per_rank);
-  const int rank = (int)((key / per_rank) % p.n_dytiles);
-  const int chunk = (int)(key / ((long long)per_rank * p.n_dytiles));
+  const int part = i % p.n_parts;
+  const int key = i / p.n_parts;
+  const int lp = key % per_rank;
+  const int rank = (key / per_rank) % p.n_dytiles;
+  const int chunk = key / (per_rank * p.n_dytiles);
   return tc_piece(p, part, lp, rank, chunk * p.chunk_rows, p.chunk_rows, w);
 }
 
@@ -417,7 +419,8 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
   const int stride = p.chunk_rows + 1, n_keys = p.n_bands * stride;
   for (int r = threadIdx.x; r < n_keys; r += blockDim.x) cnt[r] = 0;
   __syncthreads();
-  for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
+  const int n = (int)n_total;  // fewer than 2^31 items (checked at launch)
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
     TcItem w;
     if (tc_item(p, idx, &w)) atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1);
   }
@@ -432,10 +435,10 @@ __global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long l
     *n_live = run;
   }
   __syncthreads();
-  for (long long idx = threadIdx.x; idx < n_total; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
     TcItem w;
     if (tc_item(p, idx, &w))
-      items[atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1)] = (int)idx;
+      items[atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1)] = idx;
   }
 }
 
@@ -1290,16 +1293,16 @@ __global__ void __launch_bounds__(256) correction_kernel(float* __restrict__ out
   for (int sx = threadIdx.x; sx < Sx; sx += blockDim.x) {
     const int dx = sx - (Wr - 1);
     const int x0 = max(0, dx), x1 = min(Wl, Wr + dx);
-    const int j0 = x0 - dx, j1 = x1 - dx;
     const float area = cy * (float)(x1 - x0);
     const float sl = dl[x1] - dl[x0];
+    const float* dr0 = stage_all + stage_l + (x0 - dx);  // D_R[j0] of partner 0
+    const int span = x1 - x0;                             // j1 - j0
+    float* o = o0 + sx;
 #pragma unroll
     for (int w = 0; w < kCorrPartners; ++w) {
-      if (w < n_here) {
-        const float* dr = stage_all + stage_l + w * stage_r;
-        const float sr = dr[j1] - dr[j0];
-        o0[w * ostep + sx] = fmaf(cr[w], sl, fmaf(cl, sr, clr[w] * area));
-      }
+      if (w < n_here) *o = fmaf(cr[w], sl, fmaf(cl, dr0[span] - dr0[0], clr[w] * area));
+      dr0 += stage_r;
+      o += ostep;
     }
   }
 }
