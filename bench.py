@@ -851,9 +851,9 @@ def reference_gpu_study(torch, xcorr, line, reps=10):
 
 def gpu_launches(method, steps):
     # kernels per xc_correlate call: direct 1; fft 2 pads + multiply + normalise
-    # (+ cuFFT's own); tc: sums, means and accumulation windows, column sums,
-    # row scans (each over both sides), split, correction, work list, tcgen05 kernel
-    per_step = {"direct": 1, "fft": 4, "tc_bf16x3": 8, "tc_tf32x3": 8}.get(method, 1)
+    # (+ cuFFT's own); tc: sums; column sums with the means, split planes,
+    # accumulation windows and work list; row scans; correction; tcgen05 kernel
+    per_step = {"direct": 1, "fft": 4, "tc_bf16x3": 5, "tc_tf32x3": 5}.get(method, 1)
     return per_step * steps
 
 

@@ -409,17 +409,16 @@ __host__ __device__ __forceinline__ bool tc_entry(const TcParams& p, int4 e, TcI
 }
 
 // Lists the non-empty work items by output row band (in the order
-// band_rank gives), then most left rows first (a counting sort): one block.
-// Every CTA of tc_kernel reads the same list.
-__global__ void __launch_bounds__(1024) worklist_kernel(const TcParams p, long long n_total, int* __restrict__ items,
-                                                        int* __restrict__ n_live) {
+// band_rank gives), then most left rows first (a counting sort): one block,
+// `cnt` a shared array of n_bands * (chunk_rows + 1) ints.  Every CTA of
+// tc_kernel reads the same list.
+__device__ __forceinline__ void worklist_block(const TcParams& p, int n, int* __restrict__ items,
+                                               int* __restrict__ n_live, int* cnt) {
   // key = rank * (chunk_rows + 1) + (chunk_rows - rows): band first, then
   // the longest items
-  __shared__ int cnt[kMaxBands * (kMaxChunkRows + 1)];
   const int stride = p.chunk_rows + 1, n_keys = p.n_bands * stride;
   for (int r = threadIdx.x; r < n_keys; r += blockDim.x) cnt[r] = 0;
   __syncthreads();
-  const int n = (int)n_total;  // fewer than 2^31 items (checked at launch)
   for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
     TcItem w;
     if (tc_item(p, idx, &w)) atomicAdd(&cnt[p.band_rank[w.band] * stride + p.chunk_rows - w.n_rows], 1);
@@ -945,10 +944,10 @@ __device__ __forceinline__ void sum_block(const PrepSide& sd_, int b) {
   // on this GPU), FP64 across threads and blocks
   float part = 0.0f, part2 = 0.0f;
   if ((area & 3) == 0 && (per & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
-    // float4 loads, four in flight per thread
+    // float4 loads, eight in flight per thread (a slice is 8 per thread)
     const float4* a4 = reinterpret_cast<const float4*>(a);
     const long long lo4 = lo >> 2, hi4 = hi >> 2;
-#pragma unroll 4
+#pragma unroll 8
     for (long long i = lo4 + threadIdx.x; i < hi4; i += blockDim.x) {
       const float4 x = __ldg(a4 + i);
       part += (x.x + x.y) + (x.z + x.w);
@@ -1161,24 +1160,35 @@ __device__ __forceinline__ void colsum_block(const PrepSide& sd_, int b) {
   }
 }
 
-// One block per (matrix, 32-column strip) of either side (which also writes
-// the means), then the blocks of the right side's split planes, then those
-// of the accumulation windows: four independent jobs in one launch, the
-// split filling the SMs the latency-bound column sums leave idle.
+// The work list (block 0, unless the launch is banded: its schedule comes
+// from the host), then one block per (matrix, 32-column strip) of either
+// side (which also writes the means), then the blocks of the right side's
+// split planes, then those of the accumulation windows: independent jobs in
+// one launch, the split filling the SMs the latency-bound column sums leave
+// idle and the work list's serial steps hidden under both.
 __global__ void __launch_bounds__(256) colsum_kernel(const PrepSide a, const PrepSide b, unsigned a_blocks,
                                                      unsigned ab_blocks, unsigned split_end, int split_bpm,
-                                                     const WinArgs wa) {
-  if (blockIdx.x < a_blocks)
-    colsum_block(a, (int)blockIdx.x);
-  else if (blockIdx.x < ab_blocks)
-    colsum_block(b, (int)(blockIdx.x - a_blocks));
-  else if (blockIdx.x < split_end) {
+                                                     const WinArgs wa, const TcParams p, int list, int n_items,
+                                                     int* items, int* n_live) {
+  extern __shared__ int wl_cnt[];  // the work list's counts (its block only)
+  if (list) {
+    if (blockIdx.x == 0) {
+      worklist_block(p, n_items, items, n_live, wl_cnt);
+      return;
+    }
+  }
+  const unsigned bid = blockIdx.x - (list ? 1u : 0u);
+  if (bid < a_blocks)
+    colsum_block(a, (int)bid);
+  else if (bid < ab_blocks)
+    colsum_block(b, (int)(bid - a_blocks));
+  else if (bid < split_end) {
     if (b.split_tf32)
-      split_block<float>(b, (int)(blockIdx.x - ab_blocks), split_bpm);
+      split_block<float>(b, (int)(bid - ab_blocks), split_bpm);
     else
-      split_block<__nv_bfloat16>(b, (int)(blockIdx.x - ab_blocks), split_bpm);
+      split_block<__nv_bfloat16>(b, (int)(bid - ab_blocks), split_bpm);
   } else {
-    window_block(wa, blockIdx.x - split_end);
+    window_block(wa, bid - split_end);
   }
 }
 
@@ -1520,56 +1530,6 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   const int nl = pm.n_left;
   const uint64_t n_out = (uint64_t)((long long)(nl - 1) * pm.o_l + (long long)(pm.K - 1) * pm.o_k + 1);
 
-  // 1. per-matrix sums; 2. means, column prefix sums of the centred
-  // matrices, the split planes of the centred right matrices and the
-  // accumulation windows (one launch); 3. row scans of the tables
-  {
-    const long long la = (long long)g.Hl * g.Wl, ra = (long long)g.Hr * g.Wr;
-    // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
-    // (2048-element slices took 19 us instead of 10 at 64 x 256x256: the
-    // blocks' FP64 atomics on one matrix's sum serialise)
-    const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
-    const PrepSide sl{left,  g.Hl, g.Wl, la, ls, w.sums,      w.sq,      w.mu,      w.CL, (long long)nl * (g.Hl + 1),
-                      nullptr, nullptr, 0, 0};
-    const PrepSide sr{right, g.Hr, g.Wr, ra, rs, w.sums + nl, w.sq + nl, w.mu + nl, w.CR, (long long)nr * (g.Hr + 1),
-                      w.hi, w.lo, t.pitch, tf32 ? 1 : 0};
-    XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, 2 * sizeof(double) * (nl + nr), stream));
-    sum_kernel<<<(unsigned)(nl * ls + nr * rs), 256, 0, stream>>>(sl, sr, (unsigned)(nl * ls));
-    XC_CUDA_TRY(cudaGetLastError());
-    const int npg = div_up(pm.K, t.P);
-    const WinArgs wa{w.sums, w.sq, nl, (double)la, (double)ra, pm, npg, t.P, flush_rows(t.nkc), t.chunk_rows,
-                     flush_fixed(), w.flush};
-    const unsigned lc = (unsigned)(nl * ((g.Wl + 31) / 32));
-    const unsigned lrc = lc + (unsigned)(nr * ((g.Wr + 31) / 32));
-    // split: blocks of about 2048 chunks of 16 bytes, each within one matrix
-    const long long chunks = (long long)g.Hr * (t.pitch / (16 / t.es));
-    const int bpm = (int)std::max(1LL, std::min(64LL, chunks / 2048));
-    const unsigned split_end = lrc + (unsigned)(nr * bpm);
-    const unsigned wb = (unsigned)((32LL * nl * npg + 255) / 256);
-    if ((long long)split_end + wb > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
-    colsum_kernel<<<split_end + wb, 256, 0, stream>>>(sl, sr, lc, lrc, split_end, bpm, wa);
-    XC_CUDA_TRY(cudaGetLastError());
-    // second pass: every row of the left and of the right tables
-    const unsigned lb = (unsigned)((sl.sat_rows + 7) / 8);
-    rowscan_kernel<<<(unsigned)(lb + (sr.sat_rows + 7) / 8), 256, 0, stream>>>(sl, sr, lb);
-    XC_CUDA_TRY(cudaGetLastError());
-  }
-  // 4. the mean terms initialise the output
-  {
-    const int stage_l = corr_stage(g.Wl), stage_r = corr_stage(g.Wr);
-    const size_t corr_smem = (size_t)(stage_l + kCorrPartners * stage_r) * sizeof(float);
-    if (corr_smem > 200 * 1024) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths: right matrices too wide");
-    if (corr_smem > 48 * 1024)
-      XC_CUDA_TRY(cudaFuncSetAttribute(correction_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
-    const int n_kgroups = div_up(pm.K, kCorrPartners);
-    const long long n_blocks = (long long)nl * n_kgroups * g.Sy;
-    if (n_blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
-    correction_kernel<<<(unsigned)n_blocks, 256, corr_smem, stream>>>(out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl,
-                                                                      g.Hr, g.Wr, g.Sy, g.Sx, pm, n_kgroups, stage_l,
-                                                                      stage_r);
-  }
-  XC_CUDA_TRY(cudaGetLastError());
-
   CUtensorMap mhi, mlo;
   {
     const uint64_t es = (uint64_t)t.es, mat = (uint64_t)t.pitch * g.Hr * es;
@@ -1617,6 +1577,10 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   prm.flags = device_flags();
 
   const long long n_list = t.n_items;
+  if (n_list > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+  prm.items = w.items;
+  prm.sched = nullptr;
+  prm.n_live = w.items + t.n_items;  // written by the work list (unbanded)
 
   // Output row bands (one unless banded); a banded launch's pieces per band
   // come with its schedule below
@@ -1637,14 +1601,65 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
     }
   }
 
-  if (t.n_items > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+  // 1. per-matrix sums; 2. means, column prefix sums of the centred
+  // matrices, the split planes of the centred right matrices and the
+  // accumulation windows (one launch); 3. row scans of the tables
+  {
+    const long long la = (long long)g.Hl * g.Wl, ra = (long long)g.Hr * g.Wr;
+    // slices of at most 8192 elements: a thread adds at most 32 terms in FP32
+    // (2048-element slices took 19 us instead of 10 at 64 x 256x256: the
+    // blocks' FP64 atomics on one matrix's sum serialise)
+    const int ls = (int)((la + 8191) / 8192), rs = (int)((ra + 8191) / 8192);
+    const PrepSide sl{left,  g.Hl, g.Wl, la, ls, w.sums,      w.sq,      w.mu,      w.CL, (long long)nl * (g.Hl + 1),
+                      nullptr, nullptr, 0, 0};
+    const PrepSide sr{right, g.Hr, g.Wr, ra, rs, w.sums + nl, w.sq + nl, w.mu + nl, w.CR, (long long)nr * (g.Hr + 1),
+                      w.hi, w.lo, t.pitch, tf32 ? 1 : 0};
+    XC_CUDA_TRY(cudaMemsetAsync(w.sums, 0, 2 * sizeof(double) * (nl + nr), stream));
+    sum_kernel<<<(unsigned)(nl * ls + nr * rs), 256, 0, stream>>>(sl, sr, (unsigned)(nl * ls));
+    XC_CUDA_TRY(cudaGetLastError());
+    const int npg = div_up(pm.K, t.P);
+    const WinArgs wa{w.sums, w.sq, nl, (double)la, (double)ra, pm, npg, t.P, flush_rows(t.nkc), t.chunk_rows,
+                     flush_fixed(), w.flush};
+    const unsigned lc = (unsigned)(nl * ((g.Wl + 31) / 32));
+    const unsigned lrc = lc + (unsigned)(nr * ((g.Wr + 31) / 32));
+    // split: blocks of about 2048 chunks of 16 bytes, each within one matrix
+    const long long chunks = (long long)g.Hr * (t.pitch / (16 / t.es));
+    const int bpm = (int)std::max(1LL, std::min(64LL, chunks / 2048));
+    const unsigned split_end = lrc + (unsigned)(nr * bpm);
+    const unsigned wb = (unsigned)((32LL * nl * npg + 255) / 256);
+    if ((long long)split_end + wb + 1 > 0x7fffffffLL)
+      return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+    const int list = band_done == nullptr ? 1 : 0;
+    const size_t list_smem = list ? sizeof(int) * (size_t)prm.n_bands * (t.chunk_rows + 1) : 0;
+    colsum_kernel<<<split_end + wb + (unsigned)list, 256, list_smem, stream>>>(
+        sl, sr, lc, lrc, split_end, bpm, wa, prm, list, (int)n_list, w.items, w.items + t.n_items);
+    XC_CUDA_TRY(cudaGetLastError());
+    // second pass: every row of the left and of the right tables
+    const unsigned lb = (unsigned)((sl.sat_rows + 7) / 8);
+    rowscan_kernel<<<(unsigned)(lb + (sr.sat_rows + 7) / 8), 256, 0, stream>>>(sl, sr, lb);
+    XC_CUDA_TRY(cudaGetLastError());
+  }
+  // 4. the mean terms initialise the output
+  {
+    const int stage_l = corr_stage(g.Wl), stage_r = corr_stage(g.Wr);
+    const size_t corr_smem = (size_t)(stage_l + kCorrPartners * stage_r) * sizeof(float);
+    if (corr_smem > 200 * 1024) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths: right matrices too wide");
+    if (corr_smem > 48 * 1024)
+      XC_CUDA_TRY(cudaFuncSetAttribute(correction_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
+    const int n_kgroups = div_up(pm.K, kCorrPartners);
+    const long long n_blocks = (long long)nl * n_kgroups * g.Sy;
+    if (n_blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
+    correction_kernel<<<(unsigned)n_blocks, 256, corr_smem, stream>>>(out, w.CL, w.CR, w.mu, w.mu + nl, g.Hl, g.Wl,
+                                                                      g.Hr, g.Wr, g.Sy, g.Sx, pm, n_kgroups, stage_l,
+                                                                      stage_r);
+  }
+  XC_CUDA_TRY(cudaGetLastError());
+
   // persistent: one CTA per SM (about 205 KB of shared memory and all 512 TMEM
   // columns each), walking the list in snake order
   auto kern = tf32 ? tc_kernel<true> : tc_kernel<false>;
   XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
   const long long blocks = std::max(1LL, std::min<long long>(n_list, sm_count()));
-  prm.items = w.items;
-  prm.sched = nullptr;
   if (band_done) {
     // banded: the host deals the items out to the CTAs by least work
     if (blocks > sm_count()) return fail(XC_ERR_WORKSPACE, "banded launch wider than its schedule space");
@@ -1654,11 +1669,6 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
     prm.sched = reinterpret_cast<const int4*>(w.sched) + 1;
     if (bands)
       for (int k = 0; k < prm.n_bands; ++k) bands->items[k] = band_items[k];
-  } else {
-    // the work list: non-empty items, most left rows first, built on the device
-    prm.n_live = w.items + t.n_items;
-    worklist_kernel<<<1, 1024, 0, stream>>>(prm, n_list, w.items, w.items + t.n_items);
-    XC_CUDA_TRY(cudaGetLastError());
   }
   const int slot = kernel_timer_begin(stream);
   kern<<<(unsigned)blocks, kThreads, (size_t)t.smem_bytes, stream>>>(mhi, mlo, prm);
