@@ -49,3 +49,30 @@ def run_sharded(n_outputs: int, costs: Sequence[int], compute: Callable[[List[in
         for i, r in zip(idx, res):
             full[i] = r
     return full
+
+
+def correlate_pairs_sharded(lefts, rights, rank: int, world_size: int, group=None, dtype: str = "f32") -> list:
+    """Correlations of the pairs (lefts[i], rights[i]) split over the ranks of
+    a process group: each rank runs its cost-balanced share as one ragged
+    plan (xcorr.RaggedPlan: one persistent launch under a CUDA graph) on its
+    current CUDA device, and every rank returns the full, ordered list of
+    output arrays."""
+    import torch
+
+    from . import RaggedPlan
+
+    costs = [pair_cost(l.shape, r.shape) for l, r in zip(lefts, rights)]
+
+    def compute(idx):
+        if not idx:
+            return []
+        plan = RaggedPlan([lefts[i] for i in idx], [rights[i] for i in idx], [(k, k) for k in range(len(idx))],
+                          dtype)
+        try:
+            plan.execute()
+            torch.cuda.synchronize()
+            return plan.outputs()
+        finally:
+            plan.close()
+
+    return run_sharded(len(lefts), costs, compute, rank, world_size, group)
