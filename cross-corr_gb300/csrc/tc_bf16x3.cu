@@ -102,7 +102,6 @@ namespace {
 
 constexpr int kLanes = 128;                // A rows per MMA: P partners x DY row shifts
 constexpr int kStageBytes = kLanes * 128;  // one plane of one 128-byte column chunk
-constexpr int kHalfCols = 256;             // tensor-memory columns per shift half
 constexpr int kBuilderWarps = 4;
 constexpr int kEpiWarps = 16;              // four per TMEM lane quadrant, all draining each half
 // warp 0 producer, warps 1 and 22 MMA issuers (one per shift half), 2-5
@@ -125,7 +124,7 @@ template <bool TF>
 struct TcCfg {
   static constexpr int kStages = TF ? 4 : 5;
   static constexpr int kCm = TF ? 4 : 8;            // elements per 16-byte core-matrix row
-  static constexpr int kQ = TF ? 194 : 98;          // core matrices in T
+  static constexpr int kQ = TF ? kTQTf32 : kTQBf16;  // core matrices in T
   static constexpr int kTBytes = kQ * 128;          // one plane of T
   static constexpr int kTransW = TF ? 16 : 32;
   static constexpr int kTransBytes = kEpiWarps * 32 * (kTransW + 1) * 4;
@@ -324,32 +323,11 @@ __device__ __forceinline__ bool bar_red_or(bool v, int id, int nthreads) {
   return r != 0;
 }
 
-// The MMA window of half h and the K-step whose first right column is k0,
-// in the x-part starting at shift s0 and the k-part starting at column
-// kbase: the shifts sx whose left columns sx + k - (Wr-1) meet the row for
-// some column k of the K-step, clipped to the half and rounded out to 16.
-// Packed: TMEM column (bits 0-8), N / 16 (9-13), active (14), and the core
-// matrix of the Toeplitz buffer the MMA's B operand starts at (16-23): the
-// item's staged row is X[i] = Lp[s0 + kbase + i], so B[n][k] = Lp[w0 + n +
-// k0 + k] starts at X[w0 - s0 + k0 - kbase].  kreset = true: the whole half
-// from the part's first column (the first MMA of a window, which also
-// starts every accumulator column afresh).
-__host__ __device__ __forceinline__ uint32_t pack_window(int dcol, int n, bool active, int bq) {
-  return (uint32_t)dcol | ((uint32_t)(n / 16) << 9) | ((active ? 1u : 0u) << 14) | ((uint32_t)bq << 16);
-}
-
+// The MMA window of half h and the K-step whose first right column is k0
+// (window_of in tc_schedule.h) for this launch's geometry.
 __host__ __device__ __forceinline__ uint32_t kstep_window(const TcParams& p, int s0, int kbase, int h, int k0,
                                                           bool reset) {
-  const int cm = p.kstep == 16 ? 8 : 4;
-  const int H0 = s0 + h * p.half_w, H1 = min(p.Sx, H0 + p.half_w);
-  if (reset) return pack_window(h * kHalfCols, p.half_w, true, (H0 - s0) / cm);
-  if (k0 >= p.Wr || H0 >= H1) return 0;
-  const int k_hi = min(k0 + p.kstep, p.Wr) - 1;
-  const int lo = max(H0, p.Wr - 1 - k_hi), hi = min(H1, p.Wr - 1 + p.Wl - k0);
-  if (lo >= hi) return 0;
-  const int w0 = H0 + (lo - H0) / 16 * 16;
-  const int n = (hi - w0 + 15) / 16 * 16;
-  return pack_window(h * kHalfCols + (w0 - H0), n, true, (w0 - s0 + k0 - kbase) / cm);
+  return window_of(p.Sx, p.Wl, p.Wr, p.half_w, p.kstep, s0, kbase, h, k0, reset);
 }
 
 // One work item: every shift of one (left matrix, partner group, row-shift
@@ -1337,13 +1315,13 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool ba
   t->DY = kLanes / P;
   t->mats_mode = P >= 8 ? 1 : 0;
   // x-parts of 512 shifts (two halves), k-parts of 256 right columns
-  t->half_w = g.Sx > 512 ? 256 : ((g.Sx + 1) / 2 + 15) / 16 * 16;
-  t->n_kparts = (g.Wr + 255) / 256;
-  t->n_parts = ((g.Sx + 511) / 512) * t->n_kparts;
+  const TcParts parts = tc_parts(g.Sx, g.Wr, tf32);
+  t->half_w = parts.half_w;
+  t->n_kparts = parts.n_kparts;
+  t->n_parts = parts.n_xparts * parts.n_kparts;
   t->es = tf32 ? 4 : 2;                 // bytes per operand element
-  t->kstep = tf32 ? 8 : 16;             // columns per MMA K-step (32 bytes)
-  const int chunk = 128 / t->es;        // columns per 128-byte TMA box row
-  t->nkc = (std::min(g.Wr, 256) + chunk - 1) / chunk;
+  t->kstep = parts.kstep;               // columns per MMA K-step (32 bytes)
+  t->nkc = parts.nkc;                   // 128-byte column chunks of a k-part
   t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
   // left rows per item: at most 64, fewer when that leaves fewer than two
   // items per SM (small problems), at least 4.  Longer items end fewer
@@ -1528,7 +1506,6 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   const TcWs w = ws_layout(reinterpret_cast<void*>(((uintptr_t)workspace + 255) & ~uintptr_t(255)), g, pm, t);
   const long long nr = n_right_of(pm);
   const int nl = pm.n_left;
-  const uint64_t n_out = (uint64_t)((long long)(nl - 1) * pm.o_l + (long long)(pm.K - 1) * pm.o_k + 1);
 
   CUtensorMap mhi, mlo;
   {

@@ -1,10 +1,13 @@
 // Work planning of the split tensor-core kernel that needs no device: the
-// row-shift tile visiting order and the host-built schedule of a banded launch
-// (output copied out band by band while the kernel runs).  Header-only so that
-// the CUDA source and a plain C++ test harness compile the same code.
+// shift and column parts of an output and the MMA windows of their K-steps,
+// the row-shift tile visiting order and the host-built schedule of a banded
+// launch (output copied out band by band while the kernel runs).
+// Header-only so that the CUDA source and plain C++ test harnesses compile
+// the same code.
 #pragma once
 
 #include <algorithm>
+#include <cstdint>
 #include <cmath>
 #include <functional>
 #include <queue>
@@ -18,6 +21,55 @@
 #endif
 
 namespace xc {
+
+// Shift and column parts of one output: x-parts of 512 shifts, each two
+// halves of half_w shifts (tensor-memory columns [0, 256) and [256, 512)),
+// and k-parts of 256 right columns; K-steps of 16 (BF16) or 8 (TF32)
+// columns, in 128-byte chunks of 64 or 32 columns.
+constexpr int kHalfCols = 256;                   // tensor-memory columns per shift half
+constexpr int kTQBf16 = 98, kTQTf32 = 194;       // core matrices of the Toeplitz buffer
+struct TcParts {
+  int half_w, n_xparts, n_kparts, kstep, nkc;
+};
+inline TcParts tc_parts(int Sx, int Wr, bool tf32) {
+  TcParts t;
+  t.half_w = Sx > 512 ? 256 : ((Sx + 1) / 2 + 15) / 16 * 16;
+  t.n_xparts = (Sx + 511) / 512;
+  t.n_kparts = (Wr + 255) / 256;
+  t.kstep = tf32 ? 8 : 16;
+  const int chunk = tf32 ? 32 : 64;
+  t.nkc = ((Wr < 256 ? Wr : 256) + chunk - 1) / chunk;
+  return t;
+}
+
+// The MMA window of half h and the K-step whose first right column is k0,
+// in the x-part starting at shift s0 and the k-part starting at column
+// kbase: the shifts sx whose left columns sx + k - (Wr-1) meet the row for
+// some column k of the K-step, clipped to the half and rounded out to 16.
+// Packed: TMEM column (bits 0-8), N / 16 (9-13), active (14), and the core
+// matrix of the Toeplitz buffer the MMA's B operand starts at (16-23): the
+// item's staged row is X[i] = Lp[s0 + kbase + i], so B[n][k] = Lp[w0 + n +
+// k0 + k] starts at X[w0 - s0 + k0 - kbase].  reset = true: the whole half
+// from the part's first column (the first MMA of a window, which also
+// starts every accumulator column afresh).
+XC_HD uint32_t pack_window(int dcol, int n, bool active, int bq) {
+  return (uint32_t)dcol | ((uint32_t)(n / 16) << 9) | ((active ? 1u : 0u) << 14) | ((uint32_t)bq << 16);
+}
+XC_HD uint32_t window_of(int Sx, int Wl, int Wr, int half_w, int kstep, int s0, int kbase, int h, int k0,
+                         bool reset) {
+  const int cm = kstep == 16 ? 8 : 4;
+  const int H0 = s0 + h * half_w;
+  const int H1 = Sx < H0 + half_w ? Sx : H0 + half_w;
+  if (reset) return pack_window(h * kHalfCols, half_w, true, (H0 - s0) / cm);
+  if (k0 >= Wr || H0 >= H1) return 0;
+  const int k_hi = (k0 + kstep < Wr ? k0 + kstep : Wr) - 1;
+  const int lo = H0 > Wr - 1 - k_hi ? H0 : Wr - 1 - k_hi;
+  const int hi = H1 < Wr - 1 + Wl - k0 ? H1 : Wr - 1 + Wl - k0;
+  if (lo >= hi) return 0;
+  const int w0 = H0 + (lo - H0) / 16 * 16;
+  const int n = (hi - w0 + 15) / 16 * 16;
+  return pack_window(h * kHalfCols + (w0 - H0), n, true, (w0 - s0 + k0 - kbase) / cm);
+}
 
 // dy-tile visiting order: centre (heaviest overlap) first, then alternating
 // outwards, so long tiles start early.
