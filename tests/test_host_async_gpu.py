@@ -36,13 +36,16 @@ PROBLEMS = [
     ("one_to_many", "tc_bf16x3", 1, 18, 240, (256, 250), 64),
     ("n_to_mn", "tc_tf32x3", 2, 16, 200, (210, 220), 65),
     ("one_to_one", "auto", 1, 1, 70, (70, 70), 66),
+    ("n_to_m", "direct", 2, 3, 40, (36, 44), 67, np.float64),
+    ("n_to_mn", "fft", 2, 4, 64, (64, 64), 68, np.float64),
 ]
 
 
 def make(problem):
-    mode, method, n_l, n_r, side, rshape, seed = problem
-    left = seeded((n_l, side, side), seed)
-    right = seeded((n_r,) + rshape, seed + 100)
+    mode, method, n_l, n_r, side, rshape, seed = problem[:7]
+    dtype = problem[7] if len(problem) > 7 else np.float32
+    left = seeded((n_l, side, side), seed, dtype=dtype)
+    right = seeded((n_r,) + rshape, seed + 100, dtype=dtype)
     return mode, method, left, right
 
 
@@ -53,7 +56,7 @@ def test_stream_of_problems_matches_the_synchronous_call():
         mode, method, left, right = make(p)
         hl, tl = pinned(left)
         hr, tr = pinned(right)
-        ho, to = pinned(np.full(out_shape(mode, left, right), np.nan, np.float32))
+        ho, to = pinned(np.full(out_shape(mode, left, right), np.nan, left.dtype))
         keep += [tl, tr, to]
         calls.append((mode, method, left, right, ho, xcorr.correlate_host_async(mode, hl, hr, ho, method=method)))
     # wait newest first: the older calls were completed by the later ones
@@ -65,9 +68,13 @@ def test_stream_of_problems_matches_the_synchronous_call():
         assert rel_to_max(ho, ref) <= 4e-6, (mode, method)
         k = min(2, ho.shape[0])  # the oracle on the first outputs
         pairs = [oracle.pair_of_output(mode, left.shape[0], right.shape[0], o) for o in range(k)]
-        exact = oracle.run_pairs([left[a] for a, _ in pairs], [right[b] for _, b in pairs], threads=8)
+        f64 = left.dtype == np.float64
+        exact = oracle.run_pairs([left[a] for a, _ in pairs], [right[b] for _, b in pairs],
+                                 dtype="f64" if f64 else "f32acc64", threads=8)
         for o in range(k):
-            assert rel_to_max(ho[o], exact[o]) <= 1e-5, (mode, method, o)
+            # FP64 bounds of the parity tests: 1e-12 (plain kernel), 1e-10 (FFT)
+            tol = (1e-10 if method == "fft" else 1e-12) if f64 else 1e-5
+            assert rel_to_max(ho[o], exact[o]) <= tol, (mode, method, o)
 
 
 def test_pipeline_reuses_each_slot_for_the_same_problem():
