@@ -144,3 +144,23 @@ def test_release_waits_for_calls_in_flight():
     ref = xcorr.correlate_host(mode, left, right, method=method)
     for ho, _ in outs:
         assert rel_to_max(ho, ref) <= 4e-6
+
+
+def test_synchronous_calls_between_stream_calls():
+    """A synchronous host-buffer call in the middle of a stream (default
+    stream, as the Python helpers pass it) completes the calls before it as
+    needed and leaves the later ones correct."""
+    mode, method, left, right = make(PROBLEMS[1])
+    hl, _tl = pinned(left)
+    hr, _tr = pinned(right)
+    ref = xcorr.correlate_host(mode, left, right, method=method)
+    outs = [pinned(np.full(out_shape(mode, left, right), np.nan, np.float32)) for _ in range(3)]
+    t0 = xcorr.correlate_host_async(mode, hl, hr, outs[0][0], method=method)
+    mid = xcorr.correlate_host(mode, left, right, method="fft")
+    t1 = xcorr.correlate_host_async(mode, hl, hr, outs[1][0], method=method)
+    t2 = xcorr.correlate_host_async(mode, hl, hr, outs[2][0], method=method)
+    for t in (t0, t1, t2):
+        xcorr.host_wait(t)
+    for ho, _ in outs:
+        assert rel_to_max(ho, ref) <= 1e-6
+    assert rel_to_max(mid, ref) <= 1e-5
