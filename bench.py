@@ -411,6 +411,15 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "gpu_launches": gpu_launches(method, args.steps),
     }
+    if method == "fft":
+        # the step is two cuFFT transforms around four glue kernels: the
+        # transforms are the library's, timed but not modelled; the glue
+        # kernels' HBM fractions come from their own captures
+        line["roofline"] = {"bound": "hbm", "achieved": None, "peak": float(peaks.get("hbm_gbs", 6800.0)),
+                            "unit": "GB/s", "frac": None, "traffic": None, "kernel": "fft step",
+                            "note": "cuFFT transforms plus pad, conj-multiply and normalise kernels; the glue "
+                                    "kernels' achieved GB/s against this peak are in "
+                                    "profiles/fft_glue_one_to_many_256x64.md"}
     if plain is not None:
         line["plain_fp32"] = plain
     if tf32 is not None:
