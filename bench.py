@@ -595,8 +595,10 @@ def large_fft_study(torch, xcorr, reps=5):
 
 def ragged_study(torch, xcorr, reps=5):
     """Ragged n_to_m batch (512 pairs, every side drawn from U{16..512}, values
-    U[-1,1), seed 4): the persistent, graph-captured plan with its autotuned
-    tile shape against one plain-kernel launch per pair, on one stream and
+    U[-1,1), seed 4): the graph-captured plan with its autotuned variant (tile
+    shape of the persistent plain kernel, and the pairs routed to the
+    split-BF16 path) against the same plan with every pair on the plain
+    kernel, and against one plain-kernel launch per pair, on one stream and
     round-robin over 8 streams (the reference's driver).  The CPU oracle
     checks the 24 smallest and the 8 largest pairs (about 270 GMAC, run in a
     background thread while the GPU timings run)."""
@@ -625,7 +627,8 @@ def ragged_study(torch, xcorr, reps=5):
     worker = threading.Thread(target=run_oracle)
     worker.start()
     plan = xcorr.RaggedPlan(lefts, rights, pairs)
-    shape, tune_ms = plan.autotune()
+    variant, tune_ms = plan.autotune()
+    chosen = plan.describe()
     base = torch.zeros_like(plan.out)
 
     def timed(fn):
@@ -639,6 +642,11 @@ def ragged_study(torch, xcorr, reps=5):
         e1.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    # the chosen variant's tile shape with every pair on the plain kernel
+    plan.select(chosen["tile_shape"])
+    ms_plain = timed(plan.execute)
+    plain_outs = plan.outputs()
+    plan.select(variant)
     ms_graph = timed(plan.execute)
     ms_pairs = timed(lambda: plan.per_pair(base))
     base8 = torch.zeros_like(plan.out)
@@ -650,12 +658,16 @@ def ragged_study(torch, xcorr, reps=5):
     err = max(oracle.max_rel_to_max(outs[i], refs[i]) for i in small)
     err_large = max(oracle.max_rel_to_max(outs[i], refs[i]) for i in large)
     err_large_pp = max(oracle.max_rel_to_max(outs_b[i], refs[i]) for i in large)
+    err_plain = max(oracle.max_rel_to_max(plain_outs[i], refs[i]) for i in checked)
     flops = sum(2.0 * l.size * r.size for l, r in zip(lefts, rights))
     plan.close()
     return {"pairs": 512, "sides": "U{16..512} each of Hl, Wl, Hr, Wr", "values": "U[-1,1)", "seed": 4,
             "persistent_graph_ms": ms_graph, "per_pair_launches_ms": ms_pairs, "speedup": ms_pairs / ms_graph,
             "per_pair_launches_8_streams_ms": ms_streams, "speedup_vs_8_streams": ms_streams / ms_graph,
-            "autotuned_tile_shape": shape, "autotune_ms": tune_ms,
+            "autotuned_variant": chosen, "autotune_ms": tune_ms,
+            "plain_kernel_only": {"ms": ms_plain, "tflops": flops / (ms_plain / 1000.0) / 1e12,
+                                  "max_rel_err_vs_oracle_32_checked_pairs": err_plain,
+                                  "speedup_of_chosen_variant": ms_plain / ms_graph},
             "correlations_per_s": 512 / (ms_graph / 1000.0), "tflops": flops / (ms_graph / 1000.0) / 1e12,
             "max_rel_err_vs_oracle_24_smallest_pairs": err,
             "max_rel_err_vs_oracle_8_largest_pairs": err_large,

@@ -19,9 +19,6 @@
 
 namespace xc {
 const char* last_error_cstr();
-xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows = 64);
-size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32);
 }  // namespace xc
 
 using namespace xc;
@@ -1008,6 +1005,16 @@ xc_status xc_ragged_autotune(xc_ragged_plan plan, void* stream, int* chosen_shap
   if (plan == nullptr || chosen_shape == nullptr || best_ms == nullptr)
     return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
   return ragged_autotune(plan->impl, as_stream(stream), chosen_shape, best_ms);
+}
+
+xc_status xc_ragged_describe(xc_ragged_plan plan, int variant, xc_ragged_variant* out) {
+  if (plan == nullptr || out == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "NULL argument");
+  return ragged_describe(plan->impl, variant, out);
+}
+
+xc_status xc_ragged_select(xc_ragged_plan plan, int variant) {
+  if (plan == nullptr) return fail(XC_ERR_INVALID_ARGUMENT, "plan is NULL");
+  return ragged_select(plan->impl, variant);
 }
 
 xc_status xc_ragged_execute(xc_ragged_plan plan, void* stream) {

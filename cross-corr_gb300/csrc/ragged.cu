@@ -8,12 +8,19 @@
 //    tensor map per matrix;
 //  * the list of output tiles of every pair, sorted by estimated work
 //    (heaviest first), for each candidate tile shape;
-//  * a CUDA graph per tile shape holding the whole step: repack the inputs
+//  * a CUDA graph per variant holding the whole step: repack the inputs
 //    into the padded copies, reset the tile queue, one persistent launch of
 //    the plain kernel whose CTAs pull tiles from the queue until it is empty.
-// Executing the plan replays the graph.  The autotuner times every candidate
-// tile shape on the plan's own batch, keeps the fastest and remembers the
-// choice in a small JSON-lines cache keyed by the batch's signature.
+// A variant is a tile shape of the plain kernel and, for FP32 batches, a
+// route: the pairs with at least the route's multiply-add count run instead
+// as one_to_one calls of the split-BF16 tensor-core path, dealt out over
+// kTcStreams side streams (longest first, each to the least loaded stream)
+// and captured into the same graph, beside the plain kernel's branch.  Route
+// 0 keeps every pair on the plain kernel.
+// Executing the plan replays the chosen variant's graph.  The autotuner times
+// every tile shape with route 0, then the routes with the best shape, keeps
+// the fastest and remembers the choice in a small JSON-lines cache keyed by
+// the batch's signature.
 #include <cuda_runtime.h>
 #include <sys/stat.h>
 
@@ -33,6 +40,9 @@
 namespace xc {
 
 namespace {
+
+constexpr int kTcStreams = 4;  // side streams of the split-BF16 route
+constexpr int kRoutes = 5;     // route 0 (plain kernel only) and four multiply-add thresholds
 
 struct CopyJob {  // one matrix into its padded copy
   long long src, dst;
@@ -73,14 +83,24 @@ struct RaggedPlanImpl {
     bool built = false;
     RaggedTile* tiles = nullptr;
     int n_tiles = 0;
+    int tc_pairs = 0;  // pairs of the variant's route (split-BF16 calls)
     int grid = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
   };
-  std::vector<Variant> variants;
-  std::vector<void*> maps_for_variant;  // per-variant tensor-map arrays (box depends on the tile shape)
+  std::vector<Variant> variants;         // index = shape + n_shapes * route
+  std::vector<void*> maps_for_shape;     // per-shape tensor-map arrays (the box depends on the tile shape)
+  int n_shapes = 1, n_routes = 1;
   int chosen = 0;
   double tuned_ms = -1.0;
+  // split-BF16 routes (FP32)
+  std::vector<double> pair_mac;          // multiply-adds of each pair
+  std::vector<char> tc_ok;               // the split path takes the pair
+  cudaStream_t tc_streams[kTcStreams] = {};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t joins[kTcStreams] = {};
+  void* tc_ws[kTcStreams] = {};
+  size_t tc_ws_bytes = 0;
 };
 
 namespace {
@@ -99,50 +119,32 @@ double tile_cost(const RaggedPairDev& p, int sy0, int sx0, const RaggedShape& sh
   return (double)std::max(0, y_hi - y_lo) * std::max(0, x_hi - x_lo);
 }
 
-xc_status build_variant(RaggedPlanImpl* P, int index) {
-  RaggedPlanImpl::Variant& v = P->variants[index];
-  if (v.built) return XC_OK;
-  const RaggedShape sh = ragged_shape(P->dtype, index);
-  // tiles of every pair, heaviest first
-  std::vector<RaggedPairDev> hp(P->pairs.size());
-  std::vector<std::pair<double, RaggedTile>> tiles;
-  for (size_t i = 0; i < P->pairs.size(); ++i) {
-    const xc_pair_desc& pd = P->pairs[i];
-    const xc_matrix_desc& L = P->lefts[pd.left];
-    const xc_matrix_desc& R = P->rights[pd.right];
-    RaggedPairDev d;
-    d.left = (int)pd.left;
-    d.right = (int)pd.right;
-    d.Hl = (int)L.rows;
-    d.Wl = (int)L.cols;
-    d.Hr = (int)R.rows;
-    d.Wr = (int)R.cols;
-    d.out_off = (long long)pd.out_offset;
-    hp[i] = d;
-    const int Sy = d.Hl + d.Hr - 1, Sx = d.Wl + d.Wr - 1;
-    const int rem = (d.Wr - 1) % sh.vec;
-    const int origin = rem == 0 ? 0 : rem - sh.vec;
-    for (int sy0 = 0; sy0 < Sy; sy0 += sh.bsy)
-      for (int sx0 = origin; sx0 < Sx; sx0 += sh.bsx) {
-        RaggedTile t;
-        t.pair = (int)i;
-        t.sy0 = sy0;
-        t.sx0 = sx0;
-        tiles.emplace_back(tile_cost(d, sy0, sx0, sh), t);
-      }
-  }
-  std::stable_sort(tiles.begin(), tiles.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-  std::vector<RaggedTile> ht(tiles.size());
-  for (size_t i = 0; i < tiles.size(); ++i) ht[i] = tiles[i].second;
-  if (P->dpairs == nullptr) {
-    XC_CUDA_TRY(cudaMalloc(&P->dpairs, sizeof(RaggedPairDev) * hp.size()));
-    XC_CUDA_TRY(cudaMemcpy(P->dpairs, hp.data(), sizeof(RaggedPairDev) * hp.size(), cudaMemcpyHostToDevice));
-  }
-  XC_CUDA_TRY(cudaMalloc(&v.tiles, sizeof(RaggedTile) * std::max<size_t>(1, ht.size())));
-  XC_CUDA_TRY(cudaMemcpy(v.tiles, ht.data(), sizeof(RaggedTile) * ht.size(), cudaMemcpyHostToDevice));
-  v.n_tiles = (int)ht.size();
+// Smallest multiply-add count of the pairs a route sends to the split path:
+// 2^32, 2^30, 2^28, 2^26 for routes 1-4 (route 0: none).
+double route_min_mac(int route) { return route <= 0 ? 0.0 : std::ldexp(1.0, 34 - 2 * route); }
 
-  // tensor maps of the padded copies for this shape's boxes
+bool in_route(const RaggedPlanImpl* P, size_t pair, int route) {
+  return route > 0 && P->tc_ok[pair] && P->pair_mac[pair] >= route_min_mac(route);
+}
+
+RaggedPairDev pair_dev(const RaggedPlanImpl* P, size_t i) {
+  const xc_pair_desc& pd = P->pairs[i];
+  const xc_matrix_desc& L = P->lefts[pd.left];
+  const xc_matrix_desc& R = P->rights[pd.right];
+  RaggedPairDev d;
+  d.left = (int)pd.left;
+  d.right = (int)pd.right;
+  d.Hl = (int)L.rows;
+  d.Wl = (int)L.cols;
+  d.Hr = (int)R.rows;
+  d.Wr = (int)R.cols;
+  d.out_off = (long long)pd.out_offset;
+  return d;
+}
+
+// Tensor maps of the padded copies for one tile shape's boxes (built once per shape).
+xc_status shape_maps(RaggedPlanImpl* P, int shape, const RaggedShape& sh) {
+  if (P->maps_for_shape[2 * shape] != nullptr) return XC_OK;
   const CUtensorMapDataType dt = P->es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
   std::vector<CUtensorMap> lm(P->lefts.size()), rm(P->rights.size());
   long long off = 0;
@@ -169,43 +171,140 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
   }
   CUtensorMap *dl = nullptr, *dr = nullptr;
   XC_CUDA_TRY(cudaMalloc(&dl, sizeof(CUtensorMap) * lm.size()));
+  P->maps_for_shape[2 * shape] = dl;
   XC_CUDA_TRY(cudaMalloc(&dr, sizeof(CUtensorMap) * rm.size()));
+  P->maps_for_shape[2 * shape + 1] = dr;
   XC_CUDA_TRY(cudaMemcpy(dl, lm.data(), sizeof(CUtensorMap) * lm.size(), cudaMemcpyHostToDevice));
   XC_CUDA_TRY(cudaMemcpy(dr, rm.data(), sizeof(CUtensorMap) * rm.size(), cudaMemcpyHostToDevice));
-  P->maps_for_variant[2 * index] = dl;
-  P->maps_for_variant[2 * index + 1] = dr;
+  return XC_OK;
+}
 
-  // persistent grid: every SM filled to the kernel's occupancy
-  int dev = 0, sms = 0, per_sm = 0;
-  XC_CUDA_TRY(cudaGetDevice(&dev));
-  XC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  XC_CUDA_TRY(cudaFuncSetAttribute(sh.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem));
-  XC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh.kernel, sh.threads, sh.smem));
-  v.grid = std::max(1, std::min(v.n_tiles, sms * std::max(1, per_sm)));
+// Side streams, fork/join events and one workspace per side stream (sized
+// for the largest pair the split path takes), made on the first route that
+// needs them.
+xc_status tc_resources(RaggedPlanImpl* P) {
+  if (P->fork != nullptr) return XC_OK;
+  PairMap pm;
+  uint64_t n_out = 0;
+  make_pair_map(XC_ONE_TO_ONE, 1, 1, &pm, &n_out);
+  size_t ws = 0;
+  for (size_t i = 0; i < P->pairs.size(); ++i)
+    if (P->tc_ok[i]) {
+      const RaggedPairDev d = pair_dev(P, i);
+      ws = std::max(ws, tc_workspace_size(Geometry{d.Hl, d.Wl, d.Hr, d.Wr, d.Hl + d.Hr - 1, d.Wl + d.Wr - 1}, pm,
+                                          false));
+    }
+  for (int k = 0; k < kTcStreams; ++k) {
+    XC_CUDA_TRY(cudaStreamCreateWithFlags(&P->tc_streams[k], cudaStreamNonBlocking));
+    XC_CUDA_TRY(cudaEventCreateWithFlags(&P->joins[k], cudaEventDisableTiming));
+    XC_CUDA_TRY(cudaMalloc(&P->tc_ws[k], std::max<size_t>(ws, 256)));
+  }
+  P->tc_ws_bytes = std::max<size_t>(ws, 256);
+  XC_CUDA_TRY(cudaEventCreateWithFlags(&P->fork, cudaEventDisableTiming));
+  return XC_OK;
+}
 
-  // capture the step into a graph
-  RaggedLaunch rl;
-  rl.left = P->lpad;
-  rl.right = P->rpad;
-  rl.out = P->out;
-  rl.tiles = v.tiles;
-  rl.pairs = P->dpairs;
-  rl.lmaps = dl;
-  rl.rmaps = dr;
-  rl.queue = P->queue;
-  rl.n_tiles = v.n_tiles;
-  rl.grid = v.grid;
+xc_status build_variant(RaggedPlanImpl* P, int index) {
+  RaggedPlanImpl::Variant& v = P->variants[index];
+  if (v.built) return XC_OK;
+  const int shape = index % P->n_shapes, route = index / P->n_shapes;
+  const RaggedShape sh = ragged_shape(P->dtype, shape);
+  // tiles of every pair the plain kernel keeps, heaviest first; the pairs of
+  // the route, longest first
+  std::vector<RaggedPairDev> hp(P->pairs.size());
+  std::vector<std::pair<double, RaggedTile>> tiles;
+  std::vector<size_t> tc_pairs;
+  for (size_t i = 0; i < P->pairs.size(); ++i) {
+    const RaggedPairDev d = pair_dev(P, i);
+    hp[i] = d;
+    if (in_route(P, i, route)) {
+      tc_pairs.push_back(i);
+      continue;
+    }
+    const int Sy = d.Hl + d.Hr - 1, Sx = d.Wl + d.Wr - 1;
+    const int rem = (d.Wr - 1) % sh.vec;
+    const int origin = rem == 0 ? 0 : rem - sh.vec;
+    for (int sy0 = 0; sy0 < Sy; sy0 += sh.bsy)
+      for (int sx0 = origin; sx0 < Sx; sx0 += sh.bsx) {
+        RaggedTile t;
+        t.pair = (int)i;
+        t.sy0 = sy0;
+        t.sx0 = sx0;
+        tiles.emplace_back(tile_cost(d, sy0, sx0, sh), t);
+      }
+  }
+  std::stable_sort(tiles.begin(), tiles.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+  std::stable_sort(tc_pairs.begin(), tc_pairs.end(),
+                   [P](size_t a, size_t b) { return P->pair_mac[a] > P->pair_mac[b]; });
+  std::vector<RaggedTile> ht(tiles.size());
+  for (size_t i = 0; i < tiles.size(); ++i) ht[i] = tiles[i].second;
+  if (P->dpairs == nullptr) {
+    XC_CUDA_TRY(cudaMalloc(&P->dpairs, sizeof(RaggedPairDev) * hp.size()));
+    XC_CUDA_TRY(cudaMemcpy(P->dpairs, hp.data(), sizeof(RaggedPairDev) * hp.size(), cudaMemcpyHostToDevice));
+  }
+  v.n_tiles = (int)ht.size();
+  v.tc_pairs = (int)tc_pairs.size();
+  if (v.n_tiles > 0) {
+    XC_CUDA_TRY(cudaMalloc(&v.tiles, sizeof(RaggedTile) * ht.size()));
+    XC_CUDA_TRY(cudaMemcpy(v.tiles, ht.data(), sizeof(RaggedTile) * ht.size(), cudaMemcpyHostToDevice));
+    XC_TRY(shape_maps(P, shape, sh));
+    // persistent grid: every SM filled to the kernel's occupancy
+    int dev = 0, sms = 0, per_sm = 0;
+    XC_CUDA_TRY(cudaGetDevice(&dev));
+    XC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    XC_CUDA_TRY(cudaFuncSetAttribute(sh.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sh.smem));
+    XC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sh.kernel, sh.threads, sh.smem));
+    v.grid = std::max(1, std::min(v.n_tiles, sms * std::max(1, per_sm)));
+  }
+
+  // the route's pairs: each to the side stream with the least work so far
+  // (a call costs its multiply-adds plus about 2^26 of fixed work)
+  PairMap pm1;
+  uint64_t n_out1 = 0;
+  make_pair_map(XC_ONE_TO_ONE, 1, 1, &pm1, &n_out1);
+  std::vector<std::vector<size_t>> per_stream(kTcStreams);
+  if (!tc_pairs.empty()) {
+    XC_TRY(tc_resources(P));
+    double load[kTcStreams] = {0.0};
+    for (size_t i : tc_pairs) {
+      const int k = (int)(std::min_element(load, load + kTcStreams) - load);
+      per_stream[k].push_back(i);
+      load[k] += P->pair_mac[i] + std::ldexp(1.0, 26);
+      const RaggedPairDev& d = hp[i];
+      XC_TRY(tc_prepare(Geometry{d.Hl, d.Wl, d.Hr, d.Wr, d.Hl + d.Hr - 1, d.Wl + d.Wr - 1}, pm1, false));
+    }
+  }
+
+  // capture the step into a graph: the split-path branches fork from the
+  // capture stream first, so they depend on nothing; the plain branch runs
+  // beside them; the branches join before the capture ends
   cudaStream_t s = P->capture_stream;
   XC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   xc_status st = XC_OK;
-  const unsigned nb_l = (unsigned)P->lefts.size() * (unsigned)P->max_rows;  // left jobs only
-  if (P->es == 4) {
-    repack_kernel<float><<<nb_l, 128, 0, s>>>((const float*)P->left, (float*)P->lpad, P->jobs, P->max_rows);
-  } else {
-    repack_kernel<double><<<nb_l, 128, 0, s>>>((const double*)P->left, (double*)P->lpad, P->jobs, P->max_rows);
-  }
-  // rights: jobs after the lefts in the same table, different source / destination
-  {
+  const bool forked = !tc_pairs.empty();
+  if (forked && cudaEventRecord(P->fork, s) != cudaSuccess) st = XC_ERR_CUDA;
+  for (int k = 0; k < kTcStreams && forked; ++k)
+    if (st == XC_OK && !per_stream[k].empty() && cudaStreamWaitEvent(P->tc_streams[k], P->fork, 0) != cudaSuccess)
+      st = XC_ERR_CUDA;
+  if (st == XC_OK && v.n_tiles > 0) {
+    RaggedLaunch rl;
+    rl.left = P->lpad;
+    rl.right = P->rpad;
+    rl.out = P->out;
+    rl.tiles = v.tiles;
+    rl.pairs = P->dpairs;
+    rl.lmaps = static_cast<const CUtensorMap*>(P->maps_for_shape[2 * shape]);
+    rl.rmaps = static_cast<const CUtensorMap*>(P->maps_for_shape[2 * shape + 1]);
+    rl.queue = P->queue;
+    rl.n_tiles = v.n_tiles;
+    rl.grid = v.grid;
+    const unsigned nb_l = (unsigned)P->lefts.size() * (unsigned)P->max_rows;  // left jobs only
+    if (P->es == 4) {
+      repack_kernel<float><<<nb_l, 128, 0, s>>>((const float*)P->left, (float*)P->lpad, P->jobs, P->max_rows);
+    } else {
+      repack_kernel<double><<<nb_l, 128, 0, s>>>((const double*)P->left, (double*)P->lpad, P->jobs, P->max_rows);
+    }
+    // rights: jobs after the lefts in the same table, different source / destination
     const int nl = (int)P->lefts.size();
     const unsigned nb_r = (unsigned)(P->n_jobs - nl) * (unsigned)P->max_rows;
     if (nb_r > 0) {
@@ -216,9 +315,25 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
         repack_kernel<double><<<nb_r, 128, 0, s>>>((const double*)P->right, (double*)P->rpad, P->jobs + nl,
                                                    P->max_rows);
     }
+    if (cudaMemsetAsync(P->queue, 0, sizeof(unsigned int), s) != cudaSuccess) st = XC_ERR_CUDA;
+    if (st == XC_OK) st = ragged_launch(P->dtype, shape, rl, s);
   }
-  if (cudaMemsetAsync(P->queue, 0, sizeof(unsigned int), s) != cudaSuccess) st = XC_ERR_CUDA;
-  if (st == XC_OK) st = ragged_launch(P->dtype, index, rl, s);
+  for (int k = 0; k < kTcStreams && forked; ++k) {
+    if (per_stream[k].empty()) continue;
+    const cudaStream_t sk = P->tc_streams[k];
+    for (size_t i : per_stream[k]) {
+      if (st != XC_OK) break;
+      const RaggedPairDev& d = hp[i];
+      const xc_matrix_desc& L = P->lefts[d.left];
+      const xc_matrix_desc& R = P->rights[d.right];
+      st = tc_correlate((const float*)P->left + L.offset, (const float*)P->right + R.offset,
+                        (float*)P->out + d.out_off, Geometry{d.Hl, d.Wl, d.Hr, d.Wr, d.Hl + d.Hr - 1, d.Wl + d.Wr - 1},
+                        pm1, P->tc_ws[k], P->tc_ws_bytes, sk, false);
+    }
+    // every forked stream joins, also after an error, so that the capture can end
+    cudaEventRecord(P->joins[k], sk);
+    cudaStreamWaitEvent(s, P->joins[k], 0);
+  }
   cudaGraph_t graph = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(s, &graph);
   if (st != XC_OK) {
@@ -239,6 +354,15 @@ std::string cache_path() {
   return std::string(home ? home : "/tmp") + "/.cache/xcorr_gb300_autotune.jsonl";
 }
 
+// XC_RAGGED_TC=0 keeps every pair of FP32 plans on the plain kernel.
+bool tc_routes_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("XC_RAGGED_TC");
+    return !(e && std::strcmp(e, "0") == 0);
+  }();
+  return on;
+}
+
 std::string signature(const RaggedPlanImpl* P) {
   cudaDeviceProp prop;
   int dev = 0;
@@ -252,7 +376,8 @@ std::string signature(const RaggedPlanImpl* P) {
   }
   std::ostringstream ss;
   ss << prop.name << "|dtype=" << (int)P->dtype << "|pairs=" << P->pairs.size() << "|mac_log2="
-     << (int)std::floor(std::log2(std::max(1.0, mac / std::max<size_t>(1, P->pairs.size()))));
+     << (int)std::floor(std::log2(std::max(1.0, mac / std::max<size_t>(1, P->pairs.size())))) << "|variants="
+     << P->n_shapes << "x" << P->n_routes;
   return ss.str();
 }
 
@@ -284,8 +409,23 @@ xc_status ragged_plan_create(RaggedPlanImpl** out, xc_dtype dtype, const void* d
   P->lefts.assign(lefts, lefts + n_left);
   P->rights.assign(rights, rights + n_right);
   P->pairs.assign(pairs, pairs + n_pairs);
-  P->variants.resize(ragged_shape_count(dtype));
-  P->maps_for_variant.assign(2 * P->variants.size(), nullptr);
+  P->n_shapes = ragged_shape_count(dtype);
+  P->n_routes = dtype == XC_F32 && tc_routes_enabled() ? kRoutes : 1;
+  P->variants.resize((size_t)P->n_shapes * P->n_routes);
+  P->maps_for_shape.assign(2 * (size_t)P->n_shapes, nullptr);
+  // multiply-adds of every pair, and whether the split path takes it
+  {
+    PairMap pm1;
+    uint64_t n_out1 = 0;
+    make_pair_map(XC_ONE_TO_ONE, 1, 1, &pm1, &n_out1);
+    for (uint32_t i = 0; i < n_pairs; ++i) {
+      const xc_matrix_desc& L = lefts[pairs[i].left];
+      const xc_matrix_desc& R = rights[pairs[i].right];
+      P->pair_mac.push_back((double)L.rows * L.cols * R.rows * R.cols);
+      const Geometry g = make_geometry(xc_size2{L.cols, L.rows}, xc_size2{R.cols, R.rows});
+      P->tc_ok.push_back(dtype == XC_F32 && tc_workspace_size(g, pm1, false) > 0 ? 1 : 0);
+    }
+  }
   auto cleanup = [&](xc_status s) {
     ragged_plan_destroy(P);
     return s;
@@ -339,9 +479,9 @@ xc_status ragged_autotune(RaggedPlanImpl* P, cudaStream_t stream, int* chosen, d
     std::string line, hit;
     while (std::getline(in, line))
       if (line.find("\"sig\": \"" + sig + "\"") != std::string::npos) hit = line;
-    const size_t pos = hit.find("\"shape\": ");
+    const size_t pos = hit.find("\"variant\": ");
     if (pos != std::string::npos) {
-      const int idx = std::atoi(hit.c_str() + pos + 9);
+      const int idx = std::atoi(hit.c_str() + pos + 11);
       if (idx >= 0 && idx < (int)P->variants.size()) {
         P->chosen = idx;
         *chosen = idx;
@@ -355,7 +495,7 @@ xc_status ragged_autotune(RaggedPlanImpl* P, cudaStream_t stream, int* chosen, d
   XC_CUDA_TRY(cudaEventCreate(&e1));
   double best = 1e30;
   int arg = 0;
-  for (int i = 0; i < (int)P->variants.size(); ++i) {
+  auto time_variant = [&](int i) -> xc_status {
     XC_TRY(build_variant(P, i));
     for (int w = 0; w < 2; ++w) XC_CUDA_TRY(cudaGraphLaunch(P->variants[i].exec, stream));
     float ms = 0.f;
@@ -368,9 +508,25 @@ xc_status ragged_autotune(RaggedPlanImpl* P, cudaStream_t stream, int* chosen, d
       best = ms / 5.0;
       arg = i;
     }
+    return XC_OK;
+  };
+  xc_status st = XC_OK;
+  // every tile shape with all pairs on the plain kernel, then the routes
+  // with the best shape (a route whose pairs are those of the previous one,
+  // or none, is not timed again)
+  for (int sh = 0; sh < P->n_shapes && st == XC_OK; ++sh) st = time_variant(sh);
+  const int best_shape = arg;
+  size_t prev = 0;
+  for (int r = 1; r < P->n_routes && st == XC_OK; ++r) {
+    size_t n = 0;
+    for (size_t i = 0; i < P->pairs.size(); ++i) n += in_route(P, i, r) ? 1 : 0;
+    if (n == 0 || n == prev) continue;
+    prev = n;
+    st = time_variant(best_shape + P->n_shapes * r);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  XC_TRY(st);
   P->chosen = arg;
   P->tuned_ms = best;
   *chosen = arg;
@@ -384,9 +540,32 @@ xc_status ragged_autotune(RaggedPlanImpl* P, cudaStream_t stream, int* chosen, d
     f = std::fopen(path.c_str(), "a");
   }
   if (f != nullptr) {
-    std::fprintf(f, "{\"sig\": \"%s\", \"shape\": %d, \"ms\": %.6f}\n", sig.c_str(), arg, best);
+    std::fprintf(f, "{\"sig\": \"%s\", \"variant\": %d, \"ms\": %.6f}\n", sig.c_str(), arg, best);
     std::fclose(f);
   }
+  return XC_OK;
+}
+
+xc_status ragged_describe(RaggedPlanImpl* P, int variant, xc_ragged_variant* out) {
+  if (variant == -1) variant = P->chosen;
+  if (variant < 0 || variant >= (int)P->variants.size())
+    return fail(XC_ERR_INVALID_ARGUMENT, "variant " + std::to_string(variant) + " out of range");
+  const int route = variant / P->n_shapes;
+  out->index = variant;
+  out->n_variants = (int32_t)P->variants.size();
+  out->tile_shape = variant % P->n_shapes;
+  uint32_t n = 0;
+  for (size_t i = 0; i < P->pairs.size(); ++i) n += in_route(P, i, route) ? 1 : 0;
+  out->tc_pairs = n;
+  out->tc_min_macs = (uint64_t)route_min_mac(route);
+  return XC_OK;
+}
+
+xc_status ragged_select(RaggedPlanImpl* P, int variant) {
+  if (variant < 0 || variant >= (int)P->variants.size())
+    return fail(XC_ERR_INVALID_ARGUMENT, "variant " + std::to_string(variant) + " out of range");
+  XC_TRY(build_variant(P, variant));
+  P->chosen = variant;
   return XC_OK;
 }
 
@@ -397,7 +576,13 @@ void ragged_plan_destroy(RaggedPlanImpl* P) {
     if (v.graph) cudaGraphDestroy(v.graph);
     cudaFree(v.tiles);
   }
-  for (void* m : P->maps_for_variant) cudaFree(m);
+  for (void* m : P->maps_for_shape) cudaFree(m);
+  for (int k = 0; k < kTcStreams; ++k) {
+    cudaFree(P->tc_ws[k]);
+    if (P->joins[k]) cudaEventDestroy(P->joins[k]);
+    if (P->tc_streams[k]) cudaStreamDestroy(P->tc_streams[k]);
+  }
+  if (P->fork) cudaEventDestroy(P->fork);
   cudaFree(P->dpairs);
   cudaFree(P->lpad);
   cudaFree(P->rpad);

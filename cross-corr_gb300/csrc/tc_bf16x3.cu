@@ -1378,6 +1378,40 @@ int sm_count() {
   return sms;
 }
 
+// Dynamic shared-memory limits raised so far, per kernel and context.  A
+// limit is raised only when a launch needs more than the kernel has, so a
+// plan that calls tc_prepare for its problems before it captures them into a
+// graph makes no cudaFuncSetAttribute call inside the capture.
+struct SmemLimit {
+  const void* fn;
+  unsigned long long ctx;
+  int bytes;
+};
+std::mutex g_limit_mutex;
+std::vector<SmemLimit> g_limits;
+
+xc_status raise_smem_limit(const void* fn, int bytes) {
+  const unsigned long long ctx = current_context_id();
+  std::lock_guard<std::mutex> lock(g_limit_mutex);
+  for (SmemLimit& l : g_limits)
+    if (l.fn == fn && ctx != 0 && l.ctx == ctx) {
+      if (l.bytes < bytes) {
+        XC_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+        l.bytes = bytes;
+      }
+      return XC_OK;
+    }
+  XC_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  if (ctx != 0) g_limits.push_back(SmemLimit{fn, ctx, bytes});
+  return XC_OK;
+}
+
+// Shared memory of the correction kernel: a left table row and the rows of
+// kCorrPartners right tables.
+size_t corr_smem_bytes(const Geometry& g) {
+  return (size_t)(corr_stage(g.Wl) + kCorrPartners * corr_stage(g.Wr)) * sizeof(float);
+}
+
 // Workspace layout (each part 256-byte aligned).
 struct TcWs {
   float* mu;        // n_left + n_right means
@@ -1619,10 +1653,9 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   // 4. the mean terms initialise the output
   {
     const int stage_l = corr_stage(g.Wl), stage_r = corr_stage(g.Wr);
-    const size_t corr_smem = (size_t)(stage_l + kCorrPartners * stage_r) * sizeof(float);
+    const size_t corr_smem = corr_smem_bytes(g);
     if (corr_smem > 200 * 1024) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths: right matrices too wide");
-    if (corr_smem > 48 * 1024)
-      XC_CUDA_TRY(cudaFuncSetAttribute(correction_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)corr_smem));
+    if (corr_smem > 48 * 1024) XC_TRY(raise_smem_limit((const void*)correction_kernel, (int)corr_smem));
     const int n_kgroups = div_up(pm.K, kCorrPartners);
     const long long n_blocks = (long long)nl * n_kgroups * g.Sy;
     if (n_blocks > 0x7fffffffLL) return fail(XC_ERR_INVALID_ARGUMENT, "problem too large for one launch");
@@ -1635,7 +1668,7 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
   // persistent: one CTA per SM (about 205 KB of shared memory and all 512 TMEM
   // columns each), walking the list in snake order
   auto kern = tf32 ? tc_kernel<true> : tc_kernel<false>;
-  XC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, t.smem_bytes));
+  XC_TRY(raise_smem_limit((const void*)kern, t.smem_bytes));
   const long long blocks = std::max(1LL, std::min<long long>(n_list, sm_count()));
   if (band_done) {
     // banded: the host deals the items out to the CTAs by least work
@@ -1655,6 +1688,16 @@ xc_status tc_correlate_banded(const float* left, const float* right, float* out,
     band_release_kernel<<<1, 32, 0, stream>>>(band_done, prm.n_bands);
     XC_CUDA_TRY(cudaGetLastError());
   }
+  return XC_OK;
+}
+
+xc_status tc_prepare(const Geometry& g, const PairMap& pm, bool tf32) {
+  TcPlan t;
+  if (!tc_plan(g, pm, tf32, &t)) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths need Wl + Wr below 6400");
+  const size_t corr_smem = corr_smem_bytes(g);
+  if (corr_smem > 200 * 1024) return fail(XC_ERR_UNSUPPORTED, "split tensor-core paths: right matrices too wide");
+  if (corr_smem > 48 * 1024) XC_TRY(raise_smem_limit((const void*)correction_kernel, (int)corr_smem));
+  XC_TRY(raise_smem_limit(tf32 ? (const void*)tc_kernel<true> : (const void*)tc_kernel<false>, t.smem_bytes));
   return XC_OK;
 }
 

@@ -97,6 +97,8 @@ xc_status ragged_plan_create(RaggedPlanImpl** plan, xc_dtype dtype, const void* 
                              const xc_pair_desc* pairs, uint32_t n_pairs, void* d_out);
 xc_status ragged_execute(RaggedPlanImpl* plan, cudaStream_t stream);
 xc_status ragged_autotune(RaggedPlanImpl* plan, cudaStream_t stream, int* chosen, double* best_ms);
+xc_status ragged_describe(RaggedPlanImpl* plan, int variant, xc_ragged_variant* out);
+xc_status ragged_select(RaggedPlanImpl* plan, int variant);
 void ragged_plan_destroy(RaggedPlanImpl* plan);
 xc_status correlate_pairs(xc_dtype dtype, const void* d_left, const xc_matrix_desc* lefts, uint32_t n_left,
                           const void* d_right, const xc_matrix_desc* rights, uint32_t n_right,
@@ -153,5 +155,16 @@ struct TcBands {
 xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
                               const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
                               int want_bands, int* band_done, TcBands* bands, int max_rows = 64);
+
+// Split tensor-core paths (tc_bf16x3.cu): one launch sequence per problem on
+// `stream` (no host synchronisation, so it can be captured into a graph).
+xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows = 64);
+// Workspace bytes of a problem; 0 when the split paths do not take it.
+size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32);
+// Raises the kernels' shared-memory limits for a problem (what tc_correlate
+// would otherwise do on its first call): call it before capturing
+// tc_correlate into a graph.
+xc_status tc_prepare(const Geometry& g, const PairMap& pm, bool tf32);
 
 }  // namespace xc

@@ -59,6 +59,7 @@ EXPORTED = [
     "xc_run_scatter_f32", "xc_run_scatter_f64",
     "xc_normalize_fft_results_f32", "xc_normalize_fft_results_f64",
     "xc_ragged_plan_create", "xc_ragged_autotune", "xc_ragged_execute", "xc_ragged_plan_destroy",
+    "xc_ragged_describe", "xc_ragged_select",
     "xc_correlate_pairs", "xc_selector_features", "xc_mlp_forward", "xc_mlp_gradient", "xc_mlp_adam_step",
     "xc_selector_load", "xc_selector_load_builtin", "xc_select_method", "xc_autotune_method",
     "xc_algorithm", "xc_select_algorithm", "xc_correlate_algo", "xc_time_algorithm", "xc_autotune_algorithm",
@@ -90,6 +91,11 @@ class MatrixDesc(ctypes.Structure):
 
 class PairDesc(ctypes.Structure):
     _fields_ = [("left", ctypes.c_uint32), ("right", ctypes.c_uint32), ("out_offset", ctypes.c_uint64)]
+
+
+class RaggedVariant(ctypes.Structure):
+    _fields_ = [("index", ctypes.c_int32), ("n_variants", ctypes.c_int32), ("tile_shape", ctypes.c_int32),
+                ("tc_pairs", ctypes.c_uint32), ("tc_min_macs", ctypes.c_uint64)]
 
 
 def size2(rows: int, cols: int) -> Size2:
@@ -140,6 +146,8 @@ def lib():
                                             u32, vp]
         L.xc_ragged_autotune.argtypes = [vp, vp, P(c.c_int), P(c.c_double)]
         L.xc_ragged_execute.argtypes = [vp, vp]
+        L.xc_ragged_describe.argtypes = [vp, i, P(RaggedVariant)]
+        L.xc_ragged_select.argtypes = [vp, i]
         L.xc_ragged_plan_destroy.argtypes = [vp]
         L.xc_correlate_pairs.argtypes = [i, vp, P(MatrixDesc), u32, vp, P(MatrixDesc), u32, P(PairDesc), u32, vp,
                                          vp]
@@ -399,10 +407,24 @@ class RaggedPlan:
                                           len(pairs), self.out.data_ptr()))
 
     def autotune(self, stream=None):
-        shape = ctypes.c_int()
+        """Times the plan's variants; returns (chosen variant, its ms per
+        step, or < 0 when the choice came from the cache)."""
+        variant = ctypes.c_int()
         ms = ctypes.c_double()
-        check(lib().xc_ragged_autotune(self.handle, _stream_ptr(stream), ctypes.byref(shape), ctypes.byref(ms)))
-        return shape.value, ms.value
+        check(lib().xc_ragged_autotune(self.handle, _stream_ptr(stream), ctypes.byref(variant), ctypes.byref(ms)))
+        return variant.value, ms.value
+
+    def describe(self, variant=-1):
+        """Variant `variant` (-1: the chosen one) as a dict: its index, the
+        plan's variant count, the plain kernel's tile shape, and the pairs run
+        on the split-BF16 path (count and multiply-add threshold)."""
+        v = RaggedVariant()
+        check(lib().xc_ragged_describe(self.handle, variant, ctypes.byref(v)))
+        return {"index": v.index, "n_variants": v.n_variants, "tile_shape": v.tile_shape, "tc_pairs": v.tc_pairs,
+                "tc_min_macs": v.tc_min_macs}
+
+    def select(self, variant):
+        check(lib().xc_ragged_select(self.handle, variant))
 
     def execute(self, stream=None):
         check(lib().xc_ragged_execute(self.handle, _stream_ptr(stream)))

@@ -263,11 +263,33 @@ xc_status xc_ragged_plan_create(xc_ragged_plan* plan, xc_dtype dtype, const void
                                 const xc_matrix_desc* lefts, uint32_t n_left, const void* d_right,
                                 const xc_matrix_desc* rights, uint32_t n_right, const xc_pair_desc* pairs,
                                 uint32_t n_pairs, void* d_out);
-/* Times every candidate tile shape on the plan's batch and keeps the fastest;
- * decisions are cached by batch signature in $XC_AUTOTUNE_CACHE (default
- * ~/.cache/xcorr_gb300_autotune.jsonl).  best_ms < 0 when taken from the cache. */
+/* A plan's variants: a tile shape of the plain kernel and, for FP32 plans, a
+ * route.  Variant index = tile_shape + (tile shapes) x route.  Route 0 keeps
+ * every pair on the plain kernel; routes 1-4 run the pairs with at least
+ * 2^32, 2^30, 2^28, 2^26 multiply-adds (that the split path takes) as
+ * one_to_one calls of the split-BF16 tensor-core path, on four side streams
+ * captured into the same graph beside the plain kernel's launch (those
+ * pairs' outputs then carry the split path's error, up to about 1e-5 of
+ * max|out| on zero-mean data).  XC_RAGGED_TC=0 in the environment leaves FP32
+ * plans with route 0 only.  Variant 0 runs until another is chosen. */
+typedef struct xc_ragged_variant {
+  int32_t index;        /* the variant described */
+  int32_t n_variants;   /* variants of this plan */
+  int32_t tile_shape;   /* plain-kernel tile shape of the pairs left on the plain kernel */
+  uint32_t tc_pairs;    /* pairs run on the split-BF16 path */
+  uint64_t tc_min_macs; /* ... those with at least this many multiply-adds (0: none) */
+} xc_ragged_variant;
+/* Times every tile shape with route 0, then every route with the best shape,
+ * on the plan's batch, and keeps the fastest variant (`chosen_shape` receives
+ * its index); decisions are cached by batch signature in $XC_AUTOTUNE_CACHE
+ * (default ~/.cache/xcorr_gb300_autotune.jsonl).  best_ms < 0 when taken from
+ * the cache. */
 xc_status xc_ragged_autotune(xc_ragged_plan plan, void* stream, int* chosen_shape, double* best_ms);
-/* Replays the plan's graph on `stream`. */
+/* Describes variant `variant` (-1: the chosen one). */
+xc_status xc_ragged_describe(xc_ragged_plan plan, int variant, xc_ragged_variant* out);
+/* Chooses a variant (builds its graph now; allocates for the first split-path route). */
+xc_status xc_ragged_select(xc_ragged_plan plan, int variant);
+/* Replays the chosen variant's graph on `stream`. */
 xc_status xc_ragged_execute(xc_ragged_plan plan, void* stream);
 xc_status xc_ragged_plan_destroy(xc_ragged_plan plan);
 /* The same batch as one launch of the plain kernel per pair (baseline). */

@@ -59,7 +59,8 @@ def test_ragged_autotune_and_graph_replay_with_new_data():
     lefts, rights, pairs = ragged_batch(16, 10, 140, 8)
     plan = xcorr.RaggedPlan(lefts, rights, pairs)
     shape, ms = plan.autotune()
-    assert shape in (0, 1) and ms > 0
+    assert 0 <= shape < plan.describe()["n_variants"] and ms > 0
+    assert plan.describe()["index"] == shape
     # the graph re-reads the bound input buffers on every execution
     rng = np.random.default_rng(9)
     lefts2 = [rng.uniform(-1, 1, a.shape).astype(np.float32) for a in lefts]
@@ -117,4 +118,51 @@ def test_ragged_largest_pairs_match_oracle():
     for got, got_pp, ref in zip(plan.outputs(), plan.outputs(base), refs):
         assert rel_to_max(got, ref) <= 1e-5
         assert rel_to_max(got_pp, ref) <= 1e-5
+    plan.close()
+
+
+def test_ragged_split_routes_match_oracle():
+    """FP32 plans can route the pairs with the most multiply-adds through the
+    split-BF16 path (one_to_one calls on side streams, captured into the same
+    graph as the plain kernel's launch for the other pairs).  Every route, with
+    either tile shape, matches the oracle on every pair; the outputs start as
+    NaN, so a pair that no branch writes fails."""
+    rng = np.random.default_rng(12)
+    sides = [(160, 150, 170, 140),   # 5.7e8 multiply-adds: routes 3 and 4
+             (300, 280, 260, 290),   # 6.3e9: every route
+             (64, 70, 80, 90),       # 3.2e7: plain kernel only
+             (12, 30, 7, 9),
+             (200, 60, 180, 70),     # 1.5e8: route 4
+             (1, 300, 1, 290),
+             (4, 3000, 4, 2000),     # 9.6e7, a wide strip: route 4
+             (130, 128, 127, 129)]   # 2.73e8: routes 3 and 4
+    lefts = [rng.uniform(-1, 1, (a, b)).astype(np.float32) for a, b, _, _ in sides]
+    rights = [rng.uniform(-1, 1, (c, d)).astype(np.float32) for _, _, c, d in sides]
+    pairs = [(i, i) for i in range(len(sides))]
+    refs = oracle.run_pairs(lefts, rights, threads=os.cpu_count() or 1)
+    plan = xcorr.RaggedPlan(lefts, rights, pairs)
+    n = plan.describe()["n_variants"]
+    assert n == 10  # 2 tile shapes x 5 routes
+    routed = []
+    for v in range(n):
+        d = plan.describe(v)
+        assert d["index"] == v and d["tile_shape"] == v % 2
+        routed.append(d["tc_pairs"])
+        plan.select(v)
+        plan.out.fill_(float("nan"))
+        plan.execute()
+        torch.cuda.synchronize()
+        for k, (got, ref) in enumerate(zip(plan.outputs(), refs)):
+            assert got.shape == ref.shape
+            assert rel_to_max(got, ref) <= 1e-5, (v, k)
+    assert routed == [0, 0, 1, 1, 1, 1, 3, 3, 5, 5]
+    plan.close()
+
+
+def test_ragged_fp64_plans_keep_every_pair_on_the_plain_kernel():
+    lefts, rights, pairs = ragged_batch(3, 100, 140, 13, np.float64)
+    plan = xcorr.RaggedPlan(lefts, rights, pairs, dtype="f64")
+    assert plan.describe()["n_variants"] == 1
+    with pytest.raises(xcorr.XcError):
+        plan.select(1)
     plan.close()
