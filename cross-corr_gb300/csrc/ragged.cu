@@ -14,7 +14,7 @@
 // A variant is a tile shape of the plain kernel and, for FP32 batches, a
 // route: the pairs with at least the route's multiply-add count run instead
 // as one_to_one calls of the split-BF16 tensor-core path, dealt out over
-// kTcStreams side streams (longest first, each to the least loaded stream)
+// up to kMaxTcStreams side streams (longest first, each to the least loaded stream)
 // and captured into the same graph, beside the plain kernel's branch.  Route
 // 0 keeps every pair on the plain kernel.
 // Executing the plan replays the chosen variant's graph.  The autotuner times
@@ -41,7 +41,12 @@ namespace xc {
 
 namespace {
 
-constexpr int kTcStreams = 4;  // side streams of the split-BF16 route
+constexpr int kMaxTcStreams = 8;  // side streams of the split-BF16 route (XC_RAGGED_TC_STREAMS, default 8)
+// Left rows per work item of a routed pair.  A lone call shortens its items
+// until they give two per SM; with eight calls in flight longer items pay
+// (512-pair batch, 448 pairs routed: 33.3 ms with the lone-call rule, 31.1 /
+// 30.6 / 30.8 / 32.0 ms with items of 24 / 32 / 48 / 64 rows).
+constexpr int kTcItemRows = 32;
 constexpr int kRoutes = 5;     // route 0 (plain kernel only) and four multiply-add thresholds
 
 struct CopyJob {  // one matrix into its padded copy
@@ -96,10 +101,11 @@ struct RaggedPlanImpl {
   // split-BF16 routes (FP32)
   std::vector<double> pair_mac;          // multiply-adds of each pair
   std::vector<char> tc_ok;               // the split path takes the pair
-  cudaStream_t tc_streams[kTcStreams] = {};
+  int n_streams = kMaxTcStreams;
+  cudaStream_t tc_streams[kMaxTcStreams] = {};
   cudaEvent_t fork = nullptr;
-  cudaEvent_t joins[kTcStreams] = {};
-  void* tc_ws[kTcStreams] = {};
+  cudaEvent_t joins[kMaxTcStreams] = {};
+  void* tc_ws[kMaxTcStreams] = {};
   size_t tc_ws_bytes = 0;
 };
 
@@ -194,7 +200,7 @@ xc_status tc_resources(RaggedPlanImpl* P) {
       ws = std::max(ws, tc_workspace_size(Geometry{d.Hl, d.Wl, d.Hr, d.Wr, d.Hl + d.Hr - 1, d.Wl + d.Wr - 1}, pm,
                                           false));
     }
-  for (int k = 0; k < kTcStreams; ++k) {
+  for (int k = 0; k < P->n_streams; ++k) {
     XC_CUDA_TRY(cudaStreamCreateWithFlags(&P->tc_streams[k], cudaStreamNonBlocking));
     XC_CUDA_TRY(cudaEventCreateWithFlags(&P->joins[k], cudaEventDisableTiming));
     XC_CUDA_TRY(cudaMalloc(&P->tc_ws[k], std::max<size_t>(ws, 256)));
@@ -262,12 +268,12 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
   PairMap pm1;
   uint64_t n_out1 = 0;
   make_pair_map(XC_ONE_TO_ONE, 1, 1, &pm1, &n_out1);
-  std::vector<std::vector<size_t>> per_stream(kTcStreams);
+  std::vector<std::vector<size_t>> per_stream(P->n_streams);
   if (!tc_pairs.empty()) {
     XC_TRY(tc_resources(P));
-    double load[kTcStreams] = {0.0};
+    double load[kMaxTcStreams] = {0.0};
     for (size_t i : tc_pairs) {
-      const int k = (int)(std::min_element(load, load + kTcStreams) - load);
+      const int k = (int)(std::min_element(load, load + P->n_streams) - load);
       per_stream[k].push_back(i);
       load[k] += P->pair_mac[i] + std::ldexp(1.0, 26);
       const RaggedPairDev& d = hp[i];
@@ -283,7 +289,7 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
   xc_status st = XC_OK;
   const bool forked = !tc_pairs.empty();
   if (forked && cudaEventRecord(P->fork, s) != cudaSuccess) st = XC_ERR_CUDA;
-  for (int k = 0; k < kTcStreams && forked; ++k)
+  for (int k = 0; k < P->n_streams && forked; ++k)
     if (st == XC_OK && !per_stream[k].empty() && cudaStreamWaitEvent(P->tc_streams[k], P->fork, 0) != cudaSuccess)
       st = XC_ERR_CUDA;
   if (st == XC_OK && v.n_tiles > 0) {
@@ -318,7 +324,7 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
     if (cudaMemsetAsync(P->queue, 0, sizeof(unsigned int), s) != cudaSuccess) st = XC_ERR_CUDA;
     if (st == XC_OK) st = ragged_launch(P->dtype, shape, rl, s);
   }
-  for (int k = 0; k < kTcStreams && forked; ++k) {
+  for (int k = 0; k < P->n_streams && forked; ++k) {
     if (per_stream[k].empty()) continue;
     const cudaStream_t sk = P->tc_streams[k];
     for (size_t i : per_stream[k]) {
@@ -328,7 +334,7 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
       const xc_matrix_desc& R = P->rights[d.right];
       st = tc_correlate((const float*)P->left + L.offset, (const float*)P->right + R.offset,
                         (float*)P->out + d.out_off, Geometry{d.Hl, d.Wl, d.Hr, d.Wr, d.Hl + d.Hr - 1, d.Wl + d.Wr - 1},
-                        pm1, P->tc_ws[k], P->tc_ws_bytes, sk, false);
+                        pm1, P->tc_ws[k], P->tc_ws_bytes, sk, false, kTcItemRows, kTcItemRows);
     }
     // every forked stream joins, also after an error, so that the capture can end
     cudaEventRecord(P->joins[k], sk);
@@ -352,6 +358,18 @@ std::string cache_path() {
   if (e && *e) return e;
   const char* home = std::getenv("HOME");
   return std::string(home ? home : "/tmp") + "/.cache/xcorr_gb300_autotune.jsonl";
+}
+
+// Side streams of the split-BF16 routes: XC_RAGGED_TC_STREAMS (1-8), default
+// 8 (512-pair batch, 448 pairs routed, 32-row items: 31.8 ms on 6 streams,
+// 30.6 ms on 8; with the lone-call item rule 40.9 / 34.2 / 33.3 ms on 2 / 4 / 8).
+int tc_stream_count() {
+  static const int n = [] {
+    const char* e = std::getenv("XC_RAGGED_TC_STREAMS");
+    const int v = e ? std::atoi(e) : 0;
+    return v >= 1 && v <= kMaxTcStreams ? v : kMaxTcStreams;
+  }();
+  return n;
 }
 
 // XC_RAGGED_TC=0 keeps every pair of FP32 plans on the plain kernel.
@@ -411,6 +429,7 @@ xc_status ragged_plan_create(RaggedPlanImpl** out, xc_dtype dtype, const void* d
   P->pairs.assign(pairs, pairs + n_pairs);
   P->n_shapes = ragged_shape_count(dtype);
   P->n_routes = dtype == XC_F32 && tc_routes_enabled() ? kRoutes : 1;
+  P->n_streams = tc_stream_count();
   P->variants.resize((size_t)P->n_shapes * P->n_routes);
   P->maps_for_shape.assign(2 * (size_t)P->n_shapes, nullptr);
   // multiply-adds of every pair, and whether the split path takes it
@@ -577,7 +596,7 @@ void ragged_plan_destroy(RaggedPlanImpl* P) {
     cudaFree(v.tiles);
   }
   for (void* m : P->maps_for_shape) cudaFree(m);
-  for (int k = 0; k < kTcStreams; ++k) {
+  for (int k = 0; k < kMaxTcStreams; ++k) {
     cudaFree(P->tc_ws[k]);
     if (P->joins[k]) cudaEventDestroy(P->joins[k]);
     if (P->tc_streams[k]) cudaStreamDestroy(P->tc_streams[k]);

@@ -1305,7 +1305,8 @@ struct TcPlan {
 int chunk_rows_fixed();
 int sm_count();
 
-bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool banded = false, int max_rows = 64) {
+bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool banded = false, int max_rows = 64,
+             int min_rows = 4) {
   // sizes accepted: Wl + Wr below 6400 (the correction kernel stages
   // (Wl + 1) + 8 (Wr + 1) floats, well inside 200 KB there)
   if ((size_t)8 * ((g.Wl + g.Wr + 2 + 3) / 4 * 4) * sizeof(float) > 200 * 1024) return false;
@@ -1323,8 +1324,9 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool ba
   t->kstep = parts.kstep;               // columns per MMA K-step (32 bytes)
   t->nkc = parts.nkc;                   // 128-byte column chunks of a k-part
   t->pitch = (g.Wr + 16 / t->es - 1) / (16 / t->es) * (16 / t->es);
-  // left rows per item: at most 64, fewer when that leaves fewer than two
-  // items per SM (small problems), at least 4.  Longer items end fewer
+  // left rows per item: at most max_rows (64), fewer when that leaves fewer
+  // than two items per SM (small problems), at least min_rows (4; callers
+  // that run several problems at once ask for longer items).  Longer items end fewer
   // accumulator windows early (at one_to_many 256x256 x 64: 1.071 ms with
   // 32-row items, 1.039 ms with 64).  A banded launch keeps at most 32: its
   // host plan cuts each band into pieces of half to one item, and 152 CTAs
@@ -1334,7 +1336,8 @@ bool tc_plan(const Geometry& g, const PairMap& pm, bool tf32, TcPlan* t, bool ba
   const long long rows_all = span * per_tile_key;
   const long long fair = rows_all / (2LL * sm_count());
   const int chunk32 = chunk_rows_fixed() > 0 ? chunk_rows_fixed() : (int)std::max(4LL, std::min(32LL, fair));
-  t->chunk_rows = chunk_rows_fixed() > 0 || banded ? chunk32 : (int)std::max(4LL, std::min((long long)max_rows, fair));
+  const long long lo = std::max(1, std::min(min_rows, max_rows));
+  t->chunk_rows = chunk_rows_fixed() > 0 || banded ? chunk32 : (int)std::max(lo, std::min((long long)max_rows, fair));
   t->n_chunks = (int)div_up(span, (long long)t->chunk_rows);
   t->n_items = (long long)t->n_chunks * per_tile_key;
   t->n_items_ws = std::max(t->n_items, div_up(span, (long long)chunk32) * per_tile_key);
@@ -1529,9 +1532,9 @@ size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32) {
 
 xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
                               const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
-                              int want_bands, int* band_done, TcBands* bands, int max_rows) {
+                              int want_bands, int* band_done, TcBands* bands, int max_rows, int min_rows) {
   TcPlan t;
-  if (!tc_plan(g, pm, tf32, &t, band_done != nullptr, max_rows))
+  if (!tc_plan(g, pm, tf32, &t, band_done != nullptr, max_rows, min_rows))
     return fail(XC_ERR_UNSUPPORTED,
                 "split tensor-core paths need Wl + Wr below 6400");
   const size_t need = ws_layout(nullptr, g, pm, t).bytes;
@@ -1702,9 +1705,9 @@ xc_status tc_prepare(const Geometry& g, const PairMap& pm, bool tf32) {
 }
 
 xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows) {
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows, int min_rows) {
   return tc_correlate_banded(left, right, out, g, pm, workspace, ws_bytes, stream, tf32, 1, nullptr, nullptr,
-                             max_rows);
+                             max_rows, min_rows);
 }
 
 // ---------------------------------------------------------------------------

@@ -154,12 +154,16 @@ struct TcBands {
 };
 xc_status tc_correlate_banded(const float* left, const float* right, float* out, const Geometry& g,
                               const PairMap& pm, void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32,
-                              int want_bands, int* band_done, TcBands* bands, int max_rows = 64);
+                              int want_bands, int* band_done, TcBands* bands, int max_rows = 64,
+                              int min_rows = 4);
 
 // Split tensor-core paths (tc_bf16x3.cu): one launch sequence per problem on
 // `stream` (no host synchronisation, so it can be captured into a graph).
+// Work items take between min_rows and max_rows left rows: as few as give two
+// items per SM, within those bounds.
 xc_status tc_correlate(const float* left, const float* right, float* out, const Geometry& g, const PairMap& pm,
-                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows = 64);
+                       void* workspace, size_t ws_bytes, cudaStream_t stream, bool tf32, int max_rows = 64,
+                       int min_rows = 4);
 // Workspace bytes of a problem; 0 when the split paths do not take it.
 size_t tc_workspace_size(const Geometry& g, const PairMap& pm, bool tf32);
 // Raises the kernels' shared-memory limits for a problem (what tc_correlate

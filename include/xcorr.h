@@ -267,7 +267,7 @@ xc_status xc_ragged_plan_create(xc_ragged_plan* plan, xc_dtype dtype, const void
  * route.  Variant index = tile_shape + (tile shapes) x route.  Route 0 keeps
  * every pair on the plain kernel; routes 1-4 run the pairs with at least
  * 2^32, 2^30, 2^28, 2^26 multiply-adds (that the split path takes) as
- * one_to_one calls of the split-BF16 tensor-core path, on four side streams
+ * one_to_one calls of the split-BF16 tensor-core path, on eight side streams
  * captured into the same graph beside the plain kernel's launch (those
  * pairs' outputs then carry the split path's error, up to about 1e-5 of
  * max|out| on zero-mean data).  XC_RAGGED_TC=0 in the environment leaves FP32
