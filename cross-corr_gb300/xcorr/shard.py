@@ -51,12 +51,16 @@ def run_sharded(n_outputs: int, costs: Sequence[int], compute: Callable[[List[in
     return full
 
 
-def correlate_pairs_sharded(lefts, rights, rank: int, world_size: int, group=None, dtype: str = "f32") -> list:
+def correlate_pairs_sharded(lefts, rights, rank: int, world_size: int, group=None, dtype: str = "f32",
+                            variant=None) -> list:
     """Correlations of the pairs (lefts[i], rights[i]) split over the ranks of
     a process group: each rank runs its cost-balanced share as one ragged
-    plan (xcorr.RaggedPlan: one persistent launch under a CUDA graph) on its
-    current CUDA device, and every rank returns the full, ordered list of
-    output arrays."""
+    plan (xcorr.RaggedPlan: one CUDA graph) on its current CUDA device, and
+    every rank returns the full, ordered list of output arrays.  `variant`
+    picks the plan's variant: None keeps its default (every pair on the plain
+    kernel), "auto" autotunes it on the rank's share, an int selects it (for
+    FP32, the variants that route the largest pairs through the split-BF16
+    path)."""
     import torch
 
     from . import RaggedPlan
@@ -69,6 +73,10 @@ def correlate_pairs_sharded(lefts, rights, rank: int, world_size: int, group=Non
         plan = RaggedPlan([lefts[i] for i in idx], [rights[i] for i in idx], [(k, k) for k in range(len(idx))],
                           dtype)
         try:
+            if variant == "auto":
+                plan.autotune()
+            elif variant is not None:
+                plan.select(int(variant))
             plan.execute()
             torch.cuda.synchronize()
             return plan.outputs()

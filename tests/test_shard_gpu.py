@@ -15,17 +15,23 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def make_batch(seed=9, n=10):
+def make_batch(seed=9, n=10, big=False):
+    """n pairs with sides in 8..119; with `big`, three more of 4e8 to 6e8
+    multiply-adds (above the split-BF16 routes' 2^26 and 2^28 thresholds)."""
     rng = np.random.default_rng(seed)
     lefts, rights = [], []
     for _ in range(n):
         hl, wl, hr, wr = rng.integers(8, 120, size=4)
         lefts.append(rng.uniform(-1, 1, (hl, wl)).astype(np.float32))
         rights.append(rng.uniform(-1, 1, (hr, wr)).astype(np.float32))
+    if big:
+        for hl, wl, hr, wr in [(150, 140, 130, 160), (170, 150, 140, 150), (160, 160, 160, 130)]:
+            lefts.append(rng.uniform(-1, 1, (hl, wl)).astype(np.float32))
+            rights.append(rng.uniform(-1, 1, (hr, wr)).astype(np.float32))
     return lefts, rights
 
 
-def _worker(rank, world, port, q):
+def _worker(rank, world, port, q, variant=None):
     import torch.distributed as dist
 
     from xcorr import shard
@@ -34,8 +40,8 @@ def _worker(rank, world, port, q):
     os.environ["MASTER_PORT"] = str(port)
     torch.cuda.set_device(0)
     dist.init_process_group("gloo", rank=rank, world_size=world)
-    lefts, rights = make_batch()
-    full = shard.correlate_pairs_sharded(lefts, rights, rank, world)
+    lefts, rights = make_batch(big=variant is not None)
+    full = shard.correlate_pairs_sharded(lefts, rights, rank, world, variant=variant)
     dist.barrier()
     dist.destroy_process_group()
     if rank == 0:
@@ -50,7 +56,10 @@ def free_port():
     return p
 
 
-def test_two_ranks_share_a_ragged_batch_on_the_gpu():
+@pytest.mark.parametrize("variant", [None, 8])
+def test_two_ranks_share_a_ragged_batch_on_the_gpu(variant):
+    """variant 8: tile shape 0, the pairs of at least 2^26 multiply-adds on the
+    split-BF16 path."""
     import torch.multiprocessing as mp
 
     from oracle import oracle
@@ -58,14 +67,14 @@ def test_two_ranks_share_a_ragged_batch_on_the_gpu():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = free_port()
-    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q, variant)) for r in range(2)]
     for p in procs:
         p.start()
     full = q.get(timeout=300)
     for p in procs:
         p.join(timeout=120)
         assert p.exitcode == 0
-    lefts, rights = make_batch()
+    lefts, rights = make_batch(big=variant is not None)
     refs = oracle.run_pairs(lefts, rights, threads=8)
     assert len(full) == len(refs)
     for k, (o, r) in enumerate(zip(full, refs)):
