@@ -200,10 +200,12 @@ xc_status tc_resources(RaggedPlanImpl* P) {
       ws = std::max(ws, tc_workspace_size(Geometry{d.Hl, d.Wl, d.Hr, d.Wr, d.Hl + d.Hr - 1, d.Wl + d.Wr - 1}, pm,
                                           false));
     }
+  // (what an earlier, failed attempt made is kept and reused)
   for (int k = 0; k < P->n_streams; ++k) {
-    XC_CUDA_TRY(cudaStreamCreateWithFlags(&P->tc_streams[k], cudaStreamNonBlocking));
-    XC_CUDA_TRY(cudaEventCreateWithFlags(&P->joins[k], cudaEventDisableTiming));
-    XC_CUDA_TRY(cudaMalloc(&P->tc_ws[k], std::max<size_t>(ws, 256)));
+    if (P->tc_streams[k] == nullptr)
+      XC_CUDA_TRY(cudaStreamCreateWithFlags(&P->tc_streams[k], cudaStreamNonBlocking));
+    if (P->joins[k] == nullptr) XC_CUDA_TRY(cudaEventCreateWithFlags(&P->joins[k], cudaEventDisableTiming));
+    if (P->tc_ws[k] == nullptr) XC_CUDA_TRY(cudaMalloc(&P->tc_ws[k], std::max<size_t>(ws, 256)));
   }
   P->tc_ws_bytes = std::max<size_t>(ws, 256);
   XC_CUDA_TRY(cudaEventCreateWithFlags(&P->fork, cudaEventDisableTiming));
