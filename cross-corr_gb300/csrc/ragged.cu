@@ -252,6 +252,10 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
   }
   v.n_tiles = (int)ht.size();
   v.tc_pairs = (int)tc_pairs.size();
+  if (v.tiles != nullptr) {  // left by an earlier, failed build of this variant
+    cudaFree(v.tiles);
+    v.tiles = nullptr;
+  }
   if (v.n_tiles > 0) {
     XC_CUDA_TRY(cudaMalloc(&v.tiles, sizeof(RaggedTile) * ht.size()));
     XC_CUDA_TRY(cudaMemcpy(v.tiles, ht.data(), sizeof(RaggedTile) * ht.size(), cudaMemcpyHostToDevice));
@@ -290,10 +294,10 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
   XC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   xc_status st = XC_OK;
   const bool forked = !tc_pairs.empty();
-  if (forked && cudaEventRecord(P->fork, s) != cudaSuccess) st = XC_ERR_CUDA;
+  if (forked && cudaEventRecord(P->fork, s) != cudaSuccess) st = fail(XC_ERR_CUDA, "ragged capture: fork failed");
   for (int k = 0; k < P->n_streams && forked; ++k)
     if (st == XC_OK && !per_stream[k].empty() && cudaStreamWaitEvent(P->tc_streams[k], P->fork, 0) != cudaSuccess)
-      st = XC_ERR_CUDA;
+      st = fail(XC_ERR_CUDA, "ragged capture: a side stream could not join");
   if (st == XC_OK && v.n_tiles > 0) {
     RaggedLaunch rl;
     rl.left = P->lpad;
@@ -323,7 +327,8 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
         repack_kernel<double><<<nb_r, 128, 0, s>>>((const double*)P->right, (double*)P->rpad, P->jobs + nl,
                                                    P->max_rows);
     }
-    if (cudaMemsetAsync(P->queue, 0, sizeof(unsigned int), s) != cudaSuccess) st = XC_ERR_CUDA;
+    if (cudaMemsetAsync(P->queue, 0, sizeof(unsigned int), s) != cudaSuccess)
+      st = fail(XC_ERR_CUDA, "ragged capture: queue reset failed");
     if (st == XC_OK) st = ragged_launch(P->dtype, shape, rl, s);
   }
   for (int k = 0; k < P->n_streams && forked; ++k) {
