@@ -166,3 +166,52 @@ def test_ragged_fp64_plans_keep_every_pair_on_the_plain_kernel():
     with pytest.raises(xcorr.XcError):
         plan.select(1)
     plan.close()
+
+
+_SWITCH_SCRIPT = """
+import json, sys
+sys.path[:0] = [sys.argv[1], sys.argv[1] + '/cross-corr_gb300']
+import numpy as np, torch, xcorr
+from oracle import oracle
+rng = np.random.default_rng(14)
+shapes = [(150, 140, 130, 160), (120, 110, 100, 130), (30, 40, 20, 10)]
+lefts = [rng.uniform(-1, 1, (a, b)).astype(np.float32) for a, b, _, _ in shapes]
+rights = [rng.uniform(-1, 1, (c, d)).astype(np.float32) for _, _, c, d in shapes]
+plan = xcorr.RaggedPlan(lefts, rights, [(i, i) for i in range(3)])
+n = plan.describe()["n_variants"]
+err = None
+if n > 2:
+    plan.select(n - 2)  # tile shape 0, the pairs of at least 2^26 multiply-adds on the split path
+    plan.out.fill_(float("nan"))
+    plan.execute()
+    torch.cuda.synchronize()
+    refs = oracle.run_pairs(lefts, rights, threads=8)
+    err = max(float(np.nanmax(np.abs(o - r)) / np.abs(r).max()) if not np.isnan(o).any() else 1.0
+              for o, r in zip(plan.outputs(), refs))
+print(json.dumps({"n_variants": n, "tc_pairs": plan.describe(n - 2 if n > 2 else 0)["tc_pairs"], "err": err}))
+plan.close()
+"""
+
+
+@pytest.mark.parametrize("env,variants", [({"XC_RAGGED_TC": "0"}, 2), ({"XC_RAGGED_TC_STREAMS": "1"}, 10)])
+def test_ragged_environment_switches(env, variants):
+    """XC_RAGGED_TC=0 leaves FP32 plans with the plain kernel only (the two
+    tile shapes); XC_RAGGED_TC_STREAMS=1 puts every routed call on one side
+    stream, with the same results.  The switches are read once per process,
+    so each case runs in a child process."""
+    import json
+    import subprocess
+    import sys
+
+    from conftest import ROOT
+
+    out = subprocess.run([sys.executable, "-c", _SWITCH_SCRIPT, ROOT], env={**os.environ, **env}, cwd=ROOT,
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    assert res["n_variants"] == variants
+    if variants > 2:
+        assert res["tc_pairs"] == 2
+        assert res["err"] <= 1e-5
+    else:
+        assert res["tc_pairs"] == 0
