@@ -34,6 +34,7 @@
 #include <string>
 #include <vector>
 
+#include "ragged_route.h"
 #include "xc_common.cuh"
 #include "xc_internal.h"
 
@@ -47,7 +48,6 @@ constexpr int kMaxTcStreams = 8;  // side streams of the split-BF16 route (XC_RA
 // (512-pair batch, 448 pairs routed: 33.3 ms with the lone-call rule, 31.1 /
 // 30.6 / 30.8 / 32.0 ms with items of 24 / 32 / 48 / 64 rows).
 constexpr int kTcItemRows = 32;
-constexpr int kRoutes = 5;     // route 0 (plain kernel only) and four multiply-add thresholds
 
 struct CopyJob {  // one matrix into its padded copy
   long long src, dst;
@@ -125,12 +125,8 @@ double tile_cost(const RaggedPairDev& p, int sy0, int sx0, const RaggedShape& sh
   return (double)std::max(0, y_hi - y_lo) * std::max(0, x_hi - x_lo);
 }
 
-// Smallest multiply-add count of the pairs a route sends to the split path:
-// 2^32, 2^30, 2^28, 2^26 for routes 1-4 (route 0: none).
-double route_min_mac(int route) { return route <= 0 ? 0.0 : std::ldexp(1.0, 34 - 2 * route); }
-
-bool in_route(const RaggedPlanImpl* P, size_t pair, int route) {
-  return route > 0 && P->tc_ok[pair] && P->pair_mac[pair] >= route_min_mac(route);
+bool pair_in_route(const RaggedPlanImpl* P, size_t pair, int route) {
+  return in_route(P->pair_mac[pair], P->tc_ok[pair] != 0, route);
 }
 
 RaggedPairDev pair_dev(const RaggedPlanImpl* P, size_t i) {
@@ -221,14 +217,11 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
   // the route, longest first
   std::vector<RaggedPairDev> hp(P->pairs.size());
   std::vector<std::pair<double, RaggedTile>> tiles;
-  std::vector<size_t> tc_pairs;
+  const std::vector<size_t> tc_pairs = route_pairs(P->pair_mac, P->tc_ok, route);
   for (size_t i = 0; i < P->pairs.size(); ++i) {
     const RaggedPairDev d = pair_dev(P, i);
     hp[i] = d;
-    if (in_route(P, i, route)) {
-      tc_pairs.push_back(i);
-      continue;
-    }
+    if (pair_in_route(P, i, route)) continue;
     const int Sy = d.Hl + d.Hr - 1, Sx = d.Wl + d.Wr - 1;
     const int rem = (d.Wr - 1) % sh.vec;
     const int origin = rem == 0 ? 0 : rem - sh.vec;
@@ -242,8 +235,6 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
       }
   }
   std::stable_sort(tiles.begin(), tiles.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
-  std::stable_sort(tc_pairs.begin(), tc_pairs.end(),
-                   [P](size_t a, size_t b) { return P->pair_mac[a] > P->pair_mac[b]; });
   std::vector<RaggedTile> ht(tiles.size());
   for (size_t i = 0; i < tiles.size(); ++i) ht[i] = tiles[i].second;
   if (P->dpairs == nullptr) {
@@ -270,18 +261,13 @@ xc_status build_variant(RaggedPlanImpl* P, int index) {
   }
 
   // the route's pairs: each to the side stream with the least work so far
-  // (a call costs its multiply-adds plus about 2^26 of fixed work)
   PairMap pm1;
   uint64_t n_out1 = 0;
   make_pair_map(XC_ONE_TO_ONE, 1, 1, &pm1, &n_out1);
-  std::vector<std::vector<size_t>> per_stream(P->n_streams);
+  const std::vector<std::vector<size_t>> per_stream = deal_route(tc_pairs, P->pair_mac, P->n_streams);
   if (!tc_pairs.empty()) {
     XC_TRY(tc_resources(P));
-    double load[kMaxTcStreams] = {0.0};
     for (size_t i : tc_pairs) {
-      const int k = (int)(std::min_element(load, load + P->n_streams) - load);
-      per_stream[k].push_back(i);
-      load[k] += P->pair_mac[i] + std::ldexp(1.0, 26);
       const RaggedPairDev& d = hp[i];
       XC_TRY(tc_prepare(Geometry{d.Hl, d.Wl, d.Hr, d.Wr, d.Hl + d.Hr - 1, d.Wl + d.Wr - 1}, pm1, false));
     }
@@ -435,7 +421,7 @@ xc_status ragged_plan_create(RaggedPlanImpl** out, xc_dtype dtype, const void* d
   P->rights.assign(rights, rights + n_right);
   P->pairs.assign(pairs, pairs + n_pairs);
   P->n_shapes = ragged_shape_count(dtype);
-  P->n_routes = dtype == XC_F32 && tc_routes_enabled() ? kRoutes : 1;
+  P->n_routes = dtype == XC_F32 && tc_routes_enabled() ? kRaggedRoutes : 1;
   P->n_streams = tc_stream_count();
   P->variants.resize((size_t)P->n_shapes * P->n_routes);
   P->maps_for_shape.assign(2 * (size_t)P->n_shapes, nullptr);
@@ -545,7 +531,7 @@ xc_status ragged_autotune(RaggedPlanImpl* P, cudaStream_t stream, int* chosen, d
   size_t prev = 0;
   for (int r = 1; r < P->n_routes && st == XC_OK; ++r) {
     size_t n = 0;
-    for (size_t i = 0; i < P->pairs.size(); ++i) n += in_route(P, i, r) ? 1 : 0;
+    for (size_t i = 0; i < P->pairs.size(); ++i) n += pair_in_route(P, i, r) ? 1 : 0;
     if (n == 0 || n == prev) continue;
     prev = n;
     st = time_variant(best_shape + P->n_shapes * r);
@@ -581,7 +567,7 @@ xc_status ragged_describe(RaggedPlanImpl* P, int variant, xc_ragged_variant* out
   out->n_variants = (int32_t)P->variants.size();
   out->tile_shape = variant % P->n_shapes;
   uint32_t n = 0;
-  for (size_t i = 0; i < P->pairs.size(); ++i) n += in_route(P, i, route) ? 1 : 0;
+  for (size_t i = 0; i < P->pairs.size(); ++i) n += pair_in_route(P, i, route) ? 1 : 0;
   out->tc_pairs = n;
   out->tc_min_macs = (uint64_t)route_min_mac(route);
   return XC_OK;
